@@ -1,0 +1,249 @@
+"""Generate golden vectors by running the reference itself (torchlinops 0.7.4).
+
+Run in a container that has the reference source:
+
+    python tests/golden/make_golden.py --ref /root/reference/src
+
+It imports the reference's functional API with a no-op ``jaxtyping`` stub
+(``tests/golden/_stubs``) and runs its pure-torch CPU path (``ungrid_torch``,
+``grid_torch``, ``_unfold_torch``, ``_fold_torch``, ``kaiser_bessel_torch``)
+on small seeded inputs, writing ``tests/golden/*.npz``. The fixtures are the
+parity pins for the oracle (``tests/test_oracle_golden.py``) and, on the GPU,
+for the CUDA kernels (``tests/test_interp_gpu.py``, ``tests/test_blocks_gpu.py``).
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import sys
+import time
+
+import numpy as np
+import torch
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+NUFFT_BETA = float(np.pi * (((4.0 / 1.25) * (1.25 - 0.5)) ** 2 - 0.8) ** 0.5)
+
+
+def _np(t: torch.Tensor) -> np.ndarray:
+    t = t.detach().cpu()
+    if t.is_complex():
+        return torch.view_as_real(t.contiguous()).numpy()
+    return t.numpy()
+
+
+def _rand(shape, is_complex, gen):
+    if is_complex:
+        re = torch.randn(shape, generator=gen)
+        im = torch.randn(shape, generator=gen)
+        return torch.complex(re, im)
+    return torch.randn(shape, generator=gen)
+
+
+INTERP_SPECS = {
+    # name: (batch N, grid_size, locs batch, width) -- shapes of the
+    # reference fixtures in _interp/tests/conftest.py
+    "small1d": ((2,), (10,), (20,), 4.0),
+    "small2d": ((2, 2), (10, 8), (9,), 4.0),
+    "tiny2d": ((2,), (2, 2), (1,), 2.0),
+    "small3d": ((1, 1), (10, 8, 9), (3, 5), 4.0),
+    "medium1d": ((2, 2), (24,), (6, 11), 4.0),
+    "medium2d": ((2, 2), (124, 125), (3, 19), 4.0),
+    "medium3d": ((1,), (33, 35, 37), (3, 19), 4.0),
+    "aniso3d": ((3,), (12, 9, 14), (40,), (4.0, 3.0, 5.5)),
+}
+
+KERNELS = [
+    ("kaiser_bessel", {"beta": 1.0}),
+    ("kaiser_bessel", {"beta": NUFFT_BETA}),
+    ("spline", {}),
+]
+
+
+def make_interp(F, out_dir):
+    cases = {}
+    seed = 0
+    for name, (N, gsz, lbs, width) in INTERP_SPECS.items():
+        small = not name.startswith("medium")
+        kerns = KERNELS if small else [KERNELS[1]]
+        dtypes = [False, True] if small else [True]
+        for kname, kparams in kerns:
+            for pad in ("circular", "zero"):
+                for cplx in dtypes:
+                    seed += 1
+                    gen = torch.Generator().manual_seed(seed)
+                    ndim = len(gsz)
+                    # points range past both edges so wrap / zero-pad paths are hit
+                    lo, hi = (-2.5, 2.5) if small else (0.0, 0.0)
+                    locs = torch.stack(
+                        [torch.rand(lbs, generator=gen) * (g + hi - lo) + lo for g in gsz], -1
+                    ).to(torch.float32)
+                    if small:
+                        # a few exact integer and half-integer coordinates
+                        flat = locs.reshape(-1, ndim)
+                        flat[0] = torch.tensor([float(g // 2) for g in gsz])
+                        if flat.shape[0] > 1:
+                            flat[1] = torch.tensor([float(g // 2) + 0.5 for g in gsz])
+                    img = _rand((*N, *gsz), cplx, gen)
+                    pts = _rand((*N, *lbs), cplx, gen)
+                    w = width if isinstance(width, float) else tuple(width)
+                    fwd = F.interpolate(img, locs, w, kernel=kname, norm=1, pad_mode=pad, kernel_params=dict(kparams))
+                    adj = F.interpolate_adjoint(
+                        pts, locs, gsz, w, kernel=kname, norm=1, pad_mode=pad, kernel_params=dict(kparams)
+                    )
+                    key = f"{name}-{kname}-{kparams.get('beta', 0):.5f}-{pad}-{'c' if cplx else 'r'}"
+                    meta = dict(
+                        spec=name,
+                        N=list(N),
+                        grid_size=list(gsz),
+                        locs_batch=list(lbs),
+                        width=list(width) if isinstance(width, tuple) else width,
+                        kernel=kname,
+                        beta=kparams.get("beta", 1.0),
+                        pad_mode=pad,
+                        complex=cplx,
+                        norm=1,
+                    )
+                    cases[key] = dict(
+                        meta=json.dumps(meta),
+                        locs=_np(locs),
+                        img=_np(img),
+                        pts=_np(pts),
+                        fwd=_np(fwd),
+                        adj=_np(adj),
+                    )
+    np.savez_compressed(os.path.join(out_dir, "interp_cases.npz"), **_flatten(cases))
+    return len(cases)
+
+
+def make_config1(F, out_dir):
+    """Plain 2D Interpolate forward+adjoint: grid 64x64 c64, 4096 pts, KB W=4, seed 0."""
+    gen = torch.Generator().manual_seed(0)
+    img = torch.complex(torch.randn(64, 64, generator=gen), torch.randn(64, 64, generator=gen))
+    locs = (torch.rand(4096, 2, generator=gen) * 64).to(torch.float32)
+    pts = torch.complex(torch.randn(4096, generator=gen), torch.randn(4096, generator=gen))
+    kp = dict(beta=NUFFT_BETA)
+    fwd = F.interpolate(img, locs, 4.0, kernel="kaiser_bessel", kernel_params=dict(kp))
+    adj = F.interpolate_adjoint(pts, locs, (64, 64), 4.0, kernel="kaiser_bessel", kernel_params=dict(kp))
+    np.savez_compressed(
+        os.path.join(out_dir, "config1_interp2d.npz"),
+        locs=_np(locs),
+        img=_np(img),
+        pts=_np(pts),
+        fwd=_np(fwd),
+        adj=_np(adj),
+        beta=np.float64(NUFFT_BETA),
+    )
+
+
+def make_edgecases(F, out_dir):
+    """Exact integer location (reference _interp/tests/test_edgecases.py:16-65)."""
+    out = {}
+    for cplx in (False, True):
+        dt = torch.complex64 if cplx else torch.float32
+        vals = torch.arange(1, 9).to(dt)
+        locs = torch.tensor([[4.0]])
+        fwd = F.ungrid(vals, locs, width=4.0, kernel="kaiser_bessel")
+        gv = torch.tensor([[1.0]]).to(dt)
+        adj = F.grid(gv, locs, (8,), width=4.0, kernel="kaiser_bessel")
+        tag = "c" if cplx else "r"
+        out[f"fwd_{tag}"] = _np(fwd)
+        out[f"adj_{tag}"] = _np(adj)
+    np.savez_compressed(os.path.join(out_dir, "edge_intloc.npz"), **out)
+
+
+def make_kernels(K, out_dir):
+    x = torch.linspace(-1.2, 1.2, 241)
+    out = {"x": _np(x)}
+    for beta in (1.0, 2.0, NUFFT_BETA, 12.0):
+        out[f"kb_{beta:.5f}"] = _np(K.kaiser_bessel_torch(x, beta=beta))
+    out["spline"] = _np(K.spline_torch(x))
+    np.savez_compressed(os.path.join(out_dir, "kernels.npz"), **out)
+
+
+BLOCK_SPECS = {
+    # reference fixtures of _unfold/tests/conftest.py (+ the 3D mask cross)
+    "small1d": ((1,), (15,), (3,), (1,), [0, 1, 0]),
+    "medium1d": ((2, 2), (33,), (7,), (2,), None),
+    "tiny2d": ((1,), (4, 4), (2, 2), (1, 1), None),
+    "small2d": ((1,), (15, 15), (3, 3), (1, 1), [[0, 1, 0], [1, 1, 1], [0, 1, 0]]),
+    "medium2d": ((2, 2), (33, 43), (7, 7), (2, 2), None),
+    "tiny3d": ((1,), (4, 4, 4), (2, 2, 2), (1, 1, 1), None),
+    "small3d": (
+        (1,),
+        (15, 15, 15),
+        (3, 3, 3),
+        (1, 1, 1),
+        [[[0, 0, 0], [0, 1, 0], [0, 0, 0]], [[0, 1, 0], [1, 1, 1], [0, 1, 0]], [[0, 0, 0], [0, 1, 0], [0, 0, 0]]],
+    ),
+    "medium3d": ((2,), (17, 21, 13), (7, 7, 5), (2, 2, 2), None),
+    "overlap3d": ((2,), (16, 16, 16), (8, 8, 8), (4, 4, 4), None),
+}
+
+
+def make_blocks(F, out_dir):
+    cases = {}
+    seed = 1000
+    for name, (N, shape, blk, st, mask) in BLOCK_SPECS.items():
+        dts = (torch.float32, torch.float64, torch.complex64)
+        if name.startswith(("medium", "overlap")):
+            dts = (torch.float32, torch.complex64)
+        for dt in dts:
+            seed += 1
+            gen = torch.Generator().manual_seed(seed)
+            nb = F.get_nblocks(shape, blk, st)
+            cplx = dt.is_complex
+            x = _rand((*N, *shape), cplx, gen)
+            y = _rand((*N, *nb, *blk), cplx, gen)
+            if not cplx:
+                x, y = x.to(dt), y.to(dt)
+            ux = F.array_to_blocks(x, blk, st)
+            fy = F.blocks_to_array(y, shape, blk, st)
+            rec = dict(x=_np(x), y=_np(y), unfold=_np(ux), fold=_np(fy))
+            if mask is not None:
+                m = torch.tensor(mask, dtype=torch.bool)
+                ym = y[..., m].contiguous()
+                rec["mask"] = m.numpy()
+                rec["unfold_masked"] = _np(F.array_to_blocks(x, blk, st, m))
+                rec["ym"] = _np(ym)
+                rec["fold_masked"] = _np(F.blocks_to_array(ym, shape, blk, st, m))
+            meta = dict(spec=name, N=list(N), shape=list(shape), block=list(blk), stride=list(st), dtype=str(dt), nblocks=list(nb))
+            rec["meta"] = json.dumps(meta)
+            cases[f"{name}-{str(dt).split('.')[-1]}"] = rec
+    np.savez_compressed(os.path.join(out_dir, "blocks_cases.npz"), **_flatten(cases))
+    return len(cases)
+
+
+def _flatten(cases):
+    flat = {}
+    for k, rec in cases.items():
+        for f, v in rec.items():
+            flat[f"{k}|{f}"] = np.asarray(v)
+    return flat
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference/src")
+    ap.add_argument("--out", default=HERE)
+    args = ap.parse_args()
+    sys.path.insert(0, os.path.join(HERE, "_stubs"))
+    sys.path.insert(0, args.ref)
+    torch.set_num_threads(os.cpu_count() or 1)
+    import torchlinops.functional as F
+    from torchlinops.functional._interp import kernels as K
+
+    t0 = time.time()
+    make_kernels(K, args.out)
+    make_edgecases(F, args.out)
+    make_config1(F, args.out)
+    n_i = make_interp(F, args.out)
+    n_b = make_blocks(F, args.out)
+    print(f"wrote {n_i} interp cases, {n_b} block cases in {time.time() - t0:.1f}s")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,62 @@
+// Shared helpers of the tlgb CUDA library (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "tlgb.h"
+
+namespace tlgb {
+
+// Message of the last failing call on this host thread (see tlgb_last_error).
+void set_error(const std::string& msg);
+
+#define TLGB_FAIL(code, msg)      \
+  do {                            \
+    ::tlgb::set_error(msg);       \
+    return (code);                \
+  } while (0)
+
+#define TLGB_CUDA(call)                                                              \
+  do {                                                                               \
+    cudaError_t e_ = (call);                                                         \
+    if (e_ != cudaSuccess) {                                                         \
+      ::tlgb::set_error(std::string(#call) + ": " + cudaGetErrorString(e_));          \
+      return TLGB_ERR_CUDA;                                                          \
+    }                                                                                \
+  } while (0)
+
+#define TLGB_CHECK_LAUNCH()                                                          \
+  do {                                                                               \
+    cudaError_t e_ = cudaGetLastError();                                             \
+    if (e_ != cudaSuccess) {                                                         \
+      ::tlgb::set_error(std::string("kernel launch: ") + cudaGetErrorString(e_));     \
+      return TLGB_ERR_CUDA;                                                          \
+    }                                                                                \
+  } while (0)
+
+#define TLGB_TRY(expr)          \
+  do {                          \
+    int s_ = (expr);            \
+    if (s_ != TLGB_OK) return s_; \
+  } while (0)
+
+inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Exclusive prefix sum of n uint32 values (in may alias out) with one CTA;
+// used only while building plans (one-time work), deterministic.
+int exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* total_dev,
+                       cudaStream_t s);
+
+// Stable LSD radix sort of (key, val) pairs by the low `bits` bits of key.
+// keys/vals are sorted in place; keys_tmp/vals_tmp are ping-pong buffers of
+// the same length; counts_tmp needs radix_counts_len(n) uint32 entries.
+int64_t radix_counts_len(int64_t n);
+int radix_sort_pairs(uint32_t* keys, int32_t* vals, uint32_t* keys_tmp, int32_t* vals_tmp,
+                     uint32_t* counts_tmp, int64_t n, int bits, cudaStream_t s);
+
+}  // namespace tlgb
