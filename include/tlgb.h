@@ -1,0 +1,163 @@
+/*
+ * tlgb -- GB300 (sm_103a) kernels for the torchlinops interpolation and block
+ * hot path, behind a plain C ABI (pointers, sizes, a CUDA stream; no torch
+ * types). Every entry point returns TLGB_OK (0) or an error code and never
+ * throws; tlgb_last_error() gives the message of the last failing call made
+ * on the calling host thread. All device pointers are raw CUDA device memory;
+ * every launch goes on the given stream and no call synchronises the device,
+ * except tlgb_interp_plan_build (it reads the bin histogram back once).
+ *
+ * Reference interfaces each entry replaces (paths in the torchlinops source):
+ *   tlgb_interp_forward    -> ungrid / _ungrid, functional/_interp/ungrid.py:37,70
+ *   tlgb_interp_adjoint    -> grid / _grid,     functional/_interp/grid.py:37,75
+ *   tlgb_interp_grad_locs  -> (new) trajectory gradient; the reference's
+ *                             InterpolateFn.backward returns None for locs,
+ *                             functional/_interp/interp.py:46-70
+ *   tlgb_interp_plan_*     -> (new) point binning; the reference launches one
+ *                             Triton program per ~npts/65535 points instead,
+ *                             functional/_interp/ungrid.py:135-160
+ *   tlgb_unfold            -> unfold / _unfold, functional/_unfold/unfold.py:31,72
+ *   tlgb_fold              -> fold / _fold,     functional/_unfold/fold.py:32,66
+ */
+#ifndef TLGB_H_
+#define TLGB_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* A cudaStream_t; NULL is the legacy default stream. */
+typedef void* tlgb_stream_t;
+
+enum {
+  TLGB_OK = 0,
+  TLGB_ERR_INVALID = 1,     /* bad shape, size, pointer, alignment or argument */
+  TLGB_ERR_UNSUPPORTED = 2, /* valid input outside what the kernels implement   */
+  TLGB_ERR_CUDA = 3,        /* a CUDA runtime call or launch failed             */
+  TLGB_ERR_WORKSPACE = 4,   /* caller-provided workspace too small              */
+  TLGB_ERR_DEVICE = 5       /* a kernel reported an error through its status word */
+};
+
+const char* tlgb_last_error(void);
+int tlgb_version(void);
+
+/* ------------------------------------------------------------------------ */
+/* Interpolation: Kaiser-Bessel / spline ungridding and gridding, 1D-3D.      */
+/* ------------------------------------------------------------------------ */
+
+enum { TLGB_KERNEL_KAISER_BESSEL = 0, TLGB_KERNEL_SPLINE = 1 };
+enum { TLGB_PAD_CIRCULAR = 0, TLGB_PAD_ZERO = 1 };
+
+/* Problem description shared by every interpolation call.
+ * Layouts (C order): grid values [nbatch, grid_size[0..ndim-1]], point values
+ * [nbatch, npts], locs [npts, ndim] float32 in grid units ('ij' order).
+ * is_complex: values are complex64 stored as interleaved (re, im) float32. */
+typedef struct tlgb_interp_desc {
+  int32_t ndim;         /* 1, 2 or 3 */
+  int32_t kernel;       /* TLGB_KERNEL_* */
+  int32_t norm;         /* 1: product of 1D weights; 2: radial weight */
+  int32_t pad_mode;     /* TLGB_PAD_* */
+  int32_t is_complex;
+  int32_t reserved;
+  int64_t grid_size[3];
+  float width[3];       /* kernel width per dimension, grid units */
+  float beta;           /* Kaiser-Bessel shape parameter */
+  int64_t nbatch;
+  int64_t npts;
+} tlgb_interp_desc;
+
+/* Host-side summary of a plan, filled by tlgb_interp_plan_build and passed
+ * back unchanged to the calls that use the plan. */
+typedef struct tlgb_interp_plan_info {
+  int64_t n_entries;      /* (point, tile) pairs, home pairs first per tile */
+  int64_t n_tiles;
+  int32_t tile[3];        /* tile edge per internal dim */
+  int32_t n_tile[3];      /* tiles per internal dim */
+  int64_t n_fwd_items;    /* work items of tlgb_interp_forward / grad_locs */
+  int64_t n_adj_items;    /* work items of tlgb_interp_adjoint */
+  int64_t n_partials;     /* partial tiles of split (dense) output tiles */
+  int64_t n_split_tiles;  /* output tiles summed from partials */
+  int64_t chunk;          /* max entries per work item */
+  int64_t off_entries;    /* byte offsets of the plan sections */
+  int64_t off_fwd_items;
+  int64_t off_adj_items;
+  int64_t off_split;
+  int64_t plan_bytes;
+  int64_t reserved[4];
+} tlgb_interp_plan_info;
+
+/* Bytes of device memory needed by a plan for this description (worst case)
+ * and of temporary device memory needed only while it is built. */
+int tlgb_interp_plan_size(const tlgb_interp_desc* d, size_t* plan_bytes, size_t* tmp_bytes);
+
+/* Bin the points: sort (point, tile) pairs by output tile (stable, so points
+ * keep their original order inside a tile) and cut the work into items of at
+ * most `chunk` pairs. Synchronises `stream` once to size the work lists. */
+int tlgb_interp_plan_build(const tlgb_interp_desc* d, const float* locs, void* plan, size_t plan_bytes,
+                           void* tmp, size_t tmp_bytes, tlgb_interp_plan_info* info, tlgb_stream_t stream);
+
+/* Scratch bytes tlgb_interp_adjoint needs for the partial tiles of this plan. */
+int tlgb_interp_adjoint_scratch_size(const tlgb_interp_desc* d, const tlgb_interp_plan_info* info,
+                                     size_t* bytes);
+
+/* out[b, p] = sum over taps of w(p, tap) * grid[b, tap]         (ungrid) */
+int tlgb_interp_forward(const tlgb_interp_desc* d, const tlgb_interp_plan_info* info, const void* plan,
+                        const float* locs, const void* grid, void* out, tlgb_stream_t stream);
+
+/* grid[b, v] = sum over points p with v in their window of w(p, v) * vals[b, p]
+ * (gridding). Every element of `grid` is written (no accumulation into the
+ * caller's contents); the summation order is fixed, so results are
+ * bit-identical run to run; no global atomics. */
+int tlgb_interp_adjoint(const tlgb_interp_desc* d, const tlgb_interp_plan_info* info, const void* plan,
+                        const float* locs, const void* vals, void* grid, void* scratch, size_t scratch_bytes,
+                        tlgb_stream_t stream);
+
+/* grad_locs[p, e] = sum_b Re( conj(a[b, p]) * sum_taps dw(p, tap)/dx_e * grid[b, tap] )
+ * -- the gradient w.r.t. the trajectory of sum Re(conj(a) * ungrid(grid)),
+ * and (with grid := the output cotangent, a := the point values) of the
+ * gridding operator. Written, not accumulated. */
+int tlgb_interp_grad_locs(const tlgb_interp_desc* d, const tlgb_interp_plan_info* info, const void* plan,
+                          const float* locs, const void* grid, const void* a, float* grad_locs,
+                          tlgb_stream_t stream);
+
+/* ------------------------------------------------------------------------ */
+/* ArrayToBlocks / BlocksToArray (unfold / fold), 1D-3D.                      */
+/* ------------------------------------------------------------------------ */
+
+/* Element types of the block ops. Complex types are pairs of the real type. */
+enum { TLGB_F32 = 0, TLGB_F64 = 1, TLGB_C64 = 2, TLGB_C128 = 3 };
+
+/* array [nbatch, im_size...]  <->  blocks [nbatch, nblocks..., block...]
+ * or, with a mask, blocks [nbatch, nblocks..., nnz] where mask_idx[j] (int32,
+ * device) is the row-major offset inside one block of the j-th kept element
+ * (ascending) and mask_inv[k] (int32, device, prod(block) entries) is the
+ * index j of block offset k, or -1 where the mask is false. Both NULL means
+ * no mask. nblocks[e] = (im_size[e]-block[e])/stride[e]+1. */
+typedef struct tlgb_blocks_desc {
+  int32_t ndim;
+  int32_t dtype;       /* TLGB_F32 ... TLGB_C128 */
+  int64_t nbatch;
+  int64_t im_size[3];
+  int64_t block[3];
+  int64_t stride[3];
+  int64_t nnz;         /* kept elements per block (mask) or prod(block) */
+  const int32_t* mask_idx;
+  const int32_t* mask_inv;
+} tlgb_blocks_desc;
+
+/* blocks = unfold(array): a copy, bit-exact. */
+int tlgb_unfold(const tlgb_blocks_desc* d, const void* array, void* blocks, tlgb_stream_t stream);
+
+/* array = fold(blocks): each element is the sum of its (at most
+ * prod(ceil(block/stride))) block entries in ascending block order, starting
+ * from zero -- deterministic; every element of `array` is written. */
+int tlgb_fold(const tlgb_blocks_desc* d, const void* blocks, void* array, tlgb_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TLGB_H_ */

@@ -1,0 +1,90 @@
+"""C-ABI library checks that need no GPU: it loads, exports every symbol that
+include/tlgb.h declares, and validates descriptors on the host."""
+
+import ctypes
+import os
+import re
+
+import pytest
+import torch
+
+from conftest import ROOT
+from torchlinops_gb300 import _ext
+
+
+def _header_symbols():
+    txt = open(os.path.join(ROOT, "include", "tlgb.h")).read()
+    return sorted(set(re.findall(r"\b(tlgb_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_library_exports_every_declared_symbol():
+    L = _ext.lib()
+    declared = _header_symbols()
+    assert declared, "no declarations parsed"
+    for name in declared:
+        assert hasattr(L, name), f"{name} declared in include/tlgb.h but not exported"
+    assert set(declared) == set(_ext.exported_symbols())
+    assert L.tlgb_version() >= 100
+
+
+def _desc(**kw):
+    d = _ext.InterpDesc()
+    d.ndim = kw.get("ndim", 3)
+    d.kernel = kw.get("kernel", 0)
+    d.norm = kw.get("norm", 1)
+    d.pad_mode = kw.get("pad", 0)
+    for i in range(3):
+        d.grid_size[i] = kw.get("n", 64)
+        d.width[i] = kw.get("width", 4.0)
+    d.beta = 1.0
+    d.npts = kw.get("npts", 1000)
+    d.nbatch = kw.get("nbatch", 1)
+    return d
+
+
+def _size(d):
+    pb, tb = ctypes.c_size_t(), ctypes.c_size_t()
+    st = _ext.lib().tlgb_interp_plan_size(ctypes.byref(d), ctypes.byref(pb), ctypes.byref(tb))
+    return st, pb.value, tb.value
+
+
+def test_plan_size_and_host_validation():
+    st, pb, tb = _size(_desc())
+    assert st == 0 and pb > 1000 * 8 * 4 and tb > 0
+    assert _size(_desc(ndim=4))[0] == _ext.TLGB_ERR_INVALID
+    assert _size(_desc(kernel=7))[0] == _ext.TLGB_ERR_INVALID
+    assert _size(_desc(norm=3))[0] == _ext.TLGB_ERR_INVALID
+    assert _size(_desc(width=-1.0))[0] == _ext.TLGB_ERR_INVALID
+    st = _size(_desc(width=9.0))[0]  # 3D width above the supported maximum
+    assert st == _ext.TLGB_ERR_UNSUPPORTED
+    assert b"width" in _ext.lib().tlgb_last_error()
+    assert _size(_desc(ndim=2, width=9.0))[0] == 0
+
+
+def test_blocks_host_validation():
+    d = _ext.BlocksDesc()
+    d.ndim = 3
+    d.dtype = 2
+    d.nbatch = 1
+    for i in range(3):
+        d.im_size[i] = 4
+        d.block[i] = 8  # block larger than the array
+        d.stride[i] = 1
+    d.nnz = 512
+    st = _ext.lib().tlgb_unfold(ctypes.byref(d), ctypes.c_void_p(16), ctypes.c_void_p(16), None)
+    assert st == _ext.TLGB_ERR_INVALID
+    d.dtype = 9
+    assert _ext.lib().tlgb_fold(ctypes.byref(d), ctypes.c_void_p(16), ctypes.c_void_p(16), None) != 0
+
+
+def test_product_path_has_no_cpu_fallback():
+    import torchlinops_gb300 as T
+
+    x = torch.randn(8, 8, dtype=torch.complex64)
+    locs = torch.rand(10, 2) * 8
+    with pytest.raises(RuntimeError, match="CUDA"):
+        T.interpolate(x, locs, 4.0)
+    with pytest.raises(RuntimeError, match="CUDA"):
+        T.unfold(x, (2, 2), (1, 1))
+    with pytest.raises(ValueError):
+        T.interpolate(x, locs, 4.0, kernel="gaussian")

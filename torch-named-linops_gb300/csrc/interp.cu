@@ -1,0 +1,1095 @@
+// Kaiser-Bessel / spline interpolation (ungrid), gridding (adjoint) and the
+// trajectory gradient, 1D-3D, for sm_103a.
+//
+// Replaces the reference's Triton kernels _ungrid{1,2,3}d (functional/_interp/
+// ungrid.py:162-503) and _grid{1,2,3}d (grid.py:169-513); the arithmetic of a
+// tap follows the reference's pure-torch path (ungrid_torch ungrid.py:624-684,
+// grid_torch grid.py:571-639, weights_torch kernels.py:108-147,
+// kaiser_bessel_torch kernels.py:28-89) operation for operation in float32.
+//
+// Design (GB300 first, not a translation of the Triton programs):
+//  * Plan (once per trajectory): every point is paired with each output tile
+//    its valid taps touch; the pairs are sorted by tile with a stable LSD
+//    radix sort, "home" pairs (the tile holding the point's first valid tap)
+//    first. Work items are chunks of at most `chunk` pairs of one tile, so
+//    dense k-space centres are spread over many CTAs.
+//  * Forward (gather): a CTA stages its tile plus the kernel halo for a group
+//    of up to 8 batch entries in shared memory ([x][y][z][batch] order, batch
+//    fastest) and each warp interpolates one home point at a time; lanes are
+//    (tap along the last dim, batch entry) so one warp load reads 4 taps x 8
+//    entries = 256 contiguous bytes, conflict-free.
+//  * Adjoint (scatter, deterministic, no global atomics): output-stationary.
+//    A CTA owns one output tile in shared memory and visits every point whose
+//    window touches it, in plan order. Warp w owns the tile planes with
+//    (outer index) % 8 == w, so every shared-memory cell is updated by one
+//    fixed warp in one fixed order: results are bit-identical run to run.
+//    Each tile is written to HBM exactly once. Tiles denser than `chunk`
+//    pairs are split: each part writes a partial tile to scratch and a second
+//    kernel sums the parts in order.
+//  * Kernel values are evaluated directly with the reference's A&S formula
+//    (expf/sqrtf, IEEE division), not from a lookup table: a table would add
+//    an interpolation error on top of the 1e-5 budget, and the 3 x (W+1)
+//    evaluations per point visit are shared by every batch entry of the visit.
+
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "common.cuh"
+
+namespace tlgb {
+namespace {
+
+constexpr int NTMAX = 16;  // taps per dimension supported (width < 15)
+constexpr int NWARP = 8;   // warps per CTA
+constexpr int NTHR = 32 * NWARP;
+constexpr int PB = 64;     // points per adjoint batch
+constexpr int CGMAX = 8;   // batch entries per coil group
+
+struct Geo {
+  int ndim;
+  int N[3];   // internal dims (x, y, z); leading inactive dims have N = 1
+  int T[3];   // tile edge
+  int nt[3];  // tiles per dim
+  int NT[3];  // taps per dim (inactive: 1)
+  float r[3]; // kernel radius W/2 per dim
+  int act[3];
+  int kernel, norm, pad, cplx;
+  float beta;
+  long long npts, nbatch;
+  int wrap_safe;  // every active N >= NT: a window never overlaps itself
+};
+
+// ---------------------------------------------------------------- kernels math
+
+// A&S 9.8.1 / 9.8.2 coefficients (the reference's kernels.py:65-88)
+__device__ __forceinline__ float kb_value(float x, float beta) {
+  const float z = beta * __fsqrt_rn(__fsub_rn(1.0f, __fmul_rn(x, x)));
+  const float t = __fdiv_rn(z, 3.75f);
+  const float t2 = t * t;
+  if (z < 3.75f) {
+    const float t4 = t2 * t2, t6 = t4 * t2, t8 = t4 * t4, t10 = t6 * t4, t12 = t6 * t6;
+    return 1.0f + 3.5156229f * t2 + 3.0899424f * t4 + 1.2067492f * t6 + 0.2659732f * t8 + 0.0360768f * t10 +
+           0.0045813f * t12;
+  }
+  const float t3 = t2 * t, t4 = t2 * t2, t5 = t3 * t2, t6 = t4 * t2, t7 = t5 * t2, t8 = t4 * t4;
+  const float poly = 0.39894228f + __fdiv_rn(0.01328592f, t) + __fdiv_rn(0.00225319f, t2) -
+                     __fdiv_rn(0.00157565f, t3) + __fdiv_rn(0.00916281f, t4) - __fdiv_rn(0.02057706f, t5) +
+                     __fdiv_rn(0.02635537f, t6) - __fdiv_rn(0.01647633f, t7) + __fdiv_rn(0.00392377f, t8);
+  return __fdiv_rn(expf(z), __fsqrt_rn(z)) * poly;
+}
+
+// d KB(x) / dx of the same A&S expressions (x signed, |x| <= 1)
+__device__ __forceinline__ float kb_deriv(float x, float beta) {
+  const float z = beta * __fsqrt_rn(__fsub_rn(1.0f, __fmul_rn(x, x)));
+  const float b2 = beta * beta;
+  if (z < 3.75f) {
+    const float u = (z / 3.75f) * (z / 3.75f);
+    // P(u) = 1 + a1 u + ... + a6 u^6 ; P'(u)
+    const float dp = 3.5156229f + u * (2.f * 3.0899424f + u * (3.f * 1.2067492f + u * (4.f * 0.2659732f +
+                     u * (5.f * 0.0360768f + u * (6.f * 0.0045813f)))));
+    return -2.0f * b2 * x * dp / (3.75f * 3.75f);
+  }
+  const float v = 3.75f / z;
+  const float q = 0.39894228f + v * (0.01328592f + v * (0.00225319f + v * (-0.00157565f + v * (0.00916281f +
+                  v * (-0.02057706f + v * (0.02635537f + v * (-0.01647633f + v * 0.00392377f)))))));
+  const float dq = 0.01328592f + v * (2.f * 0.00225319f + v * (3.f * -0.00157565f + v * (4.f * 0.00916281f +
+                   v * (5.f * -0.02057706f + v * (6.f * 0.02635537f + v * (7.f * -0.01647633f +
+                   v * (8.f * 0.00392377f)))))));
+  const float e = expf(z) / sqrtf(z);
+  const float dI = e * (q * (1.0f - 0.5f / z) - dq * 3.75f / (z * z));
+  return dI * (-b2 * x / z);
+}
+
+__device__ __forceinline__ float kern_value(int kernel, float ax, float beta) {
+  return kernel == TLGB_KERNEL_KAISER_BESSEL ? kb_value(ax, beta) : fmaxf(1.0f - ax, 0.0f);
+}
+
+__device__ __forceinline__ float kern_deriv(int kernel, float d, float beta) {
+  if (kernel == TLGB_KERNEL_KAISER_BESSEL) return kb_deriv(d, beta);
+  return (fabsf(d) < 1.0f) ? (d > 0.f ? -1.0f : (d < 0.f ? 1.0f : 0.0f)) : 0.0f;
+}
+
+__device__ __forceinline__ bool coord_ok(float x) { return isfinite(x) && fabsf(x) < 16777216.0f; }
+
+// One tap of one dimension: the reference's dlocs = (locs - grid_locs) / radius
+// and its validity (kernels.py:126-146).
+struct Tap {
+  float d;     // signed normalised offset
+  bool valid;
+};
+
+__device__ __forceinline__ Tap tap_eval(const Geo& g, int e, float x, int lower, int k) {
+  Tap t;
+  const float gk = (float)(lower + k);
+  t.d = __fdiv_rn(__fsub_rn(x, gk), g.r[e]);
+  const float ad = fabsf(t.d);
+  bool v = ad <= g.r[e];
+  if (g.kernel == TLGB_KERNEL_KAISER_BESSEL) v = v && (ad <= 1.0f);
+  if (g.pad == TLGB_PAD_ZERO) v = v && (lower + k >= 0) && (lower + k < g.N[e]);
+  t.valid = v;
+  return t;
+}
+
+__device__ __forceinline__ int lower_of(const Geo& g, int e, float x) {
+  return (int)ceilf(__fsub_rn(x, g.r[e]));
+}
+
+__device__ __forceinline__ int wrapi(int v, int n) {
+  if (v >= 0 && v < n) return v;
+  int m = v % n;
+  return m < 0 ? m + n : m;
+}
+
+__device__ __forceinline__ float load_coord(const Geo& g, const float* locs, long long p, int e) {
+  return __ldg(locs + p * g.ndim + (e - (3 - g.ndim)));
+}
+
+// Valid tap range [s, s+n) of one dim for one point (sequential; used by the plan).
+__device__ __forceinline__ bool axis_range(const Geo& g, const float* locs, long long p, int e, int& start, int& n) {
+  if (!g.act[e]) {
+    start = 0;
+    n = 1;
+    return true;
+  }
+  const float x = load_coord(g, locs, p, e);
+  if (!coord_ok(x)) return false;
+  const int lower = lower_of(g, e, x);
+  int s = -1;
+  n = 0;
+  for (int k = 0; k < g.NT[e]; ++k) {
+    if (tap_eval(g, e, x, lower, k).valid) {
+      if (s < 0) s = k;
+      ++n;
+    }
+  }
+  if (n == 0) return false;
+  start = lower + s;
+  if (g.pad == TLGB_PAD_CIRCULAR) start = wrapi(start, g.N[e]);
+  return true;
+}
+
+// --------------------------------------------------------------------- plan
+
+// Distinct tiles touched along one dim by taps start .. start+n-1 (wrapped);
+// the first is the home tile. At most 3 (a window crossing a ragged last tile
+// and the wrap), see max_tiles_per_dim on the host.
+__device__ __forceinline__ int axis_tiles(const Geo& g, int e, int start, int n, int* tl) {
+  int cnt = 0;
+  for (int k = 0; k < n; ++k) {
+    int v = start + k;
+    if (g.pad == TLGB_PAD_CIRCULAR) v = wrapi(v, g.N[e]);
+    const int t = v / g.T[e];
+    bool seen = false;
+    for (int i = 0; i < cnt; ++i) seen = seen || (tl[i] == t);
+    if (!seen && cnt < 3) tl[cnt++] = t;
+  }
+  return cnt;
+}
+
+__global__ void plan_count_kernel(Geo g, const float* __restrict__ locs, uint32_t* __restrict__ cnt) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= g.npts) return;
+  uint32_t c = 1;
+  for (int e = 0; e < 3; ++e) {
+    int st, n, tl[3];
+    if (!axis_range(g, locs, p, e, st, n)) {
+      c = 0;
+      break;
+    }
+    c *= (uint32_t)axis_tiles(g, e, st, n, tl);
+  }
+  cnt[p] = c;
+}
+
+__global__ void plan_emit_kernel(Geo g, const float* __restrict__ locs, const uint32_t* __restrict__ off,
+                                 uint32_t* __restrict__ keys, int32_t* __restrict__ vals) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= g.npts) return;
+  int tl[3][3], nc[3];
+  for (int e = 0; e < 3; ++e) {
+    int st, n;
+    if (!axis_range(g, locs, p, e, st, n)) return;
+    nc[e] = axis_tiles(g, e, st, n, tl[e]);
+  }
+  uint32_t o = off[p];
+  for (int i = 0; i < nc[0]; ++i)
+    for (int j = 0; j < nc[1]; ++j)
+      for (int k = 0; k < nc[2]; ++k) {
+        const uint32_t tile = ((uint32_t)tl[0][i] * g.nt[1] + tl[1][j]) * g.nt[2] + tl[2][k];
+        const bool home = (i == 0 && j == 0 && k == 0);
+        keys[o] = tile * 2u + (home ? 0u : 1u);
+        vals[o] = (int32_t)p;
+        ++o;
+      }
+}
+
+__global__ void key_hist_kernel(const uint32_t* __restrict__ keys, long long n, uint32_t* __restrict__ hist) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) atomicAdd(hist + keys[i], 1u);
+}
+
+// ------------------------------------------------------------- value types
+
+template <typename V>
+struct VT;
+template <>
+struct VT<float> {
+  __device__ static float zero() { return 0.f; }
+  __device__ static void fma(float& a, float w, float v) { a = fmaf(w, v, a); }
+  __device__ static void add(float& a, float b) { a += b; }
+  __device__ static float shfl_xor(float v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+  __device__ static float re_dot(float a, float b) { return a * b; }
+};
+template <>
+struct VT<float2> {
+  __device__ static float2 zero() { return make_float2(0.f, 0.f); }
+  __device__ static void fma(float2& a, float w, float2 v) {
+    a.x = fmaf(w, v.x, a.x);
+    a.y = fmaf(w, v.y, a.y);
+  }
+  __device__ static void add(float2& a, float2 b) {
+    a.x += b.x;
+    a.y += b.y;
+  }
+  __device__ static float2 shfl_xor(float2 v, int m) {
+    return make_float2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
+  }
+  // Re(conj(a) * b)
+  __device__ static float re_dot(float2 a, float2 b) { return a.x * b.x + a.y * b.y; }
+};
+
+// Per point: start coordinate and valid-tap count per internal dim, and the
+// per-tap value used by the inner loops: the 1D weight (norm 1) or |d|
+// (norm 2). The DERIV variant adds d weight / d x (norm 1) or signed d (norm 2).
+template <bool DERIV>
+struct PTaps {
+  int start[3];
+  int n[3];
+  float w[3][NTMAX];
+  float dw[DERIV ? 3 : 1][DERIV ? NTMAX : 1];
+};
+using PointTaps = PTaps<false>;
+
+// Warp-cooperative tap evaluation of point p into `pt` (shared memory).
+// Returns false (warp-uniform) if the point has no valid tap.
+template <int NORM, bool DERIV>
+__device__ __forceinline__ bool warp_point_taps(const Geo& g, const float* locs, long long p, PTaps<DERIV>& pt,
+                                                int lane) {
+  bool ok = true;
+  for (int e = 0; e < 3; ++e) {
+    if (!g.act[e]) {
+      if (lane == 0) {
+        pt.start[e] = 0;
+        pt.n[e] = 1;
+        pt.w[e][0] = NORM == 1 ? 1.f : 0.f;  // weight 1, or |d| = 0 for the radial norm
+        if (DERIV) pt.dw[e][0] = 0.f;
+      }
+      continue;
+    }
+    const float x = load_coord(g, locs, p, e);
+    if (!coord_ok(x)) {
+      ok = false;
+      break;
+    }
+    const int lower = lower_of(g, e, x);
+    const int k = lane;
+    Tap t;
+    t.valid = false;
+    t.d = 0.f;
+    if (k < g.NT[e]) t = tap_eval(g, e, x, lower, k);
+    const unsigned m = __ballot_sync(0xffffffffu, t.valid);
+    if (m == 0) {
+      ok = false;
+      break;
+    }
+    const int s = __ffs(m) - 1;
+    const int n = __popc(m);
+    if (t.valid) {
+      const int j = k - s;
+      const float ad = fabsf(t.d);
+      if (NORM == 1) {
+        pt.w[e][j] = kern_value(g.kernel, ad, g.beta);
+        if (DERIV) pt.dw[e][j] = kern_deriv(g.kernel, t.d, g.beta) / g.r[e];
+      } else {
+        pt.w[e][j] = ad;
+        if (DERIV) pt.dw[e][j] = t.d;
+      }
+    }
+    if (lane == 0) {
+      int st = lower + s;
+      if (g.pad == TLGB_PAD_CIRCULAR) st = wrapi(st, g.N[e]);
+      pt.start[e] = st;
+      pt.n[e] = n;
+    }
+  }
+  __syncwarp();
+  return ok;
+}
+
+// norm-2 weight of one tap combination (radial), 0 outside the unit ball
+__device__ __forceinline__ float radial_w(const Geo& g, float a0, float a1, float a2) {
+  const float rho = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(a0, a0), __fmul_rn(a1, a1)), __fmul_rn(a2, a2)));
+  if (rho > 1.0f) return 0.f;
+  return kern_value(g.kernel, rho, g.beta);
+}
+
+__device__ __forceinline__ int lg2i(int v) { return 31 - __clz(v); }
+
+// ------------------------------------------------------------------ forward
+
+template <typename V, int NORM>
+__global__ void __launch_bounds__(NTHR, 2) interp_fwd_kernel(Geo g, const int4* __restrict__ items,
+                                                             const int32_t* __restrict__ entries,
+                                                             const float* __restrict__ locs,
+                                                             const V* __restrict__ gridv, V* __restrict__ out,
+                                                             int CG) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int4 it = items[blockIdx.x];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int c0 = blockIdx.y * CG;
+  const int ncoil = (int)min((long long)CG, g.nbatch - c0);
+  int tc[3];
+  {
+    int t = it.x;
+    tc[2] = t % g.nt[2];
+    t /= g.nt[2];
+    tc[1] = t % g.nt[1];
+    tc[0] = t / g.nt[1];
+  }
+  int o[3], S[3];
+  for (int e = 0; e < 3; ++e) {
+    o[e] = tc[e] * g.T[e];
+    S[e] = g.T[e] + g.NT[e] - 1;
+  }
+  const int vol = S[0] * S[1] * S[2];
+  V* reg = reinterpret_cast<V*>(smem);
+  PointTaps* ptb = reinterpret_cast<PointTaps*>(smem + (size_t)vol * CG * sizeof(V));
+  PointTaps& pt = ptb[warp];
+
+  // stage tile + halo: z fastest in global memory, batch fastest in shared
+  const long long gvol = (long long)g.N[0] * g.N[1] * g.N[2];
+  for (int i = threadIdx.x; i < vol * ncoil; i += NTHR) {
+    int z = i % S[2];
+    int r = i / S[2];
+    const int y = r % S[1];
+    r /= S[1];
+    const int x = r % S[0];
+    const int c = r / S[0];
+    int gx = o[0] + x, gy = o[1] + y, gz = o[2] + z;
+    V v = VT<V>::zero();
+    bool in = true;
+    if (g.pad == TLGB_PAD_CIRCULAR) {
+      gx = wrapi(gx, g.N[0]);
+      gy = wrapi(gy, g.N[1]);
+      gz = wrapi(gz, g.N[2]);
+    } else {
+      in = gx < g.N[0] && gy < g.N[1] && gz < g.N[2];
+    }
+    if (in) v = __ldg(gridv + (long long)(c0 + c) * gvol + ((long long)gx * g.N[1] + gy) * g.N[2] + gz);
+    reg[((x * S[1] + y) * S[2] + z) * CG + c] = v;
+  }
+  __syncthreads();
+
+  const int CGP = CG <= 1 ? 1 : (CG <= 2 ? 2 : (CG <= 4 ? 4 : 8));
+  const int lgc = lg2i(CGP);
+  const int c = lane & (CGP - 1);
+  const int q = lane >> lgc;
+  const int QN = 32 >> lgc;
+  for (int ei = it.y + warp; ei < it.z; ei += NWARP) {
+    const long long p = entries[ei];
+    if (!warp_point_taps<NORM, false>(g, locs, p, pt, lane)) continue;  // never for home pairs
+    int l[3];
+    for (int e = 0; e < 3; ++e) l[e] = pt.start[e] - o[e];
+    V acc = VT<V>::zero();
+    for (int ka = 0; ka < pt.n[0]; ++ka) {
+      for (int kb = 0; kb < pt.n[1]; ++kb) {
+        const V* row = reg + (((l[0] + ka) * S[1] + (l[1] + kb)) * S[2] + l[2]) * CG + c;
+        if (NORM == 1) {
+          const float wab = pt.w[0][ka] * pt.w[1][kb];
+          for (int kc = q; kc < pt.n[2]; kc += QN) {
+            const float w = wab * pt.w[2][kc];
+            if (c < ncoil) VT<V>::fma(acc, w, row[kc * CG]);
+          }
+        } else {
+          for (int kc = q; kc < pt.n[2]; kc += QN) {
+            const float w = radial_w(g, pt.w[0][ka], pt.w[1][kb], pt.w[2][kc]);
+            if (c < ncoil) VT<V>::fma(acc, w, row[kc * CG]);
+          }
+        }
+      }
+    }
+    for (int m = CGP; m < 32; m <<= 1) VT<V>::add(acc, VT<V>::shfl_xor(acc, m));
+    if (q == 0 && c < ncoil) out[(long long)(c0 + c) * g.npts + p] = acc;
+    __syncwarp();
+  }
+}
+
+// ------------------------------------------------------------------ adjoint
+
+template <typename V>
+struct AdjPoint {
+  PointTaps t;
+  V v[CGMAX];
+};
+
+template <typename V, int NORM>
+__global__ void __launch_bounds__(NTHR) interp_adj_kernel(Geo g, const int4* __restrict__ items,
+                                                          const int32_t* __restrict__ entries,
+                                                          const float* __restrict__ locs,
+                                                          const V* __restrict__ vals, V* __restrict__ gridv,
+                                                          V* __restrict__ partial, int CG) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int4 it = items[blockIdx.x];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int cg = blockIdx.y;
+  const int c0 = cg * CG;
+  const int ncoil = (int)min((long long)CG, g.nbatch - c0);
+  int tc[3];
+  {
+    int t = it.x;
+    tc[2] = t % g.nt[2];
+    t /= g.nt[2];
+    tc[1] = t % g.nt[1];
+    tc[0] = t / g.nt[1];
+  }
+  int o[3];
+  for (int e = 0; e < 3; ++e) o[e] = tc[e] * g.T[e];
+  const int tvol = g.T[0] * g.T[1] * g.T[2];
+  V* acc = reinterpret_cast<V*>(smem);
+  AdjPoint<V>* pb = reinterpret_cast<AdjPoint<V>*>(smem + (size_t)tvol * CG * sizeof(V));
+  for (int i = threadIdx.x; i < tvol * CG; i += NTHR) acc[i] = VT<V>::zero();
+
+  const int CGP = CG <= 1 ? 1 : (CG <= 2 ? 2 : (CG <= 4 ? 4 : 8));
+  const int lgc = lg2i(CGP);
+  const int c = lane & (CGP - 1);
+  const int q = lane >> lgc;
+  const int QN = 32 >> lgc;
+  // ownership: outer active dim; 1D grids use runs of 64 cells
+  const int od = 3 - g.ndim;
+  const int og = g.ndim == 1 ? 64 : 1;
+
+  for (int b = it.y; b < it.z; b += PB) {
+    const int nb = min(PB, it.z - b);
+    __syncthreads();
+    for (int j = warp; j < nb; j += NWARP) {
+      const long long p = entries[b + j];
+      AdjPoint<V>& P = pb[j];
+      if (!warp_point_taps<NORM, false>(g, locs, p, P.t, lane)) {
+        if (lane == 0) P.t.n[0] = 0;  // no valid tap: contributes nothing
+      }
+      if (lane < ncoil) P.v[lane] = __ldg(vals + (long long)(c0 + lane) * g.npts + p);
+    }
+    __syncthreads();
+    for (int j = 0; j < nb; ++j) {
+      const AdjPoint<V>& P = pb[j];
+      const V v = c < ncoil ? P.v[c] : VT<V>::zero();
+      for (int ka = 0; ka < P.t.n[0]; ++ka) {
+        int ga = P.t.start[0] + ka;
+        if (ga >= g.N[0]) ga = wrapi(ga, g.N[0]);
+        const int la = ga - o[0];
+        if (la < 0 || la >= g.T[0]) continue;
+        if (od == 0 && (la % NWARP) != warp) continue;
+        for (int kb = 0; kb < P.t.n[1]; ++kb) {
+          int gb = P.t.start[1] + kb;
+          if (gb >= g.N[1]) gb = wrapi(gb, g.N[1]);
+          const int lb = gb - o[1];
+          if (lb < 0 || lb >= g.T[1]) continue;
+          if (od == 1 && (lb % NWARP) != warp) continue;
+          V* row = acc + (la * g.T[1] + lb) * g.T[2] * CG + c;
+          const float wab = NORM == 1 ? P.t.w[0][ka] * P.t.w[1][kb] : 0.f;
+          if (g.wrap_safe) {
+            for (int kc = q; kc < P.t.n[2]; kc += QN) {
+              int gc = P.t.start[2] + kc;
+              if (gc >= g.N[2]) gc = wrapi(gc, g.N[2]);
+              const int lc = gc - o[2];
+              if (lc < 0 || lc >= g.T[2] || c >= ncoil) continue;
+              if (od == 2 && ((lc / og) % NWARP) != warp) continue;
+              const float w = NORM == 1 ? wab * P.t.w[2][kc] : radial_w(g, P.t.w[0][ka], P.t.w[1][kb], P.t.w[2][kc]);
+              VT<V>::fma(row[lc * CG], w, v);
+            }
+          } else {
+            // a window longer than the grid hits a cell more than once:
+            // taps in sequence, lanes split by batch entry only
+            if (q == 0 && c < ncoil) {
+              for (int kc = 0; kc < P.t.n[2]; ++kc) {
+                const int gc = wrapi(P.t.start[2] + kc, g.N[2]);
+                const int lc = gc - o[2];
+                if (lc < 0 || lc >= g.T[2]) continue;
+                if (od == 2 && ((lc / og) % NWARP) != warp) continue;
+                const float w = NORM == 1 ? wab * P.t.w[2][kc] : radial_w(g, P.t.w[0][ka], P.t.w[1][kb], P.t.w[2][kc]);
+                VT<V>::fma(row[lc * CG], w, v);
+              }
+            }
+          }
+          __syncwarp();
+        }
+      }
+    }
+  }
+  __syncthreads();
+  if (it.w >= 0) {
+    V* dst = partial + ((long long)it.w * gridDim.y + cg) * tvol * CG;
+    for (int i = threadIdx.x; i < tvol * CG; i += NTHR) dst[i] = acc[i];
+    return;
+  }
+  const long long gvol = (long long)g.N[0] * g.N[1] * g.N[2];
+  for (int i = threadIdx.x; i < tvol * ncoil; i += NTHR) {
+    const int z = i % g.T[2];
+    int r = i / g.T[2];
+    const int y = r % g.T[1];
+    r /= g.T[1];
+    const int x = r % g.T[0];
+    const int cc = r / g.T[0];
+    const int gx = o[0] + x, gy = o[1] + y, gz = o[2] + z;
+    if (gx >= g.N[0] || gy >= g.N[1] || gz >= g.N[2]) continue;
+    gridv[(long long)(c0 + cc) * gvol + ((long long)gx * g.N[1] + gy) * g.N[2] + gz] =
+        acc[((x * g.T[1] + y) * g.T[2] + z) * CG + cc];
+  }
+}
+
+// Sum the partial tiles of one split tile in slot order and write it out.
+template <typename V>
+__global__ void __launch_bounds__(NTHR) adj_reduce_kernel(Geo g, const int4* __restrict__ split,
+                                                          const V* __restrict__ partial, V* __restrict__ gridv,
+                                                          int CG, int ncg) {
+  const int4 sp = split[blockIdx.x];
+  const int cg = blockIdx.y;
+  const int c0 = cg * CG;
+  const int ncoil = (int)min((long long)CG, g.nbatch - c0);
+  int tc[3];
+  {
+    int t = sp.x;
+    tc[2] = t % g.nt[2];
+    t /= g.nt[2];
+    tc[1] = t % g.nt[1];
+    tc[0] = t / g.nt[1];
+  }
+  const int tvol = g.T[0] * g.T[1] * g.T[2];
+  const long long gvol = (long long)g.N[0] * g.N[1] * g.N[2];
+  for (int i = threadIdx.x; i < tvol * ncoil; i += NTHR) {
+    const int z = i % g.T[2];
+    int r = i / g.T[2];
+    const int y = r % g.T[1];
+    r /= g.T[1];
+    const int x = r % g.T[0];
+    const int cc = r / g.T[0];
+    const int gx = tc[0] * g.T[0] + x, gy = tc[1] * g.T[1] + y, gz = tc[2] * g.T[2] + z;
+    if (gx >= g.N[0] || gy >= g.N[1] || gz >= g.N[2]) continue;
+    const int li = ((x * g.T[1] + y) * g.T[2] + z) * CG + cc;
+    V s = partial[((long long)sp.y * ncg + cg) * tvol * CG + li];
+    for (int k = 1; k < sp.z; ++k) VT<V>::add(s, partial[((long long)(sp.y + k) * ncg + cg) * tvol * CG + li]);
+    gridv[(long long)(c0 + cc) * gvol + ((long long)gx * g.N[1] + gy) * g.N[2] + gz] = s;
+  }
+}
+
+// ------------------------------------------------------------ trajectory grad
+
+template <typename V, int NORM>
+__global__ void __launch_bounds__(NTHR) interp_grad_kernel(Geo g, const int4* __restrict__ items,
+                                                              const int32_t* __restrict__ entries,
+                                                              const float* __restrict__ locs,
+                                                              const V* __restrict__ gridv, const V* __restrict__ a,
+                                                              float* __restrict__ grad, int CG, int chunk) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int4 it = items[blockIdx.x];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int tc[3];
+  {
+    int t = it.x;
+    tc[2] = t % g.nt[2];
+    t /= g.nt[2];
+    tc[1] = t % g.nt[1];
+    tc[0] = t / g.nt[1];
+  }
+  int o[3], S[3];
+  for (int e = 0; e < 3; ++e) {
+    o[e] = tc[e] * g.T[e];
+    S[e] = g.T[e] + g.NT[e] - 1;
+  }
+  const int vol = S[0] * S[1] * S[2];
+  V* reg = reinterpret_cast<V*>(smem);
+  PTaps<true>* ptb = reinterpret_cast<PTaps<true>*>(smem + (size_t)vol * CG * sizeof(V));
+  float* gacc = reinterpret_cast<float*>(ptb + NWARP);  // [chunk][3]
+  PTaps<true>& pt = ptb[warp];
+  const int npt = it.z - it.y;
+  for (int i = threadIdx.x; i < npt * 3; i += NTHR) gacc[i] = 0.f;
+  const long long gvol = (long long)g.N[0] * g.N[1] * g.N[2];
+  const int CGP = CG <= 1 ? 1 : (CG <= 2 ? 2 : (CG <= 4 ? 4 : 8));
+  const int lgc = lg2i(CGP);
+  const int c = lane & (CGP - 1);
+  const int q = lane >> lgc;
+  const int QN = 32 >> lgc;
+  const int ncg = (int)((g.nbatch + CG - 1) / CG);
+  for (int cg = 0; cg < ncg; ++cg) {
+    const int c0 = cg * CG;
+    const int ncoil = (int)min((long long)CG, g.nbatch - c0);
+    __syncthreads();
+    for (int i = threadIdx.x; i < vol * ncoil; i += NTHR) {
+      int z = i % S[2];
+      int r = i / S[2];
+      const int y = r % S[1];
+      r /= S[1];
+      const int x = r % S[0];
+      const int cc = r / S[0];
+      int gx = o[0] + x, gy = o[1] + y, gz = o[2] + z;
+      V v = VT<V>::zero();
+      bool in = true;
+      if (g.pad == TLGB_PAD_CIRCULAR) {
+        gx = wrapi(gx, g.N[0]);
+        gy = wrapi(gy, g.N[1]);
+        gz = wrapi(gz, g.N[2]);
+      } else {
+        in = gx < g.N[0] && gy < g.N[1] && gz < g.N[2];
+      }
+      if (in) v = __ldg(gridv + (long long)(c0 + cc) * gvol + ((long long)gx * g.N[1] + gy) * g.N[2] + gz);
+      reg[((x * S[1] + y) * S[2] + z) * CG + cc] = v;
+    }
+    __syncthreads();
+    for (int ei = it.y + warp; ei < it.z; ei += NWARP) {
+      const long long p = entries[ei];
+      if (!warp_point_taps<NORM, true>(g, locs, p, pt, lane)) continue;
+      int l[3];
+      for (int e = 0; e < 3; ++e) l[e] = pt.start[e] - o[e];
+      V d0 = VT<V>::zero(), d1 = VT<V>::zero(), d2 = VT<V>::zero();
+      for (int ka = 0; ka < pt.n[0]; ++ka) {
+        for (int kb = 0; kb < pt.n[1]; ++kb) {
+          const V* row = reg + (((l[0] + ka) * S[1] + (l[1] + kb)) * S[2] + l[2]) * CG + c;
+          for (int kc = q; kc < pt.n[2]; kc += QN) {
+            if (c >= ncoil) continue;
+            const V gv = row[kc * CG];
+            float w0, w1, w2;
+            if (NORM == 1) {
+              const float wa = pt.w[0][ka], wb = pt.w[1][kb], wc = pt.w[2][kc];
+              w0 = pt.dw[0][ka] * wb * wc;
+              w1 = wa * pt.dw[1][kb] * wc;
+              w2 = wa * wb * pt.dw[2][kc];
+            } else {
+              const float a0 = pt.w[0][ka], a1 = pt.w[1][kb], a2 = pt.w[2][kc];
+              const float rho = sqrtf(a0 * a0 + a1 * a1 + a2 * a2);
+              float kd = 0.f;
+              if (rho <= 1.0f && rho > 0.f) kd = kern_deriv(g.kernel, rho, g.beta) / rho;
+              w0 = g.act[0] ? kd * pt.dw[0][ka] / g.r[0] : 0.f;
+              w1 = g.act[1] ? kd * pt.dw[1][kb] / g.r[1] : 0.f;
+              w2 = g.act[2] ? kd * pt.dw[2][kc] / g.r[2] : 0.f;
+            }
+            VT<V>::fma(d0, w0, gv);
+            VT<V>::fma(d1, w1, gv);
+            VT<V>::fma(d2, w2, gv);
+          }
+        }
+      }
+      float r0 = 0.f, r1 = 0.f, r2 = 0.f;
+      if (c < ncoil) {
+        const V av = __ldg(a + (long long)(c0 + c) * g.npts + p);
+        r0 = VT<V>::re_dot(av, d0);
+        r1 = VT<V>::re_dot(av, d1);
+        r2 = VT<V>::re_dot(av, d2);
+      }
+      for (int m = 1; m < 32; m <<= 1) {
+        r0 += __shfl_xor_sync(0xffffffffu, r0, m);
+        r1 += __shfl_xor_sync(0xffffffffu, r1, m);
+        r2 += __shfl_xor_sync(0xffffffffu, r2, m);
+      }
+      if (lane == 0) {
+        float* ga = gacc + (ei - it.y) * 3;
+        ga[0] += r0;
+        ga[1] += r1;
+        ga[2] += r2;
+      }
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < npt; i += NTHR) {
+    const long long p = entries[it.y + i];
+    for (int e = 3 - g.ndim; e < 3; ++e) grad[p * g.ndim + (e - (3 - g.ndim))] = gacc[i * 3 + e];
+  }
+}
+
+// ------------------------------------------------------------- host helpers
+
+struct PlanLayout {
+  int64_t e_max, max_fwd, max_adj, ntiles;
+  int64_t off_entries, off_fwd, off_adj, off_split, bytes;
+  // tmp
+  int64_t t_cnt, t_keys, t_keys2, t_vals2, t_counts, t_hist, t_total, t_bytes;
+};
+
+constexpr int64_t kFwdChunk = 512;
+constexpr int64_t kAdjChunk = 2048;
+
+int make_geo(const tlgb_interp_desc* d, Geo& g) {
+  if (!d) TLGB_FAIL(TLGB_ERR_INVALID, "null interp descriptor");
+  if (d->ndim < 1 || d->ndim > 3) TLGB_FAIL(TLGB_ERR_INVALID, "ndim must be 1, 2 or 3");
+  if (d->kernel != TLGB_KERNEL_KAISER_BESSEL && d->kernel != TLGB_KERNEL_SPLINE)
+    TLGB_FAIL(TLGB_ERR_INVALID, "unknown kernel");
+  if (d->norm != 1 && d->norm != 2) TLGB_FAIL(TLGB_ERR_INVALID, "norm must be 1 or 2");
+  if (d->pad_mode != TLGB_PAD_CIRCULAR && d->pad_mode != TLGB_PAD_ZERO) TLGB_FAIL(TLGB_ERR_INVALID, "unknown pad mode");
+  if (d->npts < 0 || d->nbatch < 0) TLGB_FAIL(TLGB_ERR_INVALID, "negative size");
+  memset(&g, 0, sizeof(g));
+  g.ndim = d->ndim;
+  const int off = 3 - d->ndim;
+  int maxnt = 1;
+  for (int e = 0; e < 3; ++e) {
+    if (e < off) {
+      g.N[e] = 1;
+      g.NT[e] = 1;
+      g.r[e] = 1.f;
+      g.act[e] = 0;
+      continue;
+    }
+    const int64_t n = d->grid_size[e - off];
+    const float w = d->width[e - off];
+    if (n < 1 || n > (1 << 24)) TLGB_FAIL(TLGB_ERR_INVALID, "grid size must be in [1, 2^24]");
+    if (!(w > 0.f)) TLGB_FAIL(TLGB_ERR_INVALID, "kernel width must be positive");
+    // len(torch.arange(w + 1)) taps, as the reference's diff grid
+    const int nt = (int)ceil((double)w + 1.0);
+    if (nt > NTMAX) TLGB_FAIL(TLGB_ERR_UNSUPPORTED, "kernel width must be below 15 grid units");
+    g.N[e] = (int)n;
+    g.NT[e] = nt;
+    g.r[e] = w / 2.0f;
+    g.act[e] = 1;
+    maxnt = std::max(maxnt, nt);
+  }
+  if (d->ndim == 3 && maxnt > 9) TLGB_FAIL(TLGB_ERR_UNSUPPORTED, "3D kernel width must be below 8 grid units");
+  const int T3[3] = {8, 8, 8}, T2[3] = {1, 32, 32}, T1[3] = {1, 1, 512};
+  const int* T = d->ndim == 3 ? T3 : (d->ndim == 2 ? T2 : T1);
+  g.wrap_safe = 1;
+  for (int e = 0; e < 3; ++e) {
+    g.T[e] = std::min(T[e], g.N[e]);
+    g.nt[e] = (int)cdiv(g.N[e], g.T[e]);
+    if (g.act[e] && g.N[e] < g.NT[e]) g.wrap_safe = 0;
+  }
+  g.kernel = d->kernel;
+  g.norm = d->norm;
+  g.pad = d->pad_mode;
+  g.cplx = d->is_complex ? 1 : 0;
+  g.beta = d->beta;
+  g.npts = d->npts;
+  g.nbatch = d->nbatch;
+  if ((int64_t)g.nt[0] * g.nt[1] * g.nt[2] >= (1ll << 30)) TLGB_FAIL(TLGB_ERR_UNSUPPORTED, "too many tiles");
+  return TLGB_OK;
+}
+
+// Tiles one point can touch along a dim: 2 for T >= taps - 1, 3 where a
+// circular window can cross both a ragged last tile and the wrap.
+int64_t max_tiles_per_dim(const Geo& g, int e) {
+  if (g.nt[e] == 1) return 1;
+  const int m = g.N[e] % g.T[e];
+  if (g.pad == TLGB_PAD_CIRCULAR && m != 0 && m < g.NT[e] - 1) return std::min(3, g.nt[e]);
+  return 2;
+}
+
+PlanLayout layout(const Geo& g) {
+  PlanLayout L;
+  L.e_max = g.npts * max_tiles_per_dim(g, 0) * max_tiles_per_dim(g, 1) * max_tiles_per_dim(g, 2);
+  L.ntiles = (int64_t)g.nt[0] * g.nt[1] * g.nt[2];
+  L.max_fwd = L.ntiles + cdiv(g.npts, kFwdChunk) + 1;
+  L.max_adj = L.ntiles + cdiv(L.e_max, kAdjChunk) + 1;
+  size_t o = 0;
+  L.off_entries = o;
+  o = align_up(o + (size_t)std::max<int64_t>(L.e_max, 1) * 4, 256);
+  L.off_fwd = o;
+  o = align_up(o + (size_t)L.max_fwd * 16, 256);
+  L.off_adj = o;
+  o = align_up(o + (size_t)L.max_adj * 16, 256);
+  L.off_split = o;
+  o = align_up(o + (size_t)(L.ntiles + 1) * 16, 256);
+  L.bytes = o;
+  size_t t = 0;
+  L.t_cnt = t;
+  t = align_up(t + (size_t)(g.npts + 1) * 4, 256);
+  L.t_keys = t;
+  t = align_up(t + (size_t)std::max<int64_t>(L.e_max, 1) * 4, 256);
+  L.t_keys2 = t;
+  t = align_up(t + (size_t)std::max<int64_t>(L.e_max, 1) * 4, 256);
+  L.t_vals2 = t;
+  t = align_up(t + (size_t)std::max<int64_t>(L.e_max, 1) * 4, 256);
+  L.t_counts = t;
+  t = align_up(t + (size_t)radix_counts_len(std::max<int64_t>(L.e_max, 1)) * 4, 256);
+  L.t_hist = t;
+  t = align_up(t + (size_t)(2 * L.ntiles + 1) * 4, 256);
+  L.t_total = t;
+  t = align_up(t + 16, 256);
+  L.t_bytes = t;
+  return L;
+}
+
+int value_size(const Geo& g) { return g.cplx ? 8 : 4; }
+
+// batch entries staged per CTA: as many as fit two CTAs per SM
+int fwd_cg(const Geo& g, size_t taps_bytes) {
+  int cg = (int)std::min<long long>(std::max<long long>(g.nbatch, 1), CGMAX);
+  const int64_t vol = (int64_t)(g.T[0] + g.NT[0] - 1) * (g.T[1] + g.NT[1] - 1) * (g.T[2] + g.NT[2] - 1);
+  const int64_t cap = 112 * 1024 - NWARP * (int64_t)taps_bytes - 1024;
+  while (cg > 1 && vol * cg * value_size(g) > cap) --cg;
+  return cg;
+}
+
+size_t fwd_smem(const Geo& g, int cg, size_t taps_bytes) {
+  const int64_t vol = (int64_t)(g.T[0] + g.NT[0] - 1) * (g.T[1] + g.NT[1] - 1) * (g.T[2] + g.NT[2] - 1);
+  return (size_t)vol * cg * value_size(g) + NWARP * taps_bytes;
+}
+
+int adj_cg(const Geo& g) { return (int)std::min<long long>(std::max<long long>(g.nbatch, 1), CGMAX); }
+
+size_t adj_smem(const Geo& g, int cg) {
+  const int64_t tvol = (int64_t)g.T[0] * g.T[1] * g.T[2];
+  const size_t pbs = g.cplx ? sizeof(AdjPoint<float2>) : sizeof(AdjPoint<float>);
+  return (size_t)tvol * cg * value_size(g) + PB * pbs;
+}
+
+int check_plan(const Geo& g, const tlgb_interp_plan_info* info, const void* plan) {
+  if (!info || !plan) TLGB_FAIL(TLGB_ERR_INVALID, "missing plan");
+  for (int e = 0; e < 3; ++e)
+    if (info->tile[e] != g.T[e] || info->n_tile[e] != g.nt[e])
+      TLGB_FAIL(TLGB_ERR_INVALID, "plan was built for another grid");
+  return TLGB_OK;
+}
+
+template <typename F>
+int set_smem(F* kernel, size_t bytes) {
+  TLGB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  return TLGB_OK;
+}
+
+}  // namespace
+}  // namespace tlgb
+
+using namespace tlgb;
+
+extern "C" int tlgb_interp_plan_size(const tlgb_interp_desc* d, size_t* plan_bytes, size_t* tmp_bytes) {
+  Geo g;
+  TLGB_TRY(make_geo(d, g));
+  const PlanLayout L = layout(g);
+  if (L.e_max >= (1ll << 31)) TLGB_FAIL(TLGB_ERR_UNSUPPORTED, "too many points for one plan");
+  if (plan_bytes) *plan_bytes = (size_t)L.bytes;
+  if (tmp_bytes) *tmp_bytes = (size_t)L.t_bytes;
+  return TLGB_OK;
+}
+
+extern "C" int tlgb_interp_plan_build(const tlgb_interp_desc* d, const float* locs, void* plan, size_t plan_bytes,
+                                      void* tmp, size_t tmp_bytes, tlgb_interp_plan_info* info,
+                                      tlgb_stream_t stream) {
+  Geo g;
+  TLGB_TRY(make_geo(d, g));
+  const PlanLayout L = layout(g);
+  if (L.e_max >= (1ll << 31)) TLGB_FAIL(TLGB_ERR_UNSUPPORTED, "too many points for one plan");
+  if (!info || !plan || !tmp || (g.npts > 0 && !locs)) TLGB_FAIL(TLGB_ERR_INVALID, "null pointer");
+  if (plan_bytes < (size_t)L.bytes || tmp_bytes < (size_t)L.t_bytes) TLGB_FAIL(TLGB_ERR_WORKSPACE, "plan workspace too small");
+  cudaStream_t s = (cudaStream_t)stream;
+  char* P = (char*)plan;
+  char* Tm = (char*)tmp;
+  uint32_t* cnt = (uint32_t*)(Tm + L.t_cnt);
+  uint32_t* keys = (uint32_t*)(Tm + L.t_keys);
+  uint32_t* keys2 = (uint32_t*)(Tm + L.t_keys2);
+  int32_t* vals2 = (int32_t*)(Tm + L.t_vals2);
+  uint32_t* counts = (uint32_t*)(Tm + L.t_counts);
+  uint32_t* hist = (uint32_t*)(Tm + L.t_hist);
+  uint32_t* total = (uint32_t*)(Tm + L.t_total);
+  int32_t* entries = (int32_t*)(P + L.off_entries);
+
+  uint32_t E = 0;
+  if (g.npts > 0) {
+    const unsigned nb = (unsigned)cdiv(g.npts, 256);
+    plan_count_kernel<<<nb, 256, 0, s>>>(g, locs, cnt);
+    TLGB_CHECK_LAUNCH();
+    TLGB_TRY(exclusive_scan_u32(cnt, cnt, g.npts, total, s));
+    plan_emit_kernel<<<nb, 256, 0, s>>>(g, locs, cnt, keys, entries);
+    TLGB_CHECK_LAUNCH();
+    TLGB_CUDA(cudaMemcpyAsync(&E, total, 4, cudaMemcpyDeviceToHost, s));
+    TLGB_CUDA(cudaStreamSynchronize(s));
+  }
+  int bits = 1;
+  while ((1ll << bits) < 2 * L.ntiles) ++bits;
+  TLGB_TRY(radix_sort_pairs(keys, entries, keys2, vals2, counts, (int64_t)E, bits, s));
+  TLGB_CUDA(cudaMemsetAsync(hist, 0, (size_t)(2 * L.ntiles) * 4, s));
+  if (E > 0) {
+    key_hist_kernel<<<(unsigned)cdiv(E, 256), 256, 0, s>>>(keys, E, hist);
+    TLGB_CHECK_LAUNCH();
+  }
+  std::vector<uint32_t> h((size_t)(2 * L.ntiles));
+  TLGB_CUDA(cudaMemcpyAsync(h.data(), hist, h.size() * 4, cudaMemcpyDeviceToHost, s));
+  TLGB_CUDA(cudaStreamSynchronize(s));
+
+  // work items (host): heaviest first for load balance; results do not
+  // depend on the order because every item writes its own tile or slot
+  std::vector<int4> fwd, adj, split;
+  int64_t pos = 0, n_home = 0, n_partials = 0;
+  for (int64_t t = 0; t < L.ntiles; ++t) {
+    const int64_t nh = h[2 * t], nn = h[2 * t + 1];
+    const int64_t beg = pos, hend = pos + nh, end = pos + nh + nn;
+    n_home += nh;
+    for (int64_t b = beg; b < hend; b += kFwdChunk)
+      fwd.push_back(make_int4((int)t, (int)b, (int)std::min(hend, b + kFwdChunk), -1));
+    const int64_t na = end - beg;
+    if (na <= kAdjChunk) {
+      adj.push_back(make_int4((int)t, (int)beg, (int)end, -1));
+    } else {
+      const int64_t nch = cdiv(na, kAdjChunk);
+      split.push_back(make_int4((int)t, (int)n_partials, (int)nch, 0));
+      for (int64_t k = 0; k < nch; ++k)
+        adj.push_back(make_int4((int)t, (int)(beg + k * kAdjChunk), (int)std::min(end, beg + (k + 1) * kAdjChunk),
+                                (int)(n_partials + k)));
+      n_partials += nch;
+    }
+    pos = end;
+  }
+  auto heavier = [](const int4& a, const int4& b) { return (a.z - a.y) > (b.z - b.y); };
+  std::stable_sort(fwd.begin(), fwd.end(), heavier);
+  std::stable_sort(adj.begin(), adj.end(), heavier);
+  if ((int64_t)fwd.size() > L.max_fwd || (int64_t)adj.size() > L.max_adj)
+    TLGB_FAIL(TLGB_ERR_DEVICE, "work list larger than its bound");
+  if (!fwd.empty()) TLGB_CUDA(cudaMemcpyAsync(P + L.off_fwd, fwd.data(), fwd.size() * 16, cudaMemcpyHostToDevice, s));
+  if (!adj.empty()) TLGB_CUDA(cudaMemcpyAsync(P + L.off_adj, adj.data(), adj.size() * 16, cudaMemcpyHostToDevice, s));
+  if (!split.empty())
+    TLGB_CUDA(cudaMemcpyAsync(P + L.off_split, split.data(), split.size() * 16, cudaMemcpyHostToDevice, s));
+  // host vectors are freed on return: make the copies complete first
+  TLGB_CUDA(cudaStreamSynchronize(s));
+
+  memset(info, 0, sizeof(*info));
+  info->n_entries = E;
+  info->n_tiles = L.ntiles;
+  for (int e = 0; e < 3; ++e) {
+    info->tile[e] = g.T[e];
+    info->n_tile[e] = g.nt[e];
+  }
+  info->n_fwd_items = (int64_t)fwd.size();
+  info->n_adj_items = (int64_t)adj.size();
+  info->n_partials = n_partials;
+  info->n_split_tiles = (int64_t)split.size();
+  info->chunk = kAdjChunk;
+  info->off_entries = L.off_entries;
+  info->off_fwd_items = L.off_fwd;
+  info->off_adj_items = L.off_adj;
+  info->off_split = L.off_split;
+  info->plan_bytes = L.bytes;
+  info->reserved[0] = n_home;
+  return TLGB_OK;
+}
+
+extern "C" int tlgb_interp_adjoint_scratch_size(const tlgb_interp_desc* d, const tlgb_interp_plan_info* info,
+                                                size_t* bytes) {
+  Geo g;
+  TLGB_TRY(make_geo(d, g));
+  if (!info || !bytes) TLGB_FAIL(TLGB_ERR_INVALID, "null pointer");
+  const int cg = adj_cg(g);
+  const int64_t ncg = cdiv(std::max<long long>(g.nbatch, 1), cg);
+  *bytes = (size_t)info->n_partials * ncg * g.T[0] * g.T[1] * g.T[2] * cg * value_size(g);
+  return TLGB_OK;
+}
+
+namespace tlgb {
+namespace {
+
+template <typename V, int NORM>
+int launch_fwd(const Geo& g, const tlgb_interp_plan_info* info, const char* P, const float* locs, const void* grid,
+               void* out, cudaStream_t s) {
+  const int cg = fwd_cg(g, sizeof(PTaps<false>));
+  const int64_t ncg = cdiv(g.nbatch, cg);
+  const size_t sm = fwd_smem(g, cg, sizeof(PTaps<false>));
+  auto* k = interp_fwd_kernel<V, NORM>;
+  TLGB_TRY(set_smem(k, sm));
+  dim3 grd((unsigned)info->n_fwd_items, (unsigned)ncg);
+  k<<<grd, NTHR, sm, s>>>(g, (const int4*)(P + info->off_fwd_items), (const int32_t*)(P + info->off_entries), locs,
+                         (const V*)grid, (V*)out, cg);
+  TLGB_CHECK_LAUNCH();
+  return TLGB_OK;
+}
+
+template <typename V, int NORM>
+int launch_adj(const Geo& g, const tlgb_interp_plan_info* info, const char* P, const float* locs, const void* vals,
+               void* grid, void* scratch, cudaStream_t s) {
+  const int cg = adj_cg(g);
+  const int64_t ncg = cdiv(g.nbatch, cg);
+  const size_t sm = adj_smem(g, cg);
+  auto* k = interp_adj_kernel<V, NORM>;
+  TLGB_TRY(set_smem(k, sm));
+  dim3 grd((unsigned)info->n_adj_items, (unsigned)ncg);
+  k<<<grd, NTHR, sm, s>>>(g, (const int4*)(P + info->off_adj_items), (const int32_t*)(P + info->off_entries), locs,
+                         (const V*)vals, (V*)grid, (V*)scratch, cg);
+  TLGB_CHECK_LAUNCH();
+  if (info->n_split_tiles > 0) {
+    dim3 g2((unsigned)info->n_split_tiles, (unsigned)ncg);
+    adj_reduce_kernel<V><<<g2, NTHR, 0, s>>>(g, (const int4*)(P + info->off_split), (const V*)scratch, (V*)grid, cg,
+                                             (int)ncg);
+    TLGB_CHECK_LAUNCH();
+  }
+  return TLGB_OK;
+}
+
+template <typename V, int NORM>
+int launch_grad(const Geo& g, const tlgb_interp_plan_info* info, const char* P, const float* locs, const void* grid,
+                const void* a, float* grad, cudaStream_t s) {
+  const int cg = fwd_cg(g, sizeof(PTaps<true>));
+  const size_t sm = fwd_smem(g, cg, sizeof(PTaps<true>)) + kFwdChunk * 3 * sizeof(float);
+  auto* k = interp_grad_kernel<V, NORM>;
+  TLGB_TRY(set_smem(k, sm));
+  k<<<(unsigned)info->n_fwd_items, NTHR, sm, s>>>(g, (const int4*)(P + info->off_fwd_items),
+                                                  (const int32_t*)(P + info->off_entries), locs, (const V*)grid,
+                                                  (const V*)a, grad, cg, (int)kFwdChunk);
+  TLGB_CHECK_LAUNCH();
+  return TLGB_OK;
+}
+
+}  // namespace
+}  // namespace tlgb
+
+extern "C" int tlgb_interp_forward(const tlgb_interp_desc* d, const tlgb_interp_plan_info* info, const void* plan,
+                                   const float* locs, const void* grid, void* out, tlgb_stream_t stream) {
+  Geo g;
+  TLGB_TRY(make_geo(d, g));
+  TLGB_TRY(check_plan(g, info, plan));
+  if (g.npts == 0 || g.nbatch == 0) return TLGB_OK;
+  if (!locs || !grid || !out) TLGB_FAIL(TLGB_ERR_INVALID, "null pointer");
+  cudaStream_t s = (cudaStream_t)stream;
+  if (info->reserved[0] < g.npts)  // points without a valid tap read as zero
+    TLGB_CUDA(cudaMemsetAsync(out, 0, (size_t)g.nbatch * g.npts * value_size(g), s));
+  if (info->n_fwd_items == 0) return TLGB_OK;
+  const char* P = (const char*)plan;
+  if (g.cplx)
+    return g.norm == 1 ? launch_fwd<float2, 1>(g, info, P, locs, grid, out, s) : launch_fwd<float2, 2>(g, info, P, locs, grid, out, s);
+  return g.norm == 1 ? launch_fwd<float, 1>(g, info, P, locs, grid, out, s) : launch_fwd<float, 2>(g, info, P, locs, grid, out, s);
+}
+
+extern "C" int tlgb_interp_adjoint(const tlgb_interp_desc* d, const tlgb_interp_plan_info* info, const void* plan,
+                                   const float* locs, const void* vals, void* grid, void* scratch,
+                                   size_t scratch_bytes, tlgb_stream_t stream) {
+  Geo g;
+  TLGB_TRY(make_geo(d, g));
+  TLGB_TRY(check_plan(g, info, plan));
+  if (g.nbatch == 0) return TLGB_OK;
+  if (!grid || (g.npts > 0 && (!locs || !vals))) TLGB_FAIL(TLGB_ERR_INVALID, "null pointer");
+  size_t need = 0;
+  TLGB_TRY(tlgb_interp_adjoint_scratch_size(d, info, &need));
+  if (scratch_bytes < need || (need > 0 && !scratch)) TLGB_FAIL(TLGB_ERR_WORKSPACE, "adjoint scratch too small");
+  cudaStream_t s = (cudaStream_t)stream;
+  const char* P = (const char*)plan;
+  if (g.cplx)
+    return g.norm == 1 ? launch_adj<float2, 1>(g, info, P, locs, vals, grid, scratch, s)
+                       : launch_adj<float2, 2>(g, info, P, locs, vals, grid, scratch, s);
+  return g.norm == 1 ? launch_adj<float, 1>(g, info, P, locs, vals, grid, scratch, s)
+                     : launch_adj<float, 2>(g, info, P, locs, vals, grid, scratch, s);
+}
+
+extern "C" int tlgb_interp_grad_locs(const tlgb_interp_desc* d, const tlgb_interp_plan_info* info, const void* plan,
+                                     const float* locs, const void* grid, const void* a, float* grad_locs,
+                                     tlgb_stream_t stream) {
+  Geo g;
+  TLGB_TRY(make_geo(d, g));
+  TLGB_TRY(check_plan(g, info, plan));
+  if (g.npts == 0) return TLGB_OK;
+  if (!locs || !grid || !a || !grad_locs) TLGB_FAIL(TLGB_ERR_INVALID, "null pointer");
+  cudaStream_t s = (cudaStream_t)stream;
+  if (info->reserved[0] < g.npts || g.nbatch == 0)
+    TLGB_CUDA(cudaMemsetAsync(grad_locs, 0, (size_t)g.npts * g.ndim * sizeof(float), s));
+  if (g.nbatch == 0 || info->n_fwd_items == 0) return TLGB_OK;
+  const char* P = (const char*)plan;
+  if (g.cplx)
+    return g.norm == 1 ? launch_grad<float2, 1>(g, info, P, locs, grid, a, grad_locs, s)
+                       : launch_grad<float2, 2>(g, info, P, locs, grid, a, grad_locs, s);
+  return g.norm == 1 ? launch_grad<float, 1>(g, info, P, locs, grid, a, grad_locs, s)
+                     : launch_grad<float, 2>(g, info, P, locs, grid, a, grad_locs, s);
+}
