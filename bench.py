@@ -1,0 +1,468 @@
+"""Benchmark: 3D multicoil gridding + ungridding on one GB300 (and replicas).
+
+Workload (the configuration the headline metric is quoted on): oversampled
+grid 256^3 complex64 x 8 coils; 2^21 points float32 in a ball of radius 128
+centred on the grid with radial density ~ 1/r^2 (r ~ U(0,128), direction a
+normalised N(0, I3)); Kaiser-Bessel width 4, beta for oversampling 1.25.
+One step = one ungrid (forward interpolation) + one grid (adjoint) of all
+coils: the interpolation half of one NUFFT normal operator.
+
+    python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+Prints one JSON line. ``value`` = point-coil samples interpolated per second
+(both directions counted) with inputs resident in HBM; ``e2e`` = the same
+through the public API from pinned host buffers, copies included.
+``roofline`` is for the dominant kernel (gridding) against the measured HBM
+copy bandwidth; ``cpu_baseline`` times the CPU restatement of the reference's
+torch path (oracle) on a bounded sample on the host cores.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "torch-named-linops_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import torch  # noqa: E402
+
+N_GRID = 256
+N_COIL = 8
+N_PTS = 1 << 21
+WIDTH = 4.0
+OVERSAMP = 1.25
+# algorithmic bytes of one launch (either direction): grid + locs + point values
+ALGO_BYTES = N_COIL * N_GRID**3 * 8 + N_PTS * 3 * 4 + N_COIL * N_PTS * 8
+# unfold / fold workload: 16 x 160^3 complex64, block 8^3, stride 4
+BLK_SHAPE = (16, 160, 160, 160)
+BLK = (8, 8, 8)
+BLK_STRIDE = (4, 4, 4)
+
+
+def kb_beta(width=WIDTH, os_=OVERSAMP):
+    return math.pi * (((width / os_) * (os_ - 0.5)) ** 2 - 0.8) ** 0.5
+
+
+def make_locs(n=N_PTS, seed=0):
+    g = torch.Generator().manual_seed(seed)
+    r = torch.rand(n, generator=g) * (N_GRID / 2)
+    u = torch.randn(n, 3, generator=g)
+    u = u / u.norm(dim=-1, keepdim=True)
+    return (N_GRID / 2 + r[:, None] * u).to(torch.float32)
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per gridding launch from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f).get("grid_dram_bytes_per_launch")
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-f", self.path],
+                stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL,
+            )
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+            os.unlink(self.path)
+        except Exception:
+            pass
+        return {
+            "sm_mhz": statistics.median(sm) if sm else None,
+            "sm_max_mhz": max(smax) if smax else None,
+            "reasons": sorted(reasons),
+            "samples": len(sm),
+        }
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# --------------------------------------------------------------- CPU baseline
+
+
+class CpuSample:
+    """Oracle (CPU restatement of the reference torch path) on a sample of the
+    workload: all 8 coils, the full 256^3 grid, the first `sample_pts` points."""
+
+    def __init__(self, sample_pts: int):
+        from oracle import interp as OI
+
+        self.OI = OI
+        self.threads = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+        torch.set_num_threads(self.threads)
+        self.n = sample_pts
+        self.locs = make_locs()[:sample_pts].contiguous()
+        g = torch.Generator().manual_seed(1)
+        self.img = torch.randn(N_COIL, N_GRID, N_GRID, N_GRID, dtype=torch.complex64, generator=g)
+        self.vals = torch.randn(N_COIL, sample_pts, dtype=torch.complex64, generator=g)
+        self.beta = kb_beta()
+
+    def run(self) -> float:
+        t0 = time.perf_counter()
+        self.OI.ungrid(self.img, self.locs, WIDTH, beta=self.beta)
+        self.OI.grid(self.vals, self.locs, (N_GRID,) * 3, WIDTH, beta=self.beta)
+        return time.perf_counter() - t0
+
+    def describe(self, t: float, reps: int) -> dict:
+        return {
+            "value": 2 * self.n * N_COIL / t,
+            "unit": "point-coil samples/s",
+            "cores": self.threads,
+            "kind": "port",
+            "sample": f"{self.n} of {N_PTS} points, all {N_COIL} coils, full {N_GRID}^3 grid; ungrid+grid, median of {reps}",
+        }
+
+
+def cpu_baseline(sample_pts: int, reps: int = 3):
+    cs = CpuSample(sample_pts)
+    cs.run()  # warm-up
+    t = statistics.median(cs.run() for _ in range(reps))
+    return cs.describe(t, reps)
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    cs = CpuSample(args.ref_sample)
+    per = [cs.run() for _ in range(args.warmup + args.steps)]
+    timed = per[args.warmup:]
+    t = statistics.median(timed)
+    value = 2 * args.ref_sample * N_COIL / t
+    desc = cs.describe(t, len(timed))
+    line = {
+        "impl": "reference",
+        "metric": "3D multicoil gridding+ungridding throughput (256^3 x 8 coils, 2^21 points, KB W=4)",
+        "value": value,
+        "unit": "point-coil samples/s",
+        "n_gpus": 0,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": t * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "c64",
+        "data": "synthetic (1/r^2 ball trajectory, N(0,1) complex values), seeded",
+        "config": {"workload": f"interp3d_{N_GRID}cube_{N_COIL}coil_{N_PTS}pts", "grid": [N_GRID] * 3, "coils": N_COIL,
+                   "points": N_PTS, "width": WIDTH, "oversamp": OVERSAMP, "sample_points": args.ref_sample,
+                   "step": "ungrid + grid of the sample points on the CPU (reference torch path, restated)"},
+        "cpu_baseline": {k: desc[k] for k in ("cores", "kind", "sample")} | {"value": value, "unit": "point-coil samples/s"},
+        "e2e": {"value": value, "unit": "point-coil samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------- GPU arm
+
+
+def run_gpu(args, world, rank, local):
+    import torchlinops_gb300 as T
+    from torchlinops_gb300.interp import get_plan
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    beta = kb_beta()
+    kp = dict(beta=beta)
+    locs_h = make_locs()
+    locs = locs_h.to(dev)
+    gen = torch.Generator(device=dev).manual_seed(1234 + rank)
+    img = torch.randn(N_COIL, N_GRID, N_GRID, N_GRID, dtype=torch.complex64, device=dev, generator=gen)
+    vals = torch.randn(N_COIL, N_PTS, dtype=torch.complex64, device=dev, generator=gen)
+
+    # plan (one-time per trajectory), timed separately
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    plan = get_plan(locs, (N_GRID,) * 3, WIDTH, "kaiser_bessel", "circular")
+    torch.cuda.synchronize()
+    plan_ms = (time.perf_counter() - t0) * 1e3
+    launches_per_step = 2 + (1 if plan.info.n_split_tiles > 0 else 0)
+
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(args.warmup):
+        T.ungrid(img, locs, WIDTH, kernel_params=kp)
+        T.grid(vals, locs, (N_GRID,) * 3, WIDTH, kernel_params=kp)
+    torch.cuda.synchronize()
+
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t_start.record(stream)
+    for i in range(args.steps):
+        ev[i][0].record(stream)
+        out = T.ungrid(img, locs, WIDTH, kernel_params=kp)
+        ev[i][1].record(stream)
+        g = T.grid(vals, locs, (N_GRID,) * 3, WIDTH, kernel_params=kp)
+        ev[i][2].record(stream)
+        del out, g
+    t_end.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = sampler.stop()
+    total_ms = t_start.elapsed_time(t_end)
+    total_ms = max_over_ranks(total_ms, world)
+    fwd_ms = statistics.mean(e[0].elapsed_time(e[1]) for e in ev)
+    adj_ms = statistics.mean(e[1].elapsed_time(e[2]) for e in ev)
+    ms_step = total_ms / args.steps
+    value = world * 2 * N_PTS * N_COIL / (ms_step / 1e3)
+
+    # end to end through the public API, pinned host buffers, copies inside
+    img_h = torch.empty(img.shape, dtype=img.dtype, pin_memory=True)
+    img_h.copy_(img)
+    vals_h = torch.empty(vals.shape, dtype=vals.dtype, pin_memory=True)
+    vals_h.copy_(vals)
+    out_h = torch.empty(N_COIL, N_PTS, dtype=torch.complex64, pin_memory=True)
+    grid_h = torch.empty(img.shape, dtype=img.dtype, pin_memory=True)
+    e2e_steps = max(2, min(args.steps, 5))
+    torch.cuda.synchronize()
+    e2e_times = []
+    for i in range(e2e_steps + 1):
+        barrier(world)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        im_d = img_h.to(dev, non_blocking=True)
+        va_d = vals_h.to(dev, non_blocking=True)
+        o = T.ungrid(im_d, locs, WIDTH, kernel_params=kp)
+        g = T.grid(va_d, locs, (N_GRID,) * 3, WIDTH, kernel_params=kp)
+        out_h.copy_(o, non_blocking=True)
+        grid_h.copy_(g, non_blocking=True)
+        torch.cuda.synchronize()
+        if i > 0:  # first pass is a warm-up of the pinned paths
+            e2e_times.append(time.perf_counter() - t0)
+        del im_d, va_d, o, g
+    e2e_s = max_over_ranks(statistics.median(e2e_times), world)
+    h2d = img_h.numel() * 8 + vals_h.numel() * 8
+    d2h = out_h.numel() * 8 + grid_h.numel() * 8
+
+    peak, peak_kind = measured_peaks()
+    dom_ms = max(adj_ms, fwd_ms)
+    dom = "grid" if adj_ms >= fwd_ms else "ungrid"
+    achieved = ALGO_BYTES / (dom_ms / 1e3) / 1e9
+    kernels = {
+        "ungrid": {"ms": fwd_ms, "GBps": ALGO_BYTES / (fwd_ms / 1e3) / 1e9,
+                   "frac": ALGO_BYTES / (fwd_ms / 1e3) / 1e9 / peak},
+        "grid": {"ms": adj_ms, "GBps": ALGO_BYTES / (adj_ms / 1e3) / 1e9,
+                 "frac": ALGO_BYTES / (adj_ms / 1e3) / 1e9 / peak,
+                 "partial_tiles": int(plan.info.n_partials)},
+        "plan_build_ms": plan_ms,
+        "plan_entries": int(plan.info.n_entries),
+    }
+    del img, vals, img_h, grid_h
+    torch.cuda.empty_cache()
+    if not args.skip_blocks:
+        kernels.update(bench_blocks(dev, peak, args))
+    line = None
+    if rank == 0:
+        cpu = None
+        if world == 1 and not args.skip_cpu:
+            cpu = cpu_baseline(args.ref_sample)
+        line = {
+            "metric": "3D multicoil gridding+ungridding throughput (256^3 x 8 coils, 2^21 points, KB W=4)",
+            "value": value,
+            "unit": "point-coil samples/s",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": ms_step,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "c64",
+            "data": "synthetic (1/r^2 ball trajectory, N(0,1) complex values), seeded",
+            "config": {
+                "workload": f"interp3d_{N_GRID}cube_{N_COIL}coil_{N_PTS}pts",
+                "grid": [N_GRID] * 3,
+                "coils": N_COIL,
+                "points": N_PTS,
+                "width": WIDTH,
+                "oversamp": OVERSAMP,
+                "kernel": "kaiser_bessel",
+                "step": "ungrid + grid (interpolation half of one normal op)",
+                "l2": "inputs larger than L2 (grid 1.07 GB per direction); no flush",
+                "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+            },
+            "e2e": {
+                "value": world * 2 * N_PTS * N_COIL / e2e_s,
+                "unit": "point-coil samples/s",
+                "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h,
+            },
+            "roofline": {
+                "kernel": dom,
+                "bound": "hbm",
+                "achieved": achieved,
+                "peak": peak,
+                "peak_kind": peak_kind,
+                "unit": "GB/s",
+                "frac": achieved / peak,
+                "traffic": profiled_traffic(),
+                "algorithmic_bytes_per_launch": ALGO_BYTES,
+            },
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+            "gpu_launches": launches_per_step * args.steps,
+            "kernels": kernels,
+        }
+        print(json.dumps(line), flush=True)
+    return line
+
+
+def bench_blocks(dev, peak, args):
+    """ArrayToBlocks / BlocksToArray, 16 x 160^3 complex64, block 8^3, stride 4."""
+    import torchlinops_gb300 as T
+
+    gen = torch.Generator(device=dev).manual_seed(7)
+    x = torch.randn(BLK_SHAPE, dtype=torch.complex64, device=dev, generator=gen)
+    nb = tuple((s - b) // st + 1 for s, b, st in zip(BLK_SHAPE[1:], BLK, BLK_STRIDE))
+    nbytes = x.numel() * 8 + BLK_SHAPE[0] * math.prod(nb) * math.prod(BLK) * 8
+    y = T.unfold(x, BLK, BLK_STRIDE)
+    for _ in range(3):
+        T.unfold(x, BLK, BLK_STRIDE, output=y)
+        T.fold(y, BLK_SHAPE[1:], BLK, BLK_STRIDE, output=x)
+    torch.cuda.synchronize()
+    reps = max(3, min(args.steps, 10))
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    s = torch.cuda.current_stream(dev)
+    e[0].record(s)
+    for _ in range(reps):
+        T.unfold(x, BLK, BLK_STRIDE, output=y)
+    e[1].record(s)
+    for _ in range(reps):
+        T.fold(y, BLK_SHAPE[1:], BLK, BLK_STRIDE, output=x)
+    e[2].record(s)
+    torch.cuda.synchronize()
+    u_ms = e[0].elapsed_time(e[1]) / reps
+    f_ms = e[1].elapsed_time(e[2]) / reps
+    del x, y
+    torch.cuda.empty_cache()
+    return {
+        "unfold": {"ms": u_ms, "GBps": nbytes / (u_ms / 1e3) / 1e9, "frac": nbytes / (u_ms / 1e3) / 1e9 / peak,
+                   "workload": "16x160^3 c64, block 8^3, stride 4"},
+        "fold": {"ms": f_ms, "GBps": nbytes / (f_ms / 1e3) / 1e9, "frac": nbytes / (f_ms / 1e3) / 1e9 / peak},
+    }
+
+
+def _resize(grid: int, points: int) -> None:
+    global N_GRID, N_PTS, ALGO_BYTES
+    N_GRID, N_PTS = grid, points
+    ALGO_BYTES = N_COIL * N_GRID**3 * 8 + N_PTS * 3 * 4 + N_COIL * N_PTS * 8
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="tlgb", choices=["tlgb", "reference"])
+    ap.add_argument("--ref-sample", type=int, default=1 << 16, help="points in the CPU baseline sample")
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-blocks", action="store_true")
+    ap.add_argument("--grid", type=int, default=N_GRID, help="grid edge (smaller cases for profiling)")
+    ap.add_argument("--points", type=int, default=N_PTS, help="number of points (smaller cases for profiling)")
+    args = ap.parse_args()
+    _resize(args.grid, args.points)
+    args.warmup = max(args.warmup, 3)
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_gpu(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -110,7 +110,7 @@ def unfold(
     batch_shape = x.shape[:-ndim]
     nbatch = prod(batch_shape)
     code = _dtype_code(x)
-    xc = x.contiguous()
+    xc = x.resolve_conj().resolve_neg().contiguous()
     L = _ext.lib()
     if mask is not None and output is None:
         idx, inv, nnz = _mask_tables(mask, block_size, dev)
@@ -169,7 +169,7 @@ def fold(
         y = output.view(out_shape)
     else:
         y = torch.empty(out_shape, dtype=x.dtype, device=dev)
-    xc = x.contiguous()
+    xc = x.resolve_conj().resolve_neg().contiguous()
     d = _desc(ndim, code, nbatch, im_size, block_size, stride, nnz, idx, inv)
     with torch.cuda.device(dev):
         _ext.check(L.tlgb_fold(ctypes.byref(d), _ext.ptr(xc), _ext.ptr(y), _ext.stream_ptr(dev)), "fold")

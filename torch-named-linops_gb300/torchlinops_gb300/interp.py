@@ -129,8 +129,6 @@ class InterpolatePlan:
                 "interpolation plan",
             )
         del tmp
-        # keep the float32 copy alive only if it is not the caller's tensor
-        self._locs_keep = locs_c if locs_c.data_ptr() != locs.data_ptr() else None
 
     @property
     def n_entries(self) -> int:
@@ -181,7 +179,8 @@ def _check_values(vals: Tensor) -> bool:
 
 
 def _as_f32_view(t: Tensor, is_complex: bool) -> Tensor:
-    t = t.contiguous()
+    # autograd may hand over lazily conjugated / negated views: materialise them
+    t = t.resolve_conj().resolve_neg().contiguous()
     return torch.view_as_real(t) if is_complex else t
 
 
