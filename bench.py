@@ -53,7 +53,8 @@ def kb_beta(width=WIDTH, os_=OVERSAMP):
     return math.pi * (((width / os_) * (os_ - 0.5)) ** 2 - 0.8) ** 0.5
 
 
-def make_locs(n=N_PTS, seed=0):
+def make_locs(n=None, seed=0):
+    n = N_PTS if n is None else n
     g = torch.Generator().manual_seed(seed)
     r = torch.rand(n, generator=g) * (N_GRID / 2)
     u = torch.randn(n, 3, generator=g)

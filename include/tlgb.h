@@ -156,6 +156,43 @@ int tlgb_unfold(const tlgb_blocks_desc* d, const void* array, void* blocks, tlgb
  * from zero -- deterministic; every element of `array` is written. */
 int tlgb_fold(const tlgb_blocks_desc* d, const void* blocks, void* array, tlgb_stream_t stream);
 
+/* ------------------------------------------------------------------------ */
+/* Conjugate gradients with float64 scalars.                                   */
+/* Replaces the complex64/float32 zdot and alpha/beta of the reference CG loop */
+/* (alg/pcg.py:67-87; inner product utils/_adjoint_helpers.py:8).              */
+/* ------------------------------------------------------------------------ */
+
+/* Slots of the float64 CG state vector (device, TLGB_CG_STATE_LEN doubles). */
+enum {
+  TLGB_CG_RS = 0,      /* |r|^2 of the current residual            */
+  TLGB_CG_RS_OLD = 1,  /* |r|^2 of the previous residual           */
+  TLGB_CG_PAP = 2,     /* Re <p, A p>                               */
+  TLGB_CG_ALPHA = 3,   /* last step length                          */
+  TLGB_CG_BETA = 4,    /* last direction update                     */
+  TLGB_CG_ITERS = 5,   /* iterations taken                          */
+  TLGB_CG_TMP = 6,     /* two doubles of scratch (re, im of a dot)  */
+  TLGB_CG_STATE_LEN = 8
+};
+
+/* Device scratch bytes the calls below need. */
+size_t tlgb_cg_scratch_bytes(void);
+
+/* out[0] + i out[1] = sum_k conj(x_k) y_k (complex64 vectors as float pairs)
+ * or sum_k x_k y_k (float32), accumulated in float64 with a fixed reduction
+ * order (bit-identical for a given n). out is device memory. */
+int tlgb_dot_f64(const float* x, const float* y, int64_t n, int is_complex, double* out, void* scratch,
+                 size_t scratch_bytes, tlgb_stream_t stream);
+
+/* state[TLGB_CG_PAP] = Re <p, Ap> in float64. */
+int tlgb_cg_set_pap(const float* p, const float* ap, int64_t n, int is_complex, double* state, void* scratch,
+                    size_t scratch_bytes, tlgb_stream_t stream);
+
+/* One CG update with alpha = state[RS] / state[PAP]:  x += alpha p,
+ * r -= alpha Ap, state[RS] = |r|^2 (float64), beta = RS / RS_OLD,
+ * p = r + beta p. No host synchronisation. */
+int tlgb_cg_step(float* x, float* r, float* p, const float* ap, int64_t n, int is_complex, double* state,
+                 void* scratch, size_t scratch_bytes, tlgb_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

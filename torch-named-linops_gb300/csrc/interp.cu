@@ -337,15 +337,119 @@ __device__ __forceinline__ float radial_w(const Geo& g, float a0, float a1, floa
 
 __device__ __forceinline__ int lg2i(int v) { return 31 - __clz(v); }
 
+// ------------------------------------------------- lane-per-point taps
+
+// Per point tap data staged in shared memory: start coordinate (wrapped for
+// circular padding), number of valid taps and their per-dim values (the 1D
+// weight for norm 1, |d| for norm 2) per internal dim.
+template <int NTB>
+struct Pt {
+  int st[3];
+  int n[3];
+  float w[3][NTB];
+};
+
+// One lane evaluates all taps of point p into pt. Returns false when the
+// point has no valid tap (it then contributes nothing).
+template <int NTB>
+__device__ __forceinline__ bool lane_point_taps(const Geo& g, const float* __restrict__ locs, long long p,
+                                                const float (&x3)[3], Pt<NTB>& pt) {
+  for (int e = 0; e < 3; ++e) {
+    if (!g.act[e]) {
+      pt.st[e] = 0;
+      pt.n[e] = 1;
+      pt.w[e][0] = g.norm == 1 ? 1.f : 0.f;
+      continue;
+    }
+    const float x = x3[e];
+    if (!coord_ok(x)) return false;
+    const int lower = lower_of(g, e, x);
+    int s = -1, cnt = 0;
+    for (int k = 0; k < g.NT[e]; ++k) {
+      const Tap t = tap_eval(g, e, x, lower, k);
+      if (t.valid) {
+        if (s < 0) s = k;
+        const float ad = fabsf(t.d);
+        pt.w[e][cnt] = g.norm == 1 ? kern_value(g.kernel, ad, g.beta) : ad;
+        ++cnt;
+      }
+    }
+    if (cnt == 0) return false;
+    int st = lower + s;
+    if (g.pad == TLGB_PAD_CIRCULAR) st = wrapi(st, g.N[e]);
+    pt.st[e] = st;
+    pt.n[e] = cnt;
+  }
+  return true;
+}
+
+// N floats moved as one vector (a "coil unit": 1 or 2 batch entries)
+template <int N>
+struct VecF {
+  float v[N];
+};
+template <int N>
+__device__ __forceinline__ VecF<N> ldv(const float* p) {
+  VecF<N> r;
+  if constexpr (N == 4) {
+    const float4 t = *reinterpret_cast<const float4*>(p);
+    r.v[0] = t.x; r.v[1] = t.y; r.v[2] = t.z; r.v[3] = t.w;
+  } else if constexpr (N == 2) {
+    const float2 t = *reinterpret_cast<const float2*>(p);
+    r.v[0] = t.x; r.v[1] = t.y;
+  } else {
+    r.v[0] = *p;
+  }
+  return r;
+}
+template <int N>
+__device__ __forceinline__ void stv(float* p, const VecF<N>& r) {
+  if constexpr (N == 4) {
+    *reinterpret_cast<float4*>(p) = make_float4(r.v[0], r.v[1], r.v[2], r.v[3]);
+  } else if constexpr (N == 2) {
+    *reinterpret_cast<float2*>(p) = make_float2(r.v[0], r.v[1]);
+  } else {
+    *p = r.v[0];
+  }
+}
+
+// weight of one tap combination of a staged point
+template <int NTB>
+__device__ __forceinline__ float tap_w(const Geo& g, const Pt<NTB>& P, int kx, int ky, int kz) {
+  if (g.norm == 1) return P.w[0][kx] * P.w[1][ky] * P.w[2][kz];
+  return radial_w(g, P.w[0][kx], P.w[1][ky], P.w[2][kz]);
+}
+
+// Lane roles: lane = (ux, uz, cu); cu indexes coil units (lowest bits), uz
+// the tap along z (4 slots), ux the tap along the split dim (x in 3D, y in
+// 2D, more z slots in 1D).
+struct Lanes {
+  int cu, uz, ux, NUP, UX, lgn;
+};
+__device__ __forceinline__ Lanes lane_roles(int lane, int nunits) {
+  Lanes L;
+  L.NUP = nunits <= 1 ? 1 : (nunits <= 2 ? 2 : (nunits <= 4 ? 4 : 8));
+  L.lgn = lg2i(L.NUP);
+  L.cu = lane & (L.NUP - 1);
+  L.uz = (lane >> L.lgn) & 3;
+  L.ux = lane >> (L.lgn + 2);
+  L.UX = 8 >> L.lgn;
+  return L;
+}
+
 // ------------------------------------------------------------------ forward
 
-template <typename V, int NORM>
-__global__ void __launch_bounds__(NTHR, 2) interp_fwd_kernel(Geo g, const int4* __restrict__ items,
+// CTA = 8 warps sharing one staged region (tile + halo, [x][y][z][batch]);
+// each warp interpolates 32 home points per batch.
+template <int N, int NDIM, int NTB, int NW>
+__global__ void __launch_bounds__(NW * 32, 1) interp_fwd_kernel(Geo g, const int4* __restrict__ items,
                                                              const int32_t* __restrict__ entries,
                                                              const float* __restrict__ locs,
-                                                             const V* __restrict__ gridv, V* __restrict__ out,
-                                                             int CG) {
+                                                             const float* __restrict__ gridv,
+                                                             float* __restrict__ out, int CG) {
   extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int ES = N == 4 ? 2 : N;  // floats per batch entry: complex units are (re, im) pairs
+  const int es = g.cplx ? 2 : 1;
   const int4 it = items[blockIdx.x];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int c0 = blockIdx.y * CG;
@@ -363,86 +467,137 @@ __global__ void __launch_bounds__(NTHR, 2) interp_fwd_kernel(Geo g, const int4* 
     o[e] = tc[e] * g.T[e];
     S[e] = g.T[e] + g.NT[e] - 1;
   }
-  const int vol = S[0] * S[1] * S[2];
-  V* reg = reinterpret_cast<V*>(smem);
-  PointTaps* ptb = reinterpret_cast<PointTaps*>(smem + (size_t)vol * CG * sizeof(V));
-  PointTaps& pt = ptb[warp];
+  const int vstride = CG * es;  // floats per staged voxel
+  float* reg = reinterpret_cast<float*>(smem);
+  Pt<NTB>* pbuf = reinterpret_cast<Pt<NTB>*>(smem + (size_t)S[0] * S[1] * S[2] * vstride * sizeof(float)) + warp * 32;
 
-  // stage tile + halo: z fastest in global memory, batch fastest in shared
+  // stage: rows (x, y) per warp, lanes over (z, batch entry), batch fastest
   const long long gvol = (long long)g.N[0] * g.N[1] * g.N[2];
-  for (int i = threadIdx.x; i < vol * ncoil; i += NTHR) {
-    int z = i % S[2];
-    int r = i / S[2];
-    const int y = r % S[1];
-    r /= S[1];
-    const int x = r % S[0];
-    const int c = r / S[0];
-    int gx = o[0] + x, gy = o[1] + y, gz = o[2] + z;
-    V v = VT<V>::zero();
-    bool in = true;
+  const int cgp = CG <= 1 ? 1 : (CG <= 2 ? 2 : (CG <= 4 ? 4 : 8));
+  const int lgc = lg2i(cgp);
+  for (int row = warp; row < S[0] * S[1]; row += NW) {
+    const int x = row / S[1], y = row - (row / S[1]) * S[1];
+    int gx = o[0] + x, gy = o[1] + y;
+    bool rin = true;
     if (g.pad == TLGB_PAD_CIRCULAR) {
       gx = wrapi(gx, g.N[0]);
       gy = wrapi(gy, g.N[1]);
-      gz = wrapi(gz, g.N[2]);
     } else {
-      in = gx < g.N[0] && gy < g.N[1] && gz < g.N[2];
+      rin = gx < g.N[0] && gy < g.N[1];
     }
-    if (in) v = __ldg(gridv + (long long)(c0 + c) * gvol + ((long long)gx * g.N[1] + gy) * g.N[2] + gz);
-    reg[((x * S[1] + y) * S[2] + z) * CG + c] = v;
+    const long long rbase = ((long long)gx * g.N[1] + gy) * g.N[2];
+    float* rdst = reg + (size_t)(x * S[1] + y) * S[2] * vstride;
+    for (int idx = lane; idx < S[2] * cgp; idx += 32) {
+      const int c = idx & (cgp - 1), z = idx >> lgc;
+      if (c >= CG) continue;
+      int gz = o[2] + z;
+      bool in = rin && c < ncoil;
+      if (g.pad == TLGB_PAD_CIRCULAR) gz = wrapi(gz, g.N[2]);
+      else in = in && gz < g.N[2];
+      float* d = rdst + z * vstride + c * es;
+      if (es == 2) {
+        float2 v = make_float2(0.f, 0.f);
+        if (in) v = __ldg(reinterpret_cast<const float2*>(gridv) + (long long)(c0 + c) * gvol + rbase + gz);
+        *reinterpret_cast<float2*>(d) = v;
+      } else {
+        d[0] = in ? __ldg(gridv + (long long)(c0 + c) * gvol + rbase + gz) : 0.f;
+      }
+    }
   }
   __syncthreads();
 
-  const int CGP = CG <= 1 ? 1 : (CG <= 2 ? 2 : (CG <= 4 ? 4 : 8));
-  const int lgc = lg2i(CGP);
-  const int c = lane & (CGP - 1);
-  const int q = lane >> lgc;
-  const int QN = 32 >> lgc;
-  for (int ei = it.y + warp; ei < it.z; ei += NWARP) {
-    const long long p = entries[ei];
-    if (!warp_point_taps<NORM, false>(g, locs, p, pt, lane)) continue;  // never for home pairs
-    int l[3];
-    for (int e = 0; e < 3; ++e) l[e] = pt.start[e] - o[e];
-    V acc = VT<V>::zero();
-    for (int ka = 0; ka < pt.n[0]; ++ka) {
-      for (int kb = 0; kb < pt.n[1]; ++kb) {
-        const V* row = reg + (((l[0] + ka) * S[1] + (l[1] + kb)) * S[2] + l[2]) * CG + c;
-        if (NORM == 1) {
-          const float wab = pt.w[0][ka] * pt.w[1][kb];
-          for (int kc = q; kc < pt.n[2]; kc += QN) {
-            const float w = wab * pt.w[2][kc];
-            if (c < ncoil) VT<V>::fma(acc, w, row[kc * CG]);
+  const int U = N / ES;                     // batch entries per unit
+  const int nunits = (CG + U - 1) / U;
+  const Lanes L = lane_roles(lane, nunits);
+  const int ndo = g.ndim;  // unused except to keep NDIM-specific code uniform
+  (void)ndo;
+  for (int b = it.y + warp * 32; b < it.z; b += NW * 32) {
+    const int j = b + lane;
+    const int nb = min(32, it.z - b);
+    long long p = -1;
+    if (j < it.z) {
+      p = entries[j];
+      float x3[3];
+      for (int e = 0; e < 3; ++e) x3[e] = g.act[e] ? load_coord(g, locs, p, e) : 0.f;
+      if (!lane_point_taps<NTB>(g, locs, p, x3, pbuf[lane])) pbuf[lane].n[0] = 0;
+    }
+    __syncwarp();
+    for (int jj = 0; jj < nb; ++jj) {
+      const Pt<NTB>& P = pbuf[jj];
+      const long long pj = __shfl_sync(0xffffffffu, p, jj);
+      if (P.n[0] == 0) continue;  // warp-uniform
+      const int l0 = P.st[0] - o[0], l1 = P.st[1] - o[1], l2 = P.st[2] - o[2];
+      VecF<N> acc;
+#pragma unroll
+      for (int i = 0; i < N; ++i) acc.v[i] = 0.f;
+      if (L.cu < nunits) {
+        if constexpr (NDIM == 3) {
+          for (int kx = L.ux; kx < P.n[0]; kx += L.UX)
+            for (int ky = 0; ky < P.n[1]; ++ky) {
+              const float* rowp = reg + ((size_t)((l0 + kx) * S[1] + (l1 + ky)) * S[2] + l2) * vstride + L.cu * N;
+              for (int kz = L.uz; kz < P.n[2]; kz += 4) {
+                const float w = tap_w(g, P, kx, ky, kz);
+                const VecF<N> v = ldv<N>(rowp + kz * vstride);
+#pragma unroll
+                for (int i = 0; i < N; ++i) acc.v[i] = fmaf(w, v.v[i], acc.v[i]);
+              }
+            }
+        } else if constexpr (NDIM == 2) {
+          for (int ky = L.ux; ky < P.n[1]; ky += L.UX) {
+            const float* rowp = reg + ((size_t)(l1 + ky) * S[2] + l2) * vstride + L.cu * N;
+            for (int kz = L.uz; kz < P.n[2]; kz += 4) {
+              const float w = tap_w(g, P, 0, ky, kz);
+              const VecF<N> v = ldv<N>(rowp + kz * vstride);
+#pragma unroll
+              for (int i = 0; i < N; ++i) acc.v[i] = fmaf(w, v.v[i], acc.v[i]);
+            }
           }
         } else {
-          for (int kc = q; kc < pt.n[2]; kc += QN) {
-            const float w = radial_w(g, pt.w[0][ka], pt.w[1][kb], pt.w[2][kc]);
-            if (c < ncoil) VT<V>::fma(acc, w, row[kc * CG]);
+          const float* rowp = reg + (size_t)l2 * vstride + L.cu * N;
+          for (int kz = L.uz + 4 * L.ux; kz < P.n[2]; kz += 4 * L.UX) {
+            const float w = tap_w(g, P, 0, 0, kz);
+            const VecF<N> v = ldv<N>(rowp + kz * vstride);
+#pragma unroll
+            for (int i = 0; i < N; ++i) acc.v[i] = fmaf(w, v.v[i], acc.v[i]);
+          }
+        }
+      }
+      for (int m = L.NUP; m < 32; m <<= 1)
+#pragma unroll
+        for (int i = 0; i < N; ++i) acc.v[i] += __shfl_xor_sync(0xffffffffu, acc.v[i], m);
+      if (lane < L.NUP && L.cu < nunits) {
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int c = L.cu * U + u;
+          if (c < ncoil) {
+            float* dst = out + ((long long)(c0 + c) * g.npts + pj) * es;
+            if (es == 2)
+              *reinterpret_cast<float2*>(dst) = make_float2(acc.v[u * ES], acc.v[u * ES + 1]);
+            else
+              dst[0] = acc.v[u];
           }
         }
       }
     }
-    for (int m = CGP; m < 32; m <<= 1) VT<V>::add(acc, VT<V>::shfl_xor(acc, m));
-    if (q == 0 && c < ncoil) out[(long long)(c0 + c) * g.npts + p] = acc;
     __syncwarp();
   }
 }
 
 // ------------------------------------------------------------------ adjoint
 
-template <typename V>
-struct AdjPoint {
-  PointTaps t;
-  V v[CGMAX];
-};
-
-template <typename V, int NORM>
-__global__ void __launch_bounds__(NTHR) interp_adj_kernel(Geo g, const int4* __restrict__ items,
-                                                          const int32_t* __restrict__ entries,
-                                                          const float* __restrict__ locs,
-                                                          const V* __restrict__ vals, V* __restrict__ gridv,
-                                                          V* __restrict__ partial, int CG) {
+// One warp per CTA owns one output tile in shared memory ([x][y][z][batch]),
+// so every cell is updated by one warp in plan order: deterministic.
+template <int N, int NDIM, int NTB>
+__global__ void __launch_bounds__(32) interp_adj_kernel(Geo g, const int4* __restrict__ items,
+                                                        const int32_t* __restrict__ entries,
+                                                        const float* __restrict__ locs,
+                                                        const float* __restrict__ vals, float* __restrict__ gridv,
+                                                        float* __restrict__ partial, int CG) {
   extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int ES = N == 4 ? 2 : N;
+  const int es = g.cplx ? 2 : 1;
   const int4 it = items[blockIdx.x];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int lane = threadIdx.x;
   const int cg = blockIdx.y;
   const int c0 = cg * CG;
   const int ncoil = (int)min((long long)CG, g.nbatch - c0);
@@ -457,106 +612,184 @@ __global__ void __launch_bounds__(NTHR) interp_adj_kernel(Geo g, const int4* __r
   int o[3];
   for (int e = 0; e < 3; ++e) o[e] = tc[e] * g.T[e];
   const int tvol = g.T[0] * g.T[1] * g.T[2];
-  V* acc = reinterpret_cast<V*>(smem);
-  AdjPoint<V>* pb = reinterpret_cast<AdjPoint<V>*>(smem + (size_t)tvol * CG * sizeof(V));
-  for (int i = threadIdx.x; i < tvol * CG; i += NTHR) acc[i] = VT<V>::zero();
+  const int vstride = CG * es;
+  const int tfl = (tvol * vstride + 3) & ~3;  // tile floats, rounded to whole float4
+  float* acc = reinterpret_cast<float*>(smem);
+  Pt<NTB>* pbuf = reinterpret_cast<Pt<NTB>*>(smem + (size_t)tfl * sizeof(float));
+  float* pv = reinterpret_cast<float*>(pbuf + 32);  // [32][vstride]
+  for (int i = lane * 4; i < tfl; i += 128) *reinterpret_cast<float4*>(acc + i) = make_float4(0.f, 0.f, 0.f, 0.f);
 
-  const int CGP = CG <= 1 ? 1 : (CG <= 2 ? 2 : (CG <= 4 ? 4 : 8));
-  const int lgc = lg2i(CGP);
-  const int c = lane & (CGP - 1);
-  const int q = lane >> lgc;
-  const int QN = 32 >> lgc;
-  // ownership: outer active dim; 1D grids use runs of 64 cells
-  const int od = 3 - g.ndim;
-  const int og = g.ndim == 1 ? 64 : 1;
+  const int U = N / ES;
+  const int nunits = (CG + U - 1) / U;
+  const Lanes L = lane_roles(lane, nunits);
 
-  for (int b = it.y; b < it.z; b += PB) {
-    const int nb = min(PB, it.z - b);
-    __syncthreads();
-    for (int j = warp; j < nb; j += NWARP) {
-      const long long p = entries[b + j];
-      AdjPoint<V>& P = pb[j];
-      if (!warp_point_taps<NORM, false>(g, locs, p, P.t, lane)) {
-        if (lane == 0) P.t.n[0] = 0;  // no valid tap: contributes nothing
-      }
-      if (lane < ncoil) P.v[lane] = __ldg(vals + (long long)(c0 + lane) * g.npts + p);
-    }
-    __syncthreads();
-    for (int j = 0; j < nb; ++j) {
-      const AdjPoint<V>& P = pb[j];
-      const V v = c < ncoil ? P.v[c] : VT<V>::zero();
-      for (int ka = 0; ka < P.t.n[0]; ++ka) {
-        int ga = P.t.start[0] + ka;
-        if (ga >= g.N[0]) ga = wrapi(ga, g.N[0]);
-        const int la = ga - o[0];
-        if (la < 0 || la >= g.T[0]) continue;
-        if (od == 0 && (la % NWARP) != warp) continue;
-        for (int kb = 0; kb < P.t.n[1]; ++kb) {
-          int gb = P.t.start[1] + kb;
-          if (gb >= g.N[1]) gb = wrapi(gb, g.N[1]);
-          const int lb = gb - o[1];
-          if (lb < 0 || lb >= g.T[1]) continue;
-          if (od == 1 && (lb % NWARP) != warp) continue;
-          V* row = acc + (la * g.T[1] + lb) * g.T[2] * CG + c;
-          const float wab = NORM == 1 ? P.t.w[0][ka] * P.t.w[1][kb] : 0.f;
-          if (g.wrap_safe) {
-            for (int kc = q; kc < P.t.n[2]; kc += QN) {
-              int gc = P.t.start[2] + kc;
-              if (gc >= g.N[2]) gc = wrapi(gc, g.N[2]);
-              const int lc = gc - o[2];
-              if (lc < 0 || lc >= g.T[2] || c >= ncoil) continue;
-              if (od == 2 && ((lc / og) % NWARP) != warp) continue;
-              const float w = NORM == 1 ? wab * P.t.w[2][kc] : radial_w(g, P.t.w[0][ka], P.t.w[1][kb], P.t.w[2][kc]);
-              VT<V>::fma(row[lc * CG], w, v);
-            }
+  // prefetch registers for the next batch
+  long long np_ = -1;
+  float nx3[3] = {0.f, 0.f, 0.f};
+  float nv[2 * CGMAX];
+  auto prefetch = [&](int b) {
+    const int j = b + lane;
+    np_ = -1;
+    if (j < it.z) {
+      np_ = entries[j];
+      for (int e = 0; e < 3; ++e) nx3[e] = g.act[e] ? load_coord(g, locs, np_, e) : 0.f;
+#pragma unroll
+      for (int c = 0; c < CGMAX; ++c) {
+        if (c < ncoil) {
+          if (es == 2) {
+            const float2 v = __ldg(reinterpret_cast<const float2*>(vals) + (long long)(c0 + c) * g.npts + np_);
+            nv[2 * c] = v.x;
+            nv[2 * c + 1] = v.y;
           } else {
-            // a window longer than the grid hits a cell more than once:
-            // taps in sequence, lanes split by batch entry only
-            if (q == 0 && c < ncoil) {
-              for (int kc = 0; kc < P.t.n[2]; ++kc) {
-                const int gc = wrapi(P.t.start[2] + kc, g.N[2]);
-                const int lc = gc - o[2];
-                if (lc < 0 || lc >= g.T[2]) continue;
-                if (od == 2 && ((lc / og) % NWARP) != warp) continue;
-                const float w = NORM == 1 ? wab * P.t.w[2][kc] : radial_w(g, P.t.w[0][ka], P.t.w[1][kb], P.t.w[2][kc]);
-                VT<V>::fma(row[lc * CG], w, v);
+            nv[c] = __ldg(vals + (long long)(c0 + c) * g.npts + np_);
+          }
+        }
+      }
+    }
+  };
+  if (it.y < it.z) prefetch(it.y);
+  for (int b = it.y; b < it.z; b += 32) {
+    const int nb = min(32, it.z - b);
+    __syncwarp();
+    if (np_ >= 0) {
+      if (!lane_point_taps<NTB>(g, locs, np_, nx3, pbuf[lane])) pbuf[lane].n[0] = 0;
+#pragma unroll
+      for (int c = 0; c < CGMAX; ++c)
+        if (c < ncoil) {
+          if (es == 2) {
+            pv[lane * vstride + 2 * c] = nv[2 * c];
+            pv[lane * vstride + 2 * c + 1] = nv[2 * c + 1];
+          } else {
+            pv[lane * vstride + c] = nv[c];
+          }
+        }
+    }
+    __syncwarp();
+    if (b + 32 < it.z) prefetch(b + 32);
+    for (int jj = 0; jj < nb; ++jj) {
+      const Pt<NTB>& P = pbuf[jj];
+      // lanes of one warp update cells of consecutive points: order them
+      __syncwarp();
+      if (P.n[0] == 0 || L.cu >= nunits) continue;
+      VecF<N> v;
+      {
+        const float* src = pv + jj * vstride + L.cu * N;
+#pragma unroll
+        for (int i = 0; i < N; ++i) v.v[i] = (L.cu * U + i / ES < ncoil) ? src[i] : 0.f;
+      }
+      if (!g.wrap_safe) {
+        // a window longer than the grid reaches a cell twice: taps in order, lanes by coil unit only
+        if (L.ux == 0 && L.uz == 0) {
+          for (int kx = 0; kx < P.n[0]; ++kx)
+            for (int ky = 0; ky < P.n[1]; ++ky)
+              for (int kz = 0; kz < P.n[2]; ++kz) {
+                const int lx = wrapi(P.st[0] + kx, g.N[0]) - o[0], ly = wrapi(P.st[1] + ky, g.N[1]) - o[1],
+                          lz = wrapi(P.st[2] + kz, g.N[2]) - o[2];
+                if (lx < 0 || lx >= g.T[0] || ly < 0 || ly >= g.T[1] || lz < 0 || lz >= g.T[2]) continue;
+                const float w = tap_w(g, P, kx, ky, kz);
+                float* a = acc + ((size_t)(lx * g.T[1] + ly) * g.T[2] + lz) * vstride + L.cu * N;
+                VecF<N> r = ldv<N>(a);
+#pragma unroll
+                for (int i = 0; i < N; ++i) r.v[i] = fmaf(w, v.v[i], r.v[i]);
+                stv<N>(a, r);
               }
+        }
+        continue;
+      }
+      // taps of this lane; wrap by one subtraction (N >= taps)
+      auto tap_local = [&](int e, int k) {
+        int gg = P.st[e] + k;
+        if (gg >= g.N[e]) gg -= g.N[e];
+        return gg - o[e];
+      };
+      if constexpr (NDIM == 3) {
+        for (int kx = L.ux; kx < P.n[0]; kx += L.UX) {
+          const int lx = tap_local(0, kx);
+          if (lx < 0 || lx >= g.T[0]) continue;
+          for (int ky = 0; ky < P.n[1]; ++ky) {
+            const int ly = tap_local(1, ky);
+            if (ly < 0 || ly >= g.T[1]) continue;
+            for (int kz = L.uz; kz < P.n[2]; kz += 4) {
+              const int lz = tap_local(2, kz);
+              if (lz < 0 || lz >= g.T[2]) continue;
+              const float w = tap_w(g, P, kx, ky, kz);
+              float* a = acc + ((size_t)(lx * g.T[1] + ly) * g.T[2] + lz) * vstride + L.cu * N;
+              VecF<N> r = ldv<N>(a);
+#pragma unroll
+              for (int i = 0; i < N; ++i) r.v[i] = fmaf(w, v.v[i], r.v[i]);
+              stv<N>(a, r);
             }
           }
-          __syncwarp();
+        }
+      } else if constexpr (NDIM == 2) {
+        for (int ky = L.ux; ky < P.n[1]; ky += L.UX) {
+          const int ly = tap_local(1, ky);
+          if (ly < 0 || ly >= g.T[1]) continue;
+          for (int kz = L.uz; kz < P.n[2]; kz += 4) {
+            const int lz = tap_local(2, kz);
+            if (lz < 0 || lz >= g.T[2]) continue;
+            const float w = tap_w(g, P, 0, ky, kz);
+            float* a = acc + ((size_t)ly * g.T[2] + lz) * vstride + L.cu * N;
+            VecF<N> r = ldv<N>(a);
+#pragma unroll
+            for (int i = 0; i < N; ++i) r.v[i] = fmaf(w, v.v[i], r.v[i]);
+            stv<N>(a, r);
+          }
+        }
+      } else {
+        for (int kz = L.uz + 4 * L.ux; kz < P.n[2]; kz += 4 * L.UX) {
+          const int lz = tap_local(2, kz);
+          if (lz < 0 || lz >= g.T[2]) continue;
+          const float w = tap_w(g, P, 0, 0, kz);
+          float* a = acc + (size_t)lz * vstride + L.cu * N;
+          VecF<N> r = ldv<N>(a);
+#pragma unroll
+          for (int i = 0; i < N; ++i) r.v[i] = fmaf(w, v.v[i], r.v[i]);
+          stv<N>(a, r);
         }
       }
     }
   }
-  __syncthreads();
+  __syncwarp();
   if (it.w >= 0) {
-    V* dst = partial + ((long long)it.w * gridDim.y + cg) * tvol * CG;
-    for (int i = threadIdx.x; i < tvol * CG; i += NTHR) dst[i] = acc[i];
+    float* dst = partial + ((long long)it.w * gridDim.y + cg) * tfl;
+    for (int i = lane * 4; i < tfl; i += 128)
+      *reinterpret_cast<float4*>(dst + i) = *reinterpret_cast<const float4*>(acc + i);
     return;
   }
+  // write the tile: per (x, y) row, lanes over (z, batch entry), z fastest
   const long long gvol = (long long)g.N[0] * g.N[1] * g.N[2];
-  for (int i = threadIdx.x; i < tvol * ncoil; i += NTHR) {
-    const int z = i % g.T[2];
-    int r = i / g.T[2];
-    const int y = r % g.T[1];
-    r /= g.T[1];
-    const int x = r % g.T[0];
-    const int cc = r / g.T[0];
-    const int gx = o[0] + x, gy = o[1] + y, gz = o[2] + z;
-    if (gx >= g.N[0] || gy >= g.N[1] || gz >= g.N[2]) continue;
-    gridv[(long long)(c0 + cc) * gvol + ((long long)gx * g.N[1] + gy) * g.N[2] + gz] =
-        acc[((x * g.T[1] + y) * g.T[2] + z) * CG + cc];
+  const int T2 = g.T[2];
+  const bool p2 = (T2 & (T2 - 1)) == 0;
+  const int lg2 = lg2i(T2);
+  for (int row = 0; row < g.T[0] * g.T[1]; ++row) {
+    const int x = row / g.T[1], y = row - x * g.T[1];
+    const int gx = o[0] + x, gy = o[1] + y;
+    if (gx >= g.N[0] || gy >= g.N[1]) continue;
+    const float* srow = acc + (size_t)(x * g.T[1] + y) * T2 * vstride;
+    float* drow = gridv + (((long long)gx * g.N[1] + gy) * g.N[2] + o[2]) * es;
+    for (int idx = lane; idx < T2 * ncoil; idx += 32) {
+      const int cc = p2 ? (idx >> lg2) : idx / T2;
+      const int z = idx - cc * T2;
+      if (o[2] + z >= g.N[2]) continue;
+      const float* sp = srow + z * vstride + cc * es;
+      float* d = drow + ((long long)(c0 + cc) * gvol + z) * es;
+      if (es == 2)
+        *reinterpret_cast<float2*>(d) = *reinterpret_cast<const float2*>(sp);
+      else
+        d[0] = sp[0];
+    }
   }
 }
 
 // Sum the partial tiles of one split tile in slot order and write it out.
-template <typename V>
 __global__ void __launch_bounds__(NTHR) adj_reduce_kernel(Geo g, const int4* __restrict__ split,
-                                                          const V* __restrict__ partial, V* __restrict__ gridv,
-                                                          int CG, int ncg) {
+                                                          const float* __restrict__ partial,
+                                                          float* __restrict__ gridv, int CG, int ncg) {
   const int4 sp = split[blockIdx.x];
   const int cg = blockIdx.y;
   const int c0 = cg * CG;
+  const int es = g.cplx ? 2 : 1;
   const int ncoil = (int)min((long long)CG, g.nbatch - c0);
   int tc[3];
   {
@@ -567,20 +800,24 @@ __global__ void __launch_bounds__(NTHR) adj_reduce_kernel(Geo g, const int4* __r
     tc[0] = t / g.nt[1];
   }
   const int tvol = g.T[0] * g.T[1] * g.T[2];
+  const int vstride = CG * es;
+  const int tfl = (tvol * vstride + 3) & ~3;
   const long long gvol = (long long)g.N[0] * g.N[1] * g.N[2];
-  for (int i = threadIdx.x; i < tvol * ncoil; i += NTHR) {
-    const int z = i % g.T[2];
-    int r = i / g.T[2];
+  for (int i = threadIdx.x; i < tvol * ncoil * es; i += NTHR) {
+    const int f = i % es;
+    int r = i / es;
+    const int z = r % g.T[2];
+    r /= g.T[2];
     const int y = r % g.T[1];
     r /= g.T[1];
     const int x = r % g.T[0];
     const int cc = r / g.T[0];
     const int gx = tc[0] * g.T[0] + x, gy = tc[1] * g.T[1] + y, gz = tc[2] * g.T[2] + z;
     if (gx >= g.N[0] || gy >= g.N[1] || gz >= g.N[2]) continue;
-    const int li = ((x * g.T[1] + y) * g.T[2] + z) * CG + cc;
-    V s = partial[((long long)sp.y * ncg + cg) * tvol * CG + li];
-    for (int k = 1; k < sp.z; ++k) VT<V>::add(s, partial[((long long)(sp.y + k) * ncg + cg) * tvol * CG + li]);
-    gridv[(long long)(c0 + cc) * gvol + ((long long)gx * g.N[1] + gy) * g.N[2] + gz] = s;
+    const int li = ((x * g.T[1] + y) * g.T[2] + z) * vstride + cc * es + f;
+    float s = partial[((long long)sp.y * ncg + cg) * tfl + li];
+    for (int k = 1; k < sp.z; ++k) s += partial[((long long)(sp.y + k) * ncg + cg) * tfl + li];
+    gridv[((long long)(c0 + cc) * gvol + ((long long)gx * g.N[1] + gy) * g.N[2] + gz) * es + f] = s;
   }
 }
 
@@ -819,26 +1056,52 @@ PlanLayout layout(const Geo& g) {
 
 int value_size(const Geo& g) { return g.cplx ? 8 : 4; }
 
-// batch entries staged per CTA: as many as fit two CTAs per SM
-int fwd_cg(const Geo& g, size_t taps_bytes) {
+constexpr int NWF = 16;  // warps of a forward CTA (one CTA per SM shares one staged region)
+
+// taps stored per dim by the kernels: 5 covers widths < 4 (the NUFFT default)
+int ntb_for(const Geo& g) {
+  const int m = std::max(g.NT[0], std::max(g.NT[1], g.NT[2]));
+  if (m <= 5) return 5;
+  return g.ndim == 3 ? 9 : 16;
+}
+size_t pt_bytes(int ntb) { return 24 + 12 * (size_t)ntb; }
+
+int64_t region_vol(const Geo& g) {
+  return (int64_t)(g.T[0] + g.NT[0] - 1) * (g.T[1] + g.NT[1] - 1) * (g.T[2] + g.NT[2] - 1);
+}
+
+// batch entries staged per forward CTA
+int fwd_cg(const Geo& g) {
   int cg = (int)std::min<long long>(std::max<long long>(g.nbatch, 1), CGMAX);
-  const int64_t vol = (int64_t)(g.T[0] + g.NT[0] - 1) * (g.T[1] + g.NT[1] - 1) * (g.T[2] + g.NT[2] - 1);
-  const int64_t cap = 112 * 1024 - NWARP * (int64_t)taps_bytes - 1024;
-  while (cg > 1 && vol * cg * value_size(g) > cap) --cg;
+  const int64_t cap = 220 * 1024 - NWF * 32 * (int64_t)pt_bytes(ntb_for(g));
+  while (cg > 1 && region_vol(g) * cg * value_size(g) > cap) --cg;
   return cg;
 }
 
-size_t fwd_smem(const Geo& g, int cg, size_t taps_bytes) {
-  const int64_t vol = (int64_t)(g.T[0] + g.NT[0] - 1) * (g.T[1] + g.NT[1] - 1) * (g.T[2] + g.NT[2] - 1);
-  return (size_t)vol * cg * value_size(g) + NWARP * taps_bytes;
+size_t fwd_smem(const Geo& g, int cg) {
+  return align_up((size_t)region_vol(g) * cg * value_size(g), 16) + NWF * 32 * pt_bytes(ntb_for(g));
 }
 
 int adj_cg(const Geo& g) { return (int)std::min<long long>(std::max<long long>(g.nbatch, 1), CGMAX); }
 
+int64_t tile_floats(const Geo& g, int cg) {
+  return ((int64_t)g.T[0] * g.T[1] * g.T[2] * cg * (g.cplx ? 2 : 1) + 3) & ~3ll;
+}
+
 size_t adj_smem(const Geo& g, int cg) {
-  const int64_t tvol = (int64_t)g.T[0] * g.T[1] * g.T[2];
-  const size_t pbs = g.cplx ? sizeof(AdjPoint<float2>) : sizeof(AdjPoint<float>);
-  return (size_t)tvol * cg * value_size(g) + PB * pbs;
+  return (size_t)tile_floats(g, cg) * 4 + 32 * pt_bytes(ntb_for(g)) + 32 * (size_t)cg * (g.cplx ? 2 : 1) * 4;
+}
+
+// the grad kernel keeps the warp-cooperative tap buffers
+int grad_cg(const Geo& g, size_t taps_bytes) {
+  int cg = (int)std::min<long long>(std::max<long long>(g.nbatch, 1), CGMAX);
+  const int64_t cap = 112 * 1024 - NWARP * (int64_t)taps_bytes - 1024;
+  while (cg > 1 && region_vol(g) * cg * value_size(g) > cap) --cg;
+  return cg;
+}
+
+size_t grad_smem(const Geo& g, int cg, size_t taps_bytes) {
+  return (size_t)region_vol(g) * cg * value_size(g) + NWARP * taps_bytes;
 }
 
 int check_plan(const Geo& g, const tlgb_interp_plan_info* info, const void* plan) {
@@ -977,54 +1240,93 @@ extern "C" int tlgb_interp_adjoint_scratch_size(const tlgb_interp_desc* d, const
   if (!info || !bytes) TLGB_FAIL(TLGB_ERR_INVALID, "null pointer");
   const int cg = adj_cg(g);
   const int64_t ncg = cdiv(std::max<long long>(g.nbatch, 1), cg);
-  *bytes = (size_t)info->n_partials * ncg * g.T[0] * g.T[1] * g.T[2] * cg * value_size(g);
+  *bytes = (size_t)info->n_partials * ncg * tile_floats(g, cg) * sizeof(float);
   return TLGB_OK;
 }
 
 namespace tlgb {
 namespace {
 
-template <typename V, int NORM>
-int launch_fwd(const Geo& g, const tlgb_interp_plan_info* info, const char* P, const float* locs, const void* grid,
-               void* out, cudaStream_t s) {
-  const int cg = fwd_cg(g, sizeof(PTaps<false>));
+template <int N, int NDIM, int NTB>
+int launch_fwd_t(const Geo& g, int cg, const tlgb_interp_plan_info* info, const char* P, const float* locs,
+                 const void* grid, void* out, cudaStream_t s) {
   const int64_t ncg = cdiv(g.nbatch, cg);
-  const size_t sm = fwd_smem(g, cg, sizeof(PTaps<false>));
-  auto* k = interp_fwd_kernel<V, NORM>;
+  const size_t sm = fwd_smem(g, cg);
+  auto* k = interp_fwd_kernel<N, NDIM, NTB, NWF>;
   TLGB_TRY(set_smem(k, sm));
   dim3 grd((unsigned)info->n_fwd_items, (unsigned)ncg);
-  k<<<grd, NTHR, sm, s>>>(g, (const int4*)(P + info->off_fwd_items), (const int32_t*)(P + info->off_entries), locs,
-                         (const V*)grid, (V*)out, cg);
+  k<<<grd, NWF * 32, sm, s>>>(g, (const int4*)(P + info->off_fwd_items), (const int32_t*)(P + info->off_entries),
+                             locs, (const float*)grid, (float*)out, cg);
   TLGB_CHECK_LAUNCH();
   return TLGB_OK;
 }
 
-template <typename V, int NORM>
-int launch_adj(const Geo& g, const tlgb_interp_plan_info* info, const char* P, const float* locs, const void* vals,
-               void* grid, void* scratch, cudaStream_t s) {
-  const int cg = adj_cg(g);
+template <int N, int NDIM, int NTB>
+int launch_adj_t(const Geo& g, int cg, const tlgb_interp_plan_info* info, const char* P, const float* locs,
+                 const void* vals, void* grid, void* scratch, cudaStream_t s) {
   const int64_t ncg = cdiv(g.nbatch, cg);
   const size_t sm = adj_smem(g, cg);
-  auto* k = interp_adj_kernel<V, NORM>;
+  auto* k = interp_adj_kernel<N, NDIM, NTB>;
   TLGB_TRY(set_smem(k, sm));
   dim3 grd((unsigned)info->n_adj_items, (unsigned)ncg);
-  k<<<grd, NTHR, sm, s>>>(g, (const int4*)(P + info->off_adj_items), (const int32_t*)(P + info->off_entries), locs,
-                         (const V*)vals, (V*)grid, (V*)scratch, cg);
+  k<<<grd, 32, sm, s>>>(g, (const int4*)(P + info->off_adj_items), (const int32_t*)(P + info->off_entries), locs,
+                       (const float*)vals, (float*)grid, (float*)scratch, cg);
   TLGB_CHECK_LAUNCH();
   if (info->n_split_tiles > 0) {
     dim3 g2((unsigned)info->n_split_tiles, (unsigned)ncg);
-    adj_reduce_kernel<V><<<g2, NTHR, 0, s>>>(g, (const int4*)(P + info->off_split), (const V*)scratch, (V*)grid, cg,
-                                             (int)ncg);
+    adj_reduce_kernel<<<g2, NTHR, 0, s>>>(g, (const int4*)(P + info->off_split), (const float*)scratch, (float*)grid,
+                                          cg, (int)ncg);
     TLGB_CHECK_LAUNCH();
   }
   return TLGB_OK;
 }
 
+// floats per coil unit: 2 batch entries per unit when the group size is even
+inline int unit_floats(const Geo& g, int cg) { return (g.cplx ? 2 : 1) * ((cg % 2 == 0) ? 2 : 1); }
+
+template <int NDIM, int NTB>
+int dispatch_fwd_n(const Geo& g, int cg, const tlgb_interp_plan_info* info, const char* P, const float* locs,
+                   const void* grid, void* out, cudaStream_t s) {
+  switch (unit_floats(g, cg)) {
+    case 4: return launch_fwd_t<4, NDIM, NTB>(g, cg, info, P, locs, grid, out, s);
+    case 2: return launch_fwd_t<2, NDIM, NTB>(g, cg, info, P, locs, grid, out, s);
+    default: return launch_fwd_t<1, NDIM, NTB>(g, cg, info, P, locs, grid, out, s);
+  }
+}
+
+template <int NDIM, int NTB>
+int dispatch_adj_n(const Geo& g, int cg, const tlgb_interp_plan_info* info, const char* P, const float* locs,
+                   const void* vals, void* grid, void* scratch, cudaStream_t s) {
+  switch (unit_floats(g, cg)) {
+    case 4: return launch_adj_t<4, NDIM, NTB>(g, cg, info, P, locs, vals, grid, scratch, s);
+    case 2: return launch_adj_t<2, NDIM, NTB>(g, cg, info, P, locs, vals, grid, scratch, s);
+    default: return launch_adj_t<1, NDIM, NTB>(g, cg, info, P, locs, vals, grid, scratch, s);
+  }
+}
+
+int launch_fwd(const Geo& g, const tlgb_interp_plan_info* info, const char* P, const float* locs, const void* grid,
+               void* out, cudaStream_t s) {
+  const int cg = fwd_cg(g);
+  const bool small = ntb_for(g) == 5;
+  if (g.ndim == 3) return small ? dispatch_fwd_n<3, 5>(g, cg, info, P, locs, grid, out, s) : dispatch_fwd_n<3, 9>(g, cg, info, P, locs, grid, out, s);
+  if (g.ndim == 2) return small ? dispatch_fwd_n<2, 5>(g, cg, info, P, locs, grid, out, s) : dispatch_fwd_n<2, 16>(g, cg, info, P, locs, grid, out, s);
+  return small ? dispatch_fwd_n<1, 5>(g, cg, info, P, locs, grid, out, s) : dispatch_fwd_n<1, 16>(g, cg, info, P, locs, grid, out, s);
+}
+
+int launch_adj(const Geo& g, const tlgb_interp_plan_info* info, const char* P, const float* locs, const void* vals,
+               void* grid, void* scratch, cudaStream_t s) {
+  const int cg = adj_cg(g);
+  const bool small = ntb_for(g) == 5;
+  if (g.ndim == 3) return small ? dispatch_adj_n<3, 5>(g, cg, info, P, locs, vals, grid, scratch, s) : dispatch_adj_n<3, 9>(g, cg, info, P, locs, vals, grid, scratch, s);
+  if (g.ndim == 2) return small ? dispatch_adj_n<2, 5>(g, cg, info, P, locs, vals, grid, scratch, s) : dispatch_adj_n<2, 16>(g, cg, info, P, locs, vals, grid, scratch, s);
+  return small ? dispatch_adj_n<1, 5>(g, cg, info, P, locs, vals, grid, scratch, s) : dispatch_adj_n<1, 16>(g, cg, info, P, locs, vals, grid, scratch, s);
+}
+
 template <typename V, int NORM>
 int launch_grad(const Geo& g, const tlgb_interp_plan_info* info, const char* P, const float* locs, const void* grid,
                 const void* a, float* grad, cudaStream_t s) {
-  const int cg = fwd_cg(g, sizeof(PTaps<true>));
-  const size_t sm = fwd_smem(g, cg, sizeof(PTaps<true>)) + kFwdChunk * 3 * sizeof(float);
+  const int cg = grad_cg(g, sizeof(PTaps<true>));
+  const size_t sm = grad_smem(g, cg, sizeof(PTaps<true>)) + kFwdChunk * 3 * sizeof(float);
   auto* k = interp_grad_kernel<V, NORM>;
   TLGB_TRY(set_smem(k, sm));
   k<<<(unsigned)info->n_fwd_items, NTHR, sm, s>>>(g, (const int4*)(P + info->off_fwd_items),
@@ -1049,9 +1351,7 @@ extern "C" int tlgb_interp_forward(const tlgb_interp_desc* d, const tlgb_interp_
     TLGB_CUDA(cudaMemsetAsync(out, 0, (size_t)g.nbatch * g.npts * value_size(g), s));
   if (info->n_fwd_items == 0) return TLGB_OK;
   const char* P = (const char*)plan;
-  if (g.cplx)
-    return g.norm == 1 ? launch_fwd<float2, 1>(g, info, P, locs, grid, out, s) : launch_fwd<float2, 2>(g, info, P, locs, grid, out, s);
-  return g.norm == 1 ? launch_fwd<float, 1>(g, info, P, locs, grid, out, s) : launch_fwd<float, 2>(g, info, P, locs, grid, out, s);
+  return launch_fwd(g, info, P, locs, grid, out, s);
 }
 
 extern "C" int tlgb_interp_adjoint(const tlgb_interp_desc* d, const tlgb_interp_plan_info* info, const void* plan,
@@ -1067,11 +1367,7 @@ extern "C" int tlgb_interp_adjoint(const tlgb_interp_desc* d, const tlgb_interp_
   if (scratch_bytes < need || (need > 0 && !scratch)) TLGB_FAIL(TLGB_ERR_WORKSPACE, "adjoint scratch too small");
   cudaStream_t s = (cudaStream_t)stream;
   const char* P = (const char*)plan;
-  if (g.cplx)
-    return g.norm == 1 ? launch_adj<float2, 1>(g, info, P, locs, vals, grid, scratch, s)
-                       : launch_adj<float2, 2>(g, info, P, locs, vals, grid, scratch, s);
-  return g.norm == 1 ? launch_adj<float, 1>(g, info, P, locs, vals, grid, scratch, s)
-                     : launch_adj<float, 2>(g, info, P, locs, vals, grid, scratch, s);
+  return launch_adj(g, info, P, locs, vals, grid, scratch, s);
 }
 
 extern "C" int tlgb_interp_grad_locs(const tlgb_interp_desc* d, const tlgb_interp_plan_info* info, const void* plan,

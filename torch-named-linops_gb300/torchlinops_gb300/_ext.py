@@ -90,7 +90,14 @@ _SIGNATURES = {
     "tlgb_interp_grad_locs": ([_P, _P, _P, _P, _P, _P, _P, _P], ctypes.c_int),
     "tlgb_unfold": ([_P, _P, _P, _P], ctypes.c_int),
     "tlgb_fold": ([_P, _P, _P, _P], ctypes.c_int),
+    "tlgb_cg_scratch_bytes": ([], ctypes.c_size_t),
+    "tlgb_dot_f64": ([_P, _P, ctypes.c_int64, ctypes.c_int, _P, _P, ctypes.c_size_t, _P], ctypes.c_int),
+    "tlgb_cg_set_pap": ([_P, _P, ctypes.c_int64, ctypes.c_int, _P, _P, ctypes.c_size_t, _P], ctypes.c_int),
+    "tlgb_cg_step": ([_P, _P, _P, _P, ctypes.c_int64, ctypes.c_int, _P, _P, ctypes.c_size_t, _P], ctypes.c_int),
 }
+
+# float64 CG state vector slots (include/tlgb.h)
+CG_RS, CG_RS_OLD, CG_PAP, CG_ALPHA, CG_BETA, CG_ITERS, CG_TMP, CG_STATE_LEN = 0, 1, 2, 3, 4, 5, 6, 8
 
 _lib = None
 _lock = threading.Lock()

@@ -1,0 +1,491 @@
+"""Operator layer around the GB300 kernels: Interpolate, ArrayToBlocks,
+BlocksToArray and the NUFFT chain, with ``.H``, ``.N`` and composition.
+
+This mirrors the operator interface of the reference's NamedLinop framework
+(linops/namedlinop.py:34-661, chain.py:26-232) for the operators on the hot
+path -- static ``fn`` / ``adj_fn`` / ``normal_fn`` taking the operator first,
+``.H`` (adjoint), ``.N`` (normal), ``A @ B`` (chain, B applied first) -- so a
+reference user's NUFFT / CG code runs against these kernels. The named-shape
+arguments of the reference constructors are accepted and stored; the
+named-dimension algebra, splitting across GPUs and streams are not part of
+this package. The same kernels are reached from the reference's own linops by
+re-pointing its functional calls (see the integration notes of this repo).
+
+* ``Interpolate``    <- linops/interp.py:16-137
+* ``ArrayToBlocks``  <- linops/array_to_blocks.py:16-110
+* ``BlocksToArray``  <- linops/array_to_blocks.py:113-205
+* ``NUFFT``          <- linops/nufft.py:34-392 (interpolate mode)
+* ``Diagonal``, ``Scalar``, ``Pad``, ``FFT`` <- linops/{diagonal,scalar,pad_last,fft}.py
+* ``nufft`` / ``nufft_adjoint`` <- functional/_nufft.py:16-112
+"""
+
+from __future__ import annotations
+
+from copy import copy
+from math import prod
+from typing import Optional
+
+import torch
+import torch.nn as nn
+import torch.nn.functional as F
+from torch import Tensor
+
+from . import blocks as B
+from . import interp as I
+
+__all__ = [
+    "NamedLinop",
+    "Chain",
+    "Diagonal",
+    "Scalar",
+    "Pad",
+    "FFT",
+    "Interpolate",
+    "ArrayToBlocks",
+    "BlocksToArray",
+    "NUFFT",
+    "nufft",
+    "nufft_adjoint",
+    "cfftn",
+    "cifftn",
+]
+
+
+def cfftn(x, dim=None, norm="ortho"):
+    """Centred n-D FFT (reference utils/_fft.py:7-32)."""
+    x = torch.fft.ifftshift(x, dim=dim)
+    x = torch.fft.fftn(x, dim=dim, norm=norm)
+    return torch.fft.fftshift(x, dim=dim)
+
+
+def cifftn(x, dim=None, norm="ortho"):
+    """Centred n-D inverse FFT (reference utils/_fft.py:35-60)."""
+    x = torch.fft.ifftshift(x, dim=dim)
+    x = torch.fft.ifftn(x, dim=dim, norm=norm)
+    return torch.fft.fftshift(x, dim=dim)
+
+
+class NamedLinop(nn.Module):
+    """Linear operator with static fn / adj_fn / normal_fn (namedlinop.py:88-450)."""
+
+    def __init__(self):
+        super().__init__()
+        self._adjoint = None
+        self._normal = None
+
+    def forward(self, x: Tensor) -> Tensor:
+        return self.fn(self, x)
+
+    @staticmethod
+    def fn(linop, x: Tensor, /) -> Tensor:
+        raise NotImplementedError
+
+    @staticmethod
+    def adj_fn(linop, x: Tensor, /) -> Tensor:
+        raise NotImplementedError
+
+    @staticmethod
+    def normal_fn(linop, x: Tensor, /) -> Tensor:
+        return linop.adj_fn(linop, linop.fn(linop, x))
+
+    def adjoint(self) -> "NamedLinop":
+        adj = copy(self)
+        adj._adjoint = None
+        adj._normal = None
+        adj.fn, adj.adj_fn = self.adj_fn, self.fn
+        return adj
+
+    @property
+    def H(self) -> "NamedLinop":
+        if self._adjoint is None:
+            a = self.adjoint()
+            a._adjoint = [self]
+            self._adjoint = [a]
+        return self._adjoint[0]
+
+    def normal(self, inner: Optional["NamedLinop"] = None) -> "NamedLinop":
+        if inner is not None:
+            return Chain(self, inner, self.H)
+        return _Normal(self)
+
+    @property
+    def N(self) -> "NamedLinop":
+        if self._normal is None:
+            self._normal = [self.normal()]
+        return self._normal[0]
+
+    def __matmul__(self, other: "NamedLinop") -> "NamedLinop":
+        return Chain(other, self)
+
+    def __copy__(self):
+        new = type(self).__new__(type(self))
+        new.__dict__ = self.__dict__.copy()
+        new._parameters = self._parameters.copy()
+        new._buffers = self._buffers.copy()
+        new._modules = self._modules.copy()
+        return new
+
+
+class _Normal(NamedLinop):
+    """A^H A as one operator: self-adjoint (namedlinop.py:565-600)."""
+
+    def __init__(self, linop: NamedLinop):
+        super().__init__()
+        self.inner = linop
+
+    @staticmethod
+    def fn(n, x, /):
+        return n.inner.normal_fn(n.inner, x)
+
+    @staticmethod
+    def adj_fn(n, x, /):
+        return n.inner.normal_fn(n.inner, x)
+
+
+class Chain(NamedLinop):
+    """Composition applied left to right (chain.py:26-116)."""
+
+    def __init__(self, *linops: NamedLinop, name: Optional[str] = None):
+        super().__init__()
+        flat = []
+        for op in linops:
+            flat.extend(op.linops if type(op) is Chain else [op])
+        self.linops = nn.ModuleList(flat)
+        self.name = name
+
+    def __getitem__(self, i):
+        return self.linops[i]
+
+    @staticmethod
+    def fn(chain, x, /):
+        for op in chain.linops:
+            x = op(x)
+        return x
+
+    @staticmethod
+    def adj_fn(chain, x, /):
+        for op in reversed(chain.linops):
+            x = op.H(x)
+        return x
+
+    @staticmethod
+    def normal_fn(chain, x, /):
+        return chain.adj_fn(chain, chain.fn(chain, x))
+
+    def adjoint(self):
+        adj = copy(self)
+        adj._adjoint = None
+        adj._normal = None
+        adj.linops = nn.ModuleList([op.H for op in reversed(self.linops)])
+        return adj
+
+
+class Diagonal(NamedLinop):
+    """x -> w * x; adjoint conj(w) * x (diagonal.py)."""
+
+    def __init__(self, weight: Tensor, ioshape=None, broadcast_dims=None):
+        super().__init__()
+        self.weight = nn.Parameter(weight, requires_grad=False)
+        self.ioshape = ioshape
+
+    @staticmethod
+    def fn(d, x, /):
+        return x * d.weight
+
+    @staticmethod
+    def adj_fn(d, x, /):
+        return x * d.weight.conj()
+
+    @staticmethod
+    def normal_fn(d, x, /):
+        return x * (d.weight.abs() ** 2)
+
+
+class Scalar(Diagonal):
+    """x -> alpha * x (scalar.py)."""
+
+    def __init__(self, weight, ioshape=None):
+        if not isinstance(weight, torch.Tensor):
+            weight = torch.tensor(weight)
+        super().__init__(weight, ioshape)
+
+
+def pad_to_size(grid_size, padded_size):
+    """Centred F.pad list (pad_last.py:137-178)."""
+    if len(grid_size) != len(padded_size):
+        raise ValueError(f"Dimension mismatch: cannot pad from size {grid_size} to size {padded_size}.")
+    pad = []
+    for i, p in zip(grid_size, padded_size):
+        tp = p - i
+        if tp % 2:
+            left, right = (tp // 2 + 1, tp // 2) if i % 2 else (tp // 2, tp // 2 + 1)
+        else:
+            left = right = tp // 2
+        pad.append([left, right])
+    pad.reverse()
+    return sum(pad, start=[])
+
+
+def crop_slice_from_pad(pad):
+    out = []
+    for i in range(len(pad) // 2):
+        start, stop = pad[2 * i], -pad[2 * i + 1]
+        out.append(slice(start, stop if stop != 0 else None))
+    out.reverse()
+    return out
+
+
+class Pad(NamedLinop):
+    """Centred zero pad of the last dims; adjoint crops (pad_last.py:13-122)."""
+
+    def __init__(self, pad_im_size, im_size, in_shape=None, out_shape=None, batch_shape=None):
+        super().__init__()
+        if len(pad_im_size) != len(im_size):
+            raise ValueError(f"Padded and unpadded dims should be the same length. padded: {pad_im_size} unpadded: {im_size}")
+        self.D = len(im_size)
+        self.im_size = tuple(im_size)
+        self.pad_im_size = tuple(pad_im_size)
+        self.pad = pad_to_size(self.im_size, self.pad_im_size)
+        self.crop_slice = crop_slice_from_pad(self.pad)
+
+    @staticmethod
+    def fn(p, x, /):
+        if tuple(x.shape[-p.D:]) != p.im_size:
+            raise ValueError(f"Mismatched shapes: expected {p.im_size} but got {x.shape[-p.D:]}")
+        return F.pad(x, p.pad + [0, 0] * (x.ndim - p.D))
+
+    @staticmethod
+    def adj_fn(p, y, /):
+        if tuple(y.shape[-p.D:]) != p.pad_im_size:
+            raise ValueError(f"Mismatched shapes: expected {p.pad_im_size} but got {y.shape[-p.D:]}")
+        return y[tuple([slice(None)] * (y.ndim - p.D) + p.crop_slice)]
+
+
+class FFT(NamedLinop):
+    """Centred orthonormal FFT over the last ndim dims (fft.py)."""
+
+    def __init__(self, ndim: int, centered: bool = True, norm: str = "ortho", batch_shape=None, grid_shapes=None):
+        super().__init__()
+        self.ndim = ndim
+        self.centered = centered
+        self.norm = norm
+        self.dim = tuple(range(-ndim, 0))
+
+    @staticmethod
+    def fn(f, x, /):
+        if f.centered:
+            return cfftn(x, dim=f.dim, norm=f.norm)
+        return torch.fft.fftn(x, dim=f.dim, norm=f.norm)
+
+    @staticmethod
+    def adj_fn(f, x, /):
+        if f.centered:
+            return cifftn(x, dim=f.dim, norm=f.norm)
+        return torch.fft.ifftn(x, dim=f.dim, norm=f.norm)
+
+    @staticmethod
+    def normal_fn(f, x, /):
+        return x
+
+
+class Interpolate(NamedLinop):
+    """Grid -> off-grid points (interp.py:16-137): (batch, grid) -> (batch, locs_batch)."""
+
+    def __init__(
+        self,
+        locs: Tensor,
+        grid_size: tuple[int, ...],
+        batch_shape=None,
+        locs_batch_shape=None,
+        grid_shape=None,
+        width: float = 4.0,
+        kernel: str = "kaiser_bessel",
+        norm: int = 1,
+        pad_mode: str = "circular",
+        kernel_params: Optional[dict] = None,
+    ):
+        super().__init__()
+        if locs_batch_shape is not None and len(locs_batch_shape) > len(locs.shape) - 1:
+            raise ValueError(
+                f"locs_batch_shape has length longer than batch dim of locs. locs_batch_shape: {locs_batch_shape}, locs: {locs.shape}"
+            )
+        self.locs = nn.Parameter(locs, requires_grad=False)
+        self.grid_size = tuple(grid_size)
+        kp = dict(beta=1.0)
+        if kernel_params:
+            kp.update(kernel_params)
+        self.interp_params = {
+            "width": width,
+            "kernel": kernel,
+            "norm": norm,
+            "pad_mode": pad_mode,
+            "kernel_params": kp,
+        }
+
+    @staticmethod
+    def fn(interp, x, /):
+        return I.interpolate(x, interp.locs, **interp.interp_params)
+
+    @staticmethod
+    def adj_fn(interp, x, /):
+        return I.interpolate_adjoint(x, interp.locs, interp.grid_size, **interp.interp_params)
+
+    def size(self, dim):
+        return None
+
+
+class ArrayToBlocks(NamedLinop):
+    """Sliding blocks of an array (array_to_blocks.py:16-110)."""
+
+    def __init__(self, grid_size, block_size, stride, mask=None, batch_shape=None, array_shape=None, blocks_shape=None):
+        super().__init__()
+        self.grid_size = tuple(grid_size)
+        self.ndim = len(self.grid_size)
+        self.block_size = tuple(block_size)
+        self.stride = tuple(stride)
+        self.mask = nn.Parameter(mask, requires_grad=False) if mask is not None else None
+
+    @staticmethod
+    def fn(a, x, /):
+        return B.array_to_blocks(x, a.block_size, a.stride, a.mask)
+
+    @staticmethod
+    def adj_fn(a, x, /):
+        return B.blocks_to_array(x, a.grid_size, a.block_size, a.stride, a.mask)
+
+    @staticmethod
+    def normal_fn(a, x, /):
+        return a.adj_fn(a, a.fn(a, x))
+
+    def adjoint(self):
+        return BlocksToArray(self.grid_size, self.block_size, self.stride, self.mask)
+
+
+class BlocksToArray(NamedLinop):
+    """Overlapping blocks summed into an array (array_to_blocks.py:113-205)."""
+
+    def __init__(self, grid_size, block_size, stride, mask=None, batch_shape=None, blocks_shape=None, array_shape=None):
+        super().__init__()
+        self.grid_size = tuple(grid_size)
+        self.ndim = len(self.grid_size)
+        self.block_size = tuple(block_size)
+        self.stride = tuple(stride)
+        self.mask = nn.Parameter(mask, requires_grad=False) if mask is not None else None
+
+    @staticmethod
+    def fn(b, x, /):
+        return B.blocks_to_array(x, b.grid_size, b.block_size, b.stride, b.mask)
+
+    @staticmethod
+    def adj_fn(b, x, /):
+        if tuple(x.shape[-b.ndim:]) != b.grid_size:
+            raise RuntimeError(f"BlocksToArray expected input with full size {b.grid_size} but got {x.shape}")
+        return B.array_to_blocks(x, b.block_size, b.stride, b.mask)
+
+    def adjoint(self):
+        return ArrayToBlocks(self.grid_size, self.block_size, self.stride, self.mask)
+
+
+def nufft_beta(width: float, oversamp: float) -> float:
+    return I.kaiser_bessel_beta(width, oversamp)
+
+
+def prep_locs(locs: Tensor, grid_size, padded_size, pad_mode="circular") -> Tensor:
+    """Scale centred locs in [-N/2, N/2] to the padded grid (nufft.py:242-334)."""
+    out = locs.clone()
+    for i in range(-len(grid_size), 0):
+        out[..., i] *= padded_size[i] / grid_size[i]
+        out[..., i] += padded_size[i] // 2
+        if pad_mode == "zero":
+            out[..., i] = torch.clamp(out[..., i], 0, padded_size[i] - 1)
+        elif pad_mode == "circular":
+            out[..., i] = torch.remainder(out[..., i], torch.tensor(padded_size[i], device=locs.device))
+        else:
+            raise ValueError(f"Unrecognized padding mode during prep: {pad_mode}")
+    return out
+
+
+def apodize_weights(grid_size, padded_size, oversamp, width: float, beta: float) -> Tensor:
+    """Separable KB apodization (nufft.py:349-365)."""
+    gs = torch.tensor(grid_size)
+    ps = torch.tensor(padded_size)
+    g = torch.stack(torch.meshgrid(*(torch.arange(s) for s in grid_size), indexing="ij"), dim=-1)
+    apod = (beta**2 - (torch.pi * width * (g - gs // 2) / ps) ** 2) ** 0.5
+    apod = apod / torch.sinh(apod)
+    return torch.prod(apod, dim=-1)
+
+
+class NUFFT(Chain):
+    """Apodize -> pad -> centred FFT -> Interpolate -> scale (nufft.py:34-215)."""
+
+    def __init__(
+        self,
+        locs: Tensor,
+        grid_size: tuple[int, ...],
+        output_shape=None,
+        input_shape=None,
+        input_kshape=None,
+        batch_shape=None,
+        oversamp: float = 1.25,
+        width: float = 4.0,
+        mode: str = "interpolate",
+        do_prep_locs: bool = True,
+        apodize_weights: Optional[Tensor] = None,
+        **options,
+    ):
+        if mode != "interpolate":
+            raise ValueError(f"Unrecognized NUFFT mode: {mode}")
+        device = locs.device
+        ndim = len(grid_size)
+        padded_size = tuple(int(i * oversamp) for i in grid_size)
+        pad = Pad(padded_size, grid_size)
+        fft = FFT(ndim=locs.shape[-1], centered=True, norm="ortho")
+        locs_prepared = prep_locs(locs, grid_size, padded_size) if do_prep_locs else locs
+        beta = nufft_beta(width, oversamp)
+        if apodize_weights is None:
+            weight = globals()["apodize_weights"](grid_size, padded_size, oversamp, width, beta).to(device)
+        else:
+            weight = apodize_weights
+        if weight.isnan().any() or weight.isinf().any():
+            raise ValueError(f"Nan/Inf values detected in apodization weight (width={width}, oversamp={oversamp}).")
+        apodize = Diagonal(weight)
+        interp = Interpolate(
+            locs_prepared, padded_size, width=width, kernel="kaiser_bessel", kernel_params=dict(beta=beta)
+        )
+        scale_factor = width**ndim * (prod(grid_size) / prod(padded_size)) ** 0.5
+        scale = Scalar(torch.tensor(1.0 / scale_factor, device=device))
+        super().__init__(apodize, pad, fft, interp, scale, name="NUFFT")
+        self.locs = locs
+        self.grid_size = tuple(grid_size)
+        self.oversamp = oversamp
+        self.width = width
+        self.pad = pad
+        self.fft = fft
+        self.interp = interp
+
+
+def nufft(x: Tensor, locs: Tensor, oversamp: float = 1.25, width: float = 4.0) -> Tensor:
+    """Functional NUFFT (functional/_nufft.py:16-62)."""
+    grid_size = tuple(x.shape[-locs.shape[-1]:])
+    ndim = locs.shape[-1]
+    padded = tuple(int(s * oversamp) for s in grid_size)
+    beta = nufft_beta(width, oversamp)
+    x = x * apodize_weights(grid_size, padded, oversamp, width, beta).to(x.device)
+    x = Pad.fn(Pad(padded, grid_size), x)
+    x = cfftn(x, dim=tuple(range(-ndim, 0)), norm="ortho")
+    x = I.interpolate(x, prep_locs(locs, grid_size, padded), width, kernel="kaiser_bessel", kernel_params=dict(beta=beta))
+    return x / (width**ndim * (prod(grid_size) / prod(padded)) ** 0.5)
+
+
+def nufft_adjoint(x: Tensor, locs: Tensor, grid_size, oversamp: float = 1.25, width: float = 4.0) -> Tensor:
+    """Functional adjoint NUFFT (functional/_nufft.py:65-112)."""
+    grid_size = tuple(grid_size)
+    ndim = locs.shape[-1]
+    padded = tuple(int(s * oversamp) for s in grid_size)
+    beta = nufft_beta(width, oversamp)
+    x = x / (width**ndim * (prod(grid_size) / prod(padded)) ** 0.5)
+    x = I.interpolate_adjoint(x, prep_locs(locs, grid_size, padded), padded, width, kernel="kaiser_bessel",
+                              kernel_params=dict(beta=beta))
+    x = cifftn(x, dim=tuple(range(-ndim, 0)), norm="ortho")
+    x = Pad.adj_fn(Pad(padded, grid_size), x)
+    return x * apodize_weights(grid_size, padded, oversamp, width, beta).to(x.device)
