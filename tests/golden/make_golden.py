@@ -155,6 +155,22 @@ def make_edgecases(F, out_dir):
     np.savez_compressed(os.path.join(out_dir, "edge_intloc.npz"), **out)
 
 
+def make_nufft(F, out_dir):
+    """Functional NUFFT / adjoint (functional/_nufft.py:16-112), 2D and 3D."""
+    out = {}
+    for name, shape, npts, batch in (("2d", (24, 20), 300, (2,)), ("3d", (12, 10, 14), 400, (1,))):
+        gen = torch.Generator().manual_seed(len(name) * 31 + npts)
+        x = torch.complex(torch.randn(*batch, *shape, generator=gen), torch.randn(*batch, *shape, generator=gen))
+        locs = torch.stack([torch.rand(npts, generator=gen) * s - s / 2 for s in shape], -1).to(torch.float32)
+        y = torch.complex(torch.randn(*batch, npts, generator=gen), torch.randn(*batch, npts, generator=gen))
+        out[f"{name}_x"] = _np(x)
+        out[f"{name}_locs"] = _np(locs)
+        out[f"{name}_y"] = _np(y)
+        out[f"{name}_fwd"] = _np(F.nufft(x, locs, oversamp=1.25, width=4.0))
+        out[f"{name}_adj"] = _np(F.nufft_adjoint(y, locs, shape, oversamp=1.25, width=4.0))
+    np.savez_compressed(os.path.join(out_dir, "nufft.npz"), **out)
+
+
 def make_kernels(K, out_dir):
     x = torch.linspace(-1.2, 1.2, 241)
     out = {"x": _np(x)}
@@ -240,6 +256,7 @@ def main():
     make_kernels(K, args.out)
     make_edgecases(F, args.out)
     make_config1(F, args.out)
+    make_nufft(F, args.out)
     n_i = make_interp(F, args.out)
     n_b = make_blocks(F, args.out)
     print(f"wrote {n_i} interp cases, {n_b} block cases in {time.time() - t0:.1f}s")

@@ -1,0 +1,120 @@
+"""NUFFT chain, operator algebra (.H, .N, @) and the float64 CG on the GPU."""
+
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import GOLDEN, rel_l2, to_torch
+
+import torchlinops_gb300 as T
+from torchlinops_gb300 import alg, linops
+
+pytestmark = pytest.mark.gpu
+DEV = "cuda"
+
+
+@pytest.mark.parametrize("name", ["2d", "3d"])
+def test_functional_nufft_matches_reference(name):
+    d = np.load(f"{GOLDEN}/nufft.npz")
+    x = to_torch(d[f"{name}_x"], True).to(DEV)
+    locs = torch.from_numpy(d[f"{name}_locs"]).to(DEV)
+    y = to_torch(d[f"{name}_y"], True).to(DEV)
+    shape = tuple(x.shape[-locs.shape[-1]:])
+    fwd = linops.nufft(x, locs)
+    adj = linops.nufft_adjoint(y, locs, shape)
+    assert rel_l2(fwd.cpu(), to_torch(d[f"{name}_fwd"], True)) < 1e-5
+    assert rel_l2(adj.cpu(), to_torch(d[f"{name}_adj"], True)) < 1e-5
+
+
+def _nudft(x, locs):
+    """Exact type-2 NUDFT in float64 (centred), small problems only."""
+    shape = x.shape[-locs.shape[-1]:]
+    grids = torch.meshgrid(*(torch.arange(s, dtype=torch.float64) - s // 2 for s in shape), indexing="ij")
+    phase = sum(l[:, None] * g.reshape(1, -1) / s for l, g, s in zip(locs.double().T, grids, shape))
+    E = torch.exp(-2j * math.pi * phase)
+    return (x.reshape(*x.shape[: -len(shape)], -1).to(torch.complex128) @ E.T) / math.sqrt(math.prod(shape))
+
+
+def test_nufft_linop_approximates_nudft():
+    gen = torch.Generator().manual_seed(1)
+    shape = (32, 32)
+    locs = torch.rand(500, 2, generator=gen) * 32 - 16
+    x = torch.randn(2, *shape, dtype=torch.complex64, generator=gen)
+    A = linops.NUFFT(locs.to(DEV), shape, oversamp=1.25, width=4.0)
+    y = A(x.to(DEV)).cpu()
+    ref = _nudft(x, locs)
+    assert rel_l2(y, ref) < 2e-2  # NUFFT approximation error at oversampling 1.25, width 4
+
+
+def test_nufft_adjoint_normal_identities():
+    gen = torch.Generator().manual_seed(2)
+    shape = (24, 24, 24)
+    locs = (torch.rand(4000, 3, generator=gen) * 24 - 12).to(DEV)
+    A = linops.NUFFT(locs, shape)
+    x = torch.randn(3, *shape, dtype=torch.complex64, generator=gen).to(DEV)
+    y = torch.randn(3, 4000, dtype=torch.complex64, generator=gen).to(DEV)
+    Ax, AHy = A(x), A.H(y)
+    lhs = torch.vdot(Ax.flatten().to(torch.complex128), y.flatten().to(torch.complex128))
+    rhs = torch.vdot(x.flatten().to(torch.complex128), AHy.flatten().to(torch.complex128))
+    assert abs(lhs - rhs) / abs(lhs) < 1e-5
+    torch.testing.assert_close(A.N(x), A.H(A(x)), rtol=1e-5, atol=1e-5)
+    B = A.H @ A
+    torch.testing.assert_close(B(x), A.N(x), rtol=1e-5, atol=1e-5)
+
+
+def test_array_to_blocks_linop():
+    mask = torch.zeros(3, 3, 3, dtype=torch.bool)
+    mask[1] = True
+    A = linops.ArrayToBlocks((15, 15, 15), (3, 3, 3), (1, 1, 1), mask)
+    x = torch.randn(2, 15, 15, 15, device=DEV)
+    y = torch.randn(2, 13, 13, 13, 9, device=DEV)
+    lhs = torch.vdot(A(x).flatten().double(), y.flatten().double())
+    rhs = torch.vdot(x.flatten().double(), A.H(y).flatten().double())
+    assert abs(lhs - rhs) / abs(lhs) < 1e-6
+    torch.testing.assert_close(A.N(x), A.H(A(x)))
+    assert isinstance(A.H, linops.BlocksToArray)
+
+
+def test_dot64_matches_float64():
+    gen = torch.Generator().manual_seed(3)
+    x = torch.randn(1_000_003, dtype=torch.complex64, generator=gen)
+    y = torch.randn(1_000_003, dtype=torch.complex64, generator=gen)
+    d = alg.dot64(x.to(DEV), y.to(DEV)).cpu()
+    ref = torch.vdot(x.to(torch.complex128), y.to(torch.complex128))
+    assert abs(complex(d[0], d[1]) - complex(ref)) / abs(complex(ref)) < 1e-12
+    d2 = alg.dot64(x.to(DEV), y.to(DEV)).cpu()
+    assert torch.equal(d, d2)
+
+
+def test_cg_float64_scalars_solve_spd_system():
+    gen = torch.Generator().manual_seed(4)
+    n = 256
+    Q, _ = torch.linalg.qr(torch.randn(n, n, dtype=torch.complex128, generator=gen))
+    ev = torch.logspace(0, 3, n, dtype=torch.float64)
+    M = (Q * ev) @ Q.conj().T
+    Mc = M.to(torch.complex64).to(DEV)
+    xt = torch.randn(n, dtype=torch.complex64, generator=gen).to(DEV)
+    b = Mc @ xt
+    x, info = alg.cg_solve(lambda v: Mc @ v, b, rtol=1e-5, max_iters=1000)
+    assert info.converged and info.true_rel_residual < 2e-5
+    # reference signature still works
+    x2 = alg.conjugate_gradients(lambda v: Mc @ v, b, max_num_iters=600, disable_tracking=True)
+    assert float(alg.norm64((b - Mc @ x2).contiguous())) / float(alg.norm64(b)) < 1e-4
+
+
+def test_cg_on_nufft_normal_equations():
+    gen = torch.Generator().manual_seed(5)
+    shape = (32, 32, 32)
+    locs = (torch.rand(60000, 3, generator=gen) * 32 - 16).to(DEV)
+    A = linops.NUFFT(locs, shape)
+    xt = torch.randn(*shape, dtype=torch.complex64, generator=gen).to(DEV)
+    lam = 1e-2
+    N = lambda v: A.N(v) + lam * v  # noqa: E731
+    b = N(xt)
+    x, info = alg.cg_solve(N, b, rtol=1e-4, max_iters=300)
+    assert info.converged and info.true_rel_residual < 2e-4
+    # flexible PCG with a fixed diagonal preconditioner converges too
+    x2, info2 = alg.cg_solve(N, b, rtol=1e-4, max_iters=300, M=lambda r: r * 0.5)
+    assert info2.converged and info2.true_rel_residual < 2e-4

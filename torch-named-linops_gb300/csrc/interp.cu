@@ -339,48 +339,83 @@ __device__ __forceinline__ int lg2i(int v) { return 31 - __clz(v); }
 
 // ------------------------------------------------- lane-per-point taps
 
-// Per point tap data staged in shared memory: start coordinate (wrapped for
-// circular padding), number of valid taps and their per-dim values (the 1D
-// weight for norm 1, |d| for norm 2) per internal dim.
+// KB(x) by the same A&S expansions as kb_value, with one division (3.75 / z)
+// and Horner evaluation instead of one division per term: equal to kb_value
+// to a few float32 ulps, ~3x fewer instructions. Used on the hot paths.
+__device__ __forceinline__ float kb_fast(float x, float beta) {
+  const float z = beta * __fsqrt_rn(__fsub_rn(1.0f, __fmul_rn(x, x)));
+  if (z < 3.75f) {
+    const float u = (z * (1.0f / 3.75f)) * (z * (1.0f / 3.75f));
+    return 1.0f + u * (3.5156229f + u * (3.0899424f + u * (1.2067492f + u * (0.2659732f +
+           u * (0.0360768f + u * 0.0045813f)))));
+  }
+  const float v = __fdiv_rn(3.75f, z);
+  const float q = 0.39894228f + v * (0.01328592f + v * (0.00225319f + v * (-0.00157565f + v * (0.00916281f +
+                  v * (-0.02057706f + v * (0.02635537f + v * (-0.01647633f + v * 0.00392377f)))))));
+  return expf(z) * rsqrtf(z) * q;
+}
+
+__device__ __forceinline__ float kern_fast(int kernel, float ax, float beta) {
+  return kernel == TLGB_KERNEL_KAISER_BESSEL ? kb_fast(ax, beta) : fmaxf(1.0f - ax, 0.0f);
+}
+
+// Per point record staged in shared memory: for each internal dim the taps
+// that land in the CTA's tile (gridding) or region (gather), as a local
+// coordinate and the 1D weight (norm 1) or |d| (norm 2). Taps outside the
+// tile are dropped here, so the inner loops carry no bounds checks.
 template <int NTB>
-struct Pt {
-  int st[3];
-  int n[3];
-  float w[3][NTB];
+struct Rec {
+  short lc[3][NTB];
+  float wv[3][NTB];
+  int m[3];
 };
 
-// One lane evaluates all taps of point p into pt. Returns false when the
-// point has no valid tap (it then contributes nothing).
+// One lane builds the record of point p (coordinates x3) for the tile with
+// origin o and extent T. region: gather mode, local coordinates run
+// contiguously from the wrapped start (the staged region holds the wrap).
 template <int NTB>
-__device__ __forceinline__ bool lane_point_taps(const Geo& g, const float* __restrict__ locs, long long p,
-                                                const float (&x3)[3], Pt<NTB>& pt) {
+__device__ __forceinline__ void lane_rec(const Geo& g, const float (&x3)[3], const int (&o)[3], bool region,
+                                         Rec<NTB>& R) {
+  bool ok = true;
   for (int e = 0; e < 3; ++e) {
     if (!g.act[e]) {
-      pt.st[e] = 0;
-      pt.n[e] = 1;
-      pt.w[e][0] = g.norm == 1 ? 1.f : 0.f;
+      R.lc[e][0] = 0;
+      R.wv[e][0] = g.norm == 1 ? 1.f : 0.f;
+      R.m[e] = 1;
       continue;
     }
     const float x = x3[e];
-    if (!coord_ok(x)) return false;
-    const int lower = lower_of(g, e, x);
-    int s = -1, cnt = 0;
-    for (int k = 0; k < g.NT[e]; ++k) {
-      const Tap t = tap_eval(g, e, x, lower, k);
-      if (t.valid) {
+    int cnt = 0;
+    if (ok && coord_ok(x)) {
+      const int lower = lower_of(g, e, x);
+      int s = -1;
+      for (int k = 0; k < g.NT[e]; ++k) {
+        const Tap t = tap_eval(g, e, x, lower, k);
+        if (!t.valid) continue;
         if (s < 0) s = k;
-        const float ad = fabsf(t.d);
-        pt.w[e][cnt] = g.norm == 1 ? kern_value(g.kernel, ad, g.beta) : ad;
-        ++cnt;
+        int l;
+        if (region) {
+          int st = lower + s;
+          if (g.pad == TLGB_PAD_CIRCULAR) st = wrapi(st, g.N[e]);
+          l = st - o[e] + (k - s);
+        } else {
+          int gg = lower + k;
+          if (g.pad == TLGB_PAD_CIRCULAR) gg = wrapi(gg, g.N[e]);
+          l = gg - o[e];
+          if (l < 0 || l >= g.T[e]) continue;
+        }
+        if (cnt < NTB) {
+          const float ad = fabsf(t.d);
+          R.lc[e][cnt] = (short)l;
+          R.wv[e][cnt] = g.norm == 1 ? kern_fast(g.kernel, ad, g.beta) : ad;
+          ++cnt;
+        }
       }
     }
-    if (cnt == 0) return false;
-    int st = lower + s;
-    if (g.pad == TLGB_PAD_CIRCULAR) st = wrapi(st, g.N[e]);
-    pt.st[e] = st;
-    pt.n[e] = cnt;
+    R.m[e] = cnt;
+    if (cnt == 0) ok = false;
   }
-  return true;
+  if (!ok) R.m[0] = 0;
 }
 
 // N floats moved as one vector (a "coil unit": 1 or 2 batch entries)
@@ -413,13 +448,6 @@ __device__ __forceinline__ void stv(float* p, const VecF<N>& r) {
   }
 }
 
-// weight of one tap combination of a staged point
-template <int NTB>
-__device__ __forceinline__ float tap_w(const Geo& g, const Pt<NTB>& P, int kx, int ky, int kz) {
-  if (g.norm == 1) return P.w[0][kx] * P.w[1][ky] * P.w[2][kz];
-  return radial_w(g, P.w[0][kx], P.w[1][ky], P.w[2][kz]);
-}
-
 // Lane roles: lane = (ux, uz, cu); cu indexes coil units (lowest bits), uz
 // the tap along z (4 slots), ux the tap along the split dim (x in 3D, y in
 // 2D, more z slots in 1D).
@@ -437,18 +465,52 @@ __device__ __forceinline__ Lanes lane_roles(int lane, int nunits) {
   return L;
 }
 
+// Visit the taps of record R assigned to this lane: f(lx, ly, lz, w).
+// 3D: x split over ux, z over uz, y looped; 2D: y over ux, z over uz;
+// 1D: z over (ux, uz).
+template <int NDIM, int NTB, typename F>
+__device__ __forceinline__ void for_lane_taps(const Geo& g, const Rec<NTB>& R, const Lanes& L, F&& f) {
+  if constexpr (NDIM == 3) {
+    for (int kz = L.uz; kz < R.m[2]; kz += 4) {
+      const int lz = R.lc[2][kz];
+      const float wz = R.wv[2][kz];
+      for (int kx = L.ux; kx < R.m[0]; kx += L.UX) {
+        const int lx = R.lc[0][kx];
+        const float wxz = R.wv[0][kx] * wz;
+        for (int ky = 0; ky < R.m[1]; ++ky) {
+          const float w = g.norm == 1 ? wxz * R.wv[1][ky] : radial_w(g, R.wv[0][kx], R.wv[1][ky], wz);
+          f(lx, (int)R.lc[1][ky], lz, w);
+        }
+      }
+    }
+  } else if constexpr (NDIM == 2) {
+    for (int kz = L.uz; kz < R.m[2]; kz += 4) {
+      const int lz = R.lc[2][kz];
+      const float wz = R.wv[2][kz];
+      for (int ky = L.ux; ky < R.m[1]; ky += L.UX) {
+        const float w = g.norm == 1 ? R.wv[1][ky] * wz : radial_w(g, 0.f, R.wv[1][ky], wz);
+        f(0, (int)R.lc[1][ky], lz, w);
+      }
+    }
+  } else {
+    for (int kz = L.uz + 4 * L.ux; kz < R.m[2]; kz += 4 * L.UX) {
+      const float w = g.norm == 1 ? R.wv[2][kz] : radial_w(g, 0.f, 0.f, R.wv[2][kz]);
+      f(0, 0, (int)R.lc[2][kz], w);
+    }
+  }
+}
+
 // ------------------------------------------------------------------ forward
 
-// CTA = 8 warps sharing one staged region (tile + halo, [x][y][z][batch]);
+// CTA = NW warps sharing one staged region (tile + halo, [x][y][z][batch]);
 // each warp interpolates 32 home points per batch.
 template <int N, int NDIM, int NTB, int NW>
 __global__ void __launch_bounds__(NW * 32, 1) interp_fwd_kernel(Geo g, const int4* __restrict__ items,
-                                                             const int32_t* __restrict__ entries,
-                                                             const float* __restrict__ locs,
-                                                             const float* __restrict__ gridv,
-                                                             float* __restrict__ out, int CG) {
+                                                                const int32_t* __restrict__ entries,
+                                                                const float* __restrict__ locs,
+                                                                const float* __restrict__ gridv,
+                                                                float* __restrict__ out, int CG) {
   extern __shared__ __align__(16) unsigned char smem[];
-  constexpr int ES = N == 4 ? 2 : N;  // floats per batch entry: complex units are (re, im) pairs
   const int es = g.cplx ? 2 : 1;
   const int4 it = items[blockIdx.x];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -469,14 +531,16 @@ __global__ void __launch_bounds__(NW * 32, 1) interp_fwd_kernel(Geo g, const int
   }
   const int vstride = CG * es;  // floats per staged voxel
   float* reg = reinterpret_cast<float*>(smem);
-  Pt<NTB>* pbuf = reinterpret_cast<Pt<NTB>*>(smem + (size_t)S[0] * S[1] * S[2] * vstride * sizeof(float)) + warp * 32;
+  const size_t reg_bytes = (((size_t)S[0] * S[1] * S[2] * vstride * sizeof(float)) + 15) & ~(size_t)15;
+  Rec<NTB>* rbuf = reinterpret_cast<Rec<NTB>*>(smem + reg_bytes) + warp * 32;
 
   // stage: rows (x, y) per warp, lanes over (z, batch entry), batch fastest
   const long long gvol = (long long)g.N[0] * g.N[1] * g.N[2];
   const int cgp = CG <= 1 ? 1 : (CG <= 2 ? 2 : (CG <= 4 ? 4 : 8));
   const int lgc = lg2i(cgp);
+  const int rowlen = S[2] * cgp;
   for (int row = warp; row < S[0] * S[1]; row += NW) {
-    const int x = row / S[1], y = row - (row / S[1]) * S[1];
+    const int x = row / S[1], y = row - x * S[1];
     int gx = o[0] + x, gy = o[1] + y;
     bool rin = true;
     if (g.pad == TLGB_PAD_CIRCULAR) {
@@ -487,7 +551,39 @@ __global__ void __launch_bounds__(NW * 32, 1) interp_fwd_kernel(Geo g, const int
     }
     const long long rbase = ((long long)gx * g.N[1] + gy) * g.N[2];
     float* rdst = reg + (size_t)(x * S[1] + y) * S[2] * vstride;
-    for (int idx = lane; idx < S[2] * cgp; idx += 32) {
+    // all loads of the row first (independent), then the stores
+    constexpr int MAXI = 8;
+    float2 vv[MAXI];
+#pragma unroll
+    for (int i = 0; i < MAXI; ++i) {
+      vv[i] = make_float2(0.f, 0.f);
+      const int idx = lane + 32 * i;
+      if (idx < rowlen) {
+        const int c = idx & (cgp - 1), z = idx >> lgc;
+        int gz = o[2] + z;
+        bool in = rin && c < ncoil;
+        if (g.pad == TLGB_PAD_CIRCULAR) gz = wrapi(gz, g.N[2]);
+        else in = in && gz < g.N[2];
+        if (in) {
+          const long long gi = (long long)(c0 + c) * gvol + rbase + gz;
+          if (es == 2) vv[i] = __ldg(reinterpret_cast<const float2*>(gridv) + gi);
+          else vv[i].x = __ldg(gridv + gi);
+        }
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < MAXI; ++i) {
+      const int idx = lane + 32 * i;
+      if (idx < rowlen) {
+        const int c = idx & (cgp - 1), z = idx >> lgc;
+        if (c < CG) {
+          float* d = rdst + z * vstride + c * es;
+          if (es == 2) *reinterpret_cast<float2*>(d) = vv[i];
+          else d[0] = vv[i].x;
+        }
+      }
+    }
+    for (int idx = lane + 32 * MAXI; idx < rowlen; idx += 32) {  // long rows (1D tiles)
       const int c = idx & (cgp - 1), z = idx >> lgc;
       if (c >= CG) continue;
       int gz = o[2] + z;
@@ -495,22 +591,16 @@ __global__ void __launch_bounds__(NW * 32, 1) interp_fwd_kernel(Geo g, const int
       if (g.pad == TLGB_PAD_CIRCULAR) gz = wrapi(gz, g.N[2]);
       else in = in && gz < g.N[2];
       float* d = rdst + z * vstride + c * es;
-      if (es == 2) {
-        float2 v = make_float2(0.f, 0.f);
-        if (in) v = __ldg(reinterpret_cast<const float2*>(gridv) + (long long)(c0 + c) * gvol + rbase + gz);
-        *reinterpret_cast<float2*>(d) = v;
-      } else {
-        d[0] = in ? __ldg(gridv + (long long)(c0 + c) * gvol + rbase + gz) : 0.f;
-      }
+      const long long gi = (long long)(c0 + c) * gvol + rbase + gz;
+      if (es == 2) *reinterpret_cast<float2*>(d) = in ? __ldg(reinterpret_cast<const float2*>(gridv) + gi) : make_float2(0.f, 0.f);
+      else d[0] = in ? __ldg(gridv + gi) : 0.f;
     }
   }
   __syncthreads();
 
-  const int U = N / ES;                     // batch entries per unit
+  const int U = N / es;  // batch entries per unit
   const int nunits = (CG + U - 1) / U;
   const Lanes L = lane_roles(lane, nunits);
-  const int ndo = g.ndim;  // unused except to keep NDIM-specific code uniform
-  (void)ndo;
   for (int b = it.y + warp * 32; b < it.z; b += NW * 32) {
     const int j = b + lane;
     const int nb = min(32, it.z - b);
@@ -519,60 +609,35 @@ __global__ void __launch_bounds__(NW * 32, 1) interp_fwd_kernel(Geo g, const int
       p = entries[j];
       float x3[3];
       for (int e = 0; e < 3; ++e) x3[e] = g.act[e] ? load_coord(g, locs, p, e) : 0.f;
-      if (!lane_point_taps<NTB>(g, locs, p, x3, pbuf[lane])) pbuf[lane].n[0] = 0;
+      lane_rec<NTB>(g, x3, o, true, rbuf[lane]);
     }
     __syncwarp();
     for (int jj = 0; jj < nb; ++jj) {
-      const Pt<NTB>& P = pbuf[jj];
+      const Rec<NTB>& R = rbuf[jj];
       const long long pj = __shfl_sync(0xffffffffu, p, jj);
-      if (P.n[0] == 0) continue;  // warp-uniform
-      const int l0 = P.st[0] - o[0], l1 = P.st[1] - o[1], l2 = P.st[2] - o[2];
+      if (R.m[0] == 0) continue;  // warp-uniform
       VecF<N> acc;
 #pragma unroll
       for (int i = 0; i < N; ++i) acc.v[i] = 0.f;
       if (L.cu < nunits) {
-        if constexpr (NDIM == 3) {
-          for (int kx = L.ux; kx < P.n[0]; kx += L.UX)
-            for (int ky = 0; ky < P.n[1]; ++ky) {
-              const float* rowp = reg + ((size_t)((l0 + kx) * S[1] + (l1 + ky)) * S[2] + l2) * vstride + L.cu * N;
-              for (int kz = L.uz; kz < P.n[2]; kz += 4) {
-                const float w = tap_w(g, P, kx, ky, kz);
-                const VecF<N> v = ldv<N>(rowp + kz * vstride);
+        const float* base = reg + L.cu * N;
+        for_lane_taps<NDIM, NTB>(g, R, L, [&](int lx, int ly, int lz, float w) {
+          const VecF<N> v = ldv<N>(base + ((size_t)(lx * S[1] + ly) * S[2] + lz) * vstride);
 #pragma unroll
-                for (int i = 0; i < N; ++i) acc.v[i] = fmaf(w, v.v[i], acc.v[i]);
-              }
-            }
-        } else if constexpr (NDIM == 2) {
-          for (int ky = L.ux; ky < P.n[1]; ky += L.UX) {
-            const float* rowp = reg + ((size_t)(l1 + ky) * S[2] + l2) * vstride + L.cu * N;
-            for (int kz = L.uz; kz < P.n[2]; kz += 4) {
-              const float w = tap_w(g, P, 0, ky, kz);
-              const VecF<N> v = ldv<N>(rowp + kz * vstride);
-#pragma unroll
-              for (int i = 0; i < N; ++i) acc.v[i] = fmaf(w, v.v[i], acc.v[i]);
-            }
-          }
-        } else {
-          const float* rowp = reg + (size_t)l2 * vstride + L.cu * N;
-          for (int kz = L.uz + 4 * L.ux; kz < P.n[2]; kz += 4 * L.UX) {
-            const float w = tap_w(g, P, 0, 0, kz);
-            const VecF<N> v = ldv<N>(rowp + kz * vstride);
-#pragma unroll
-            for (int i = 0; i < N; ++i) acc.v[i] = fmaf(w, v.v[i], acc.v[i]);
-          }
-        }
+          for (int i = 0; i < N; ++i) acc.v[i] = fmaf(w, v.v[i], acc.v[i]);
+        });
       }
       for (int m = L.NUP; m < 32; m <<= 1)
 #pragma unroll
         for (int i = 0; i < N; ++i) acc.v[i] += __shfl_xor_sync(0xffffffffu, acc.v[i], m);
       if (lane < L.NUP && L.cu < nunits) {
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-          const int c = L.cu * U + u;
+        for (int u = 0; u < N; u += (N >= 2 && es == 2) ? 2 : 1) {
+          const int c = L.cu * U + u / es;
           if (c < ncoil) {
             float* dst = out + ((long long)(c0 + c) * g.npts + pj) * es;
             if (es == 2)
-              *reinterpret_cast<float2*>(dst) = make_float2(acc.v[u * ES], acc.v[u * ES + 1]);
+              *reinterpret_cast<float2*>(dst) = make_float2(acc.v[u], acc.v[u + 1]);
             else
               dst[0] = acc.v[u];
           }
@@ -594,7 +659,6 @@ __global__ void __launch_bounds__(32) interp_adj_kernel(Geo g, const int4* __res
                                                         const float* __restrict__ vals, float* __restrict__ gridv,
                                                         float* __restrict__ partial, int CG) {
   extern __shared__ __align__(16) unsigned char smem[];
-  constexpr int ES = N == 4 ? 2 : N;
   const int es = g.cplx ? 2 : 1;
   const int4 it = items[blockIdx.x];
   const int lane = threadIdx.x;
@@ -611,19 +675,20 @@ __global__ void __launch_bounds__(32) interp_adj_kernel(Geo g, const int4* __res
   }
   int o[3];
   for (int e = 0; e < 3; ++e) o[e] = tc[e] * g.T[e];
-  const int tvol = g.T[0] * g.T[1] * g.T[2];
+  const int T1 = g.T[1], T2 = g.T[2];
+  const int tvol = g.T[0] * T1 * T2;
   const int vstride = CG * es;
   const int tfl = (tvol * vstride + 3) & ~3;  // tile floats, rounded to whole float4
   float* acc = reinterpret_cast<float*>(smem);
-  Pt<NTB>* pbuf = reinterpret_cast<Pt<NTB>*>(smem + (size_t)tfl * sizeof(float));
-  float* pv = reinterpret_cast<float*>(pbuf + 32);  // [32][vstride]
+  Rec<NTB>* rbuf = reinterpret_cast<Rec<NTB>*>(smem + (size_t)tfl * sizeof(float));
+  float* pv = reinterpret_cast<float*>(rbuf + 32);  // [32][vstride]
   for (int i = lane * 4; i < tfl; i += 128) *reinterpret_cast<float4*>(acc + i) = make_float4(0.f, 0.f, 0.f, 0.f);
 
-  const int U = N / ES;
+  const int U = N / es;
   const int nunits = (CG + U - 1) / U;
   const Lanes L = lane_roles(lane, nunits);
 
-  // prefetch registers for the next batch
+  // registers of the next batch (prefetched while the current one is spread)
   long long np_ = -1;
   float nx3[3] = {0.f, 0.f, 0.f};
   float nv[2 * CGMAX];
@@ -652,101 +717,49 @@ __global__ void __launch_bounds__(32) interp_adj_kernel(Geo g, const int4* __res
     const int nb = min(32, it.z - b);
     __syncwarp();
     if (np_ >= 0) {
-      if (!lane_point_taps<NTB>(g, locs, np_, nx3, pbuf[lane])) pbuf[lane].n[0] = 0;
+      lane_rec<NTB>(g, nx3, o, false, rbuf[lane]);
 #pragma unroll
       for (int c = 0; c < CGMAX; ++c)
-        if (c < ncoil) {
+        if (c < CG) {
           if (es == 2) {
-            pv[lane * vstride + 2 * c] = nv[2 * c];
-            pv[lane * vstride + 2 * c + 1] = nv[2 * c + 1];
+            pv[lane * vstride + 2 * c] = c < ncoil ? nv[2 * c] : 0.f;
+            pv[lane * vstride + 2 * c + 1] = c < ncoil ? nv[2 * c + 1] : 0.f;
           } else {
-            pv[lane * vstride + c] = nv[c];
+            pv[lane * vstride + c] = c < ncoil ? nv[c] : 0.f;
           }
         }
     }
     __syncwarp();
     if (b + 32 < it.z) prefetch(b + 32);
     for (int jj = 0; jj < nb; ++jj) {
-      const Pt<NTB>& P = pbuf[jj];
+      const Rec<NTB>& R = rbuf[jj];
       // lanes of one warp update cells of consecutive points: order them
       __syncwarp();
-      if (P.n[0] == 0 || L.cu >= nunits) continue;
-      VecF<N> v;
-      {
-        const float* src = pv + jj * vstride + L.cu * N;
+      if (R.m[0] == 0 || L.cu >= nunits) continue;
+      const VecF<N> v = ldv<N>(pv + jj * vstride + L.cu * N);
+      float* base = acc + L.cu * N;
+      if (g.wrap_safe) {
+        for_lane_taps<NDIM, NTB>(g, R, L, [&](int lx, int ly, int lz, float w) {
+          float* a = base + ((size_t)(lx * T1 + ly) * T2 + lz) * vstride;
+          VecF<N> r = ldv<N>(a);
 #pragma unroll
-        for (int i = 0; i < N; ++i) v.v[i] = (L.cu * U + i / ES < ncoil) ? src[i] : 0.f;
-      }
-      if (!g.wrap_safe) {
-        // a window longer than the grid reaches a cell twice: taps in order, lanes by coil unit only
-        if (L.ux == 0 && L.uz == 0) {
-          for (int kx = 0; kx < P.n[0]; ++kx)
-            for (int ky = 0; ky < P.n[1]; ++ky)
-              for (int kz = 0; kz < P.n[2]; ++kz) {
-                const int lx = wrapi(P.st[0] + kx, g.N[0]) - o[0], ly = wrapi(P.st[1] + ky, g.N[1]) - o[1],
-                          lz = wrapi(P.st[2] + kz, g.N[2]) - o[2];
-                if (lx < 0 || lx >= g.T[0] || ly < 0 || ly >= g.T[1] || lz < 0 || lz >= g.T[2]) continue;
-                const float w = tap_w(g, P, kx, ky, kz);
-                float* a = acc + ((size_t)(lx * g.T[1] + ly) * g.T[2] + lz) * vstride + L.cu * N;
-                VecF<N> r = ldv<N>(a);
-#pragma unroll
-                for (int i = 0; i < N; ++i) r.v[i] = fmaf(w, v.v[i], r.v[i]);
-                stv<N>(a, r);
-              }
-        }
-        continue;
-      }
-      // taps of this lane; wrap by one subtraction (N >= taps)
-      auto tap_local = [&](int e, int k) {
-        int gg = P.st[e] + k;
-        if (gg >= g.N[e]) gg -= g.N[e];
-        return gg - o[e];
-      };
-      if constexpr (NDIM == 3) {
-        for (int kx = L.ux; kx < P.n[0]; kx += L.UX) {
-          const int lx = tap_local(0, kx);
-          if (lx < 0 || lx >= g.T[0]) continue;
-          for (int ky = 0; ky < P.n[1]; ++ky) {
-            const int ly = tap_local(1, ky);
-            if (ly < 0 || ly >= g.T[1]) continue;
-            for (int kz = L.uz; kz < P.n[2]; kz += 4) {
-              const int lz = tap_local(2, kz);
-              if (lz < 0 || lz >= g.T[2]) continue;
-              const float w = tap_w(g, P, kx, ky, kz);
-              float* a = acc + ((size_t)(lx * g.T[1] + ly) * g.T[2] + lz) * vstride + L.cu * N;
+          for (int i = 0; i < N; ++i) r.v[i] = fmaf(w, v.v[i], r.v[i]);
+          stv<N>(a, r);
+        });
+      } else if (L.ux == 0 && L.uz == 0) {
+        // a window longer than the grid reaches a cell twice: taps in order,
+        // lanes split by coil unit only
+        for (int kx = 0; kx < R.m[0]; ++kx)
+          for (int ky = 0; ky < R.m[1]; ++ky)
+            for (int kz = 0; kz < R.m[2]; ++kz) {
+              const float w = g.norm == 1 ? R.wv[0][kx] * R.wv[1][ky] * R.wv[2][kz]
+                                          : radial_w(g, R.wv[0][kx], R.wv[1][ky], R.wv[2][kz]);
+              float* a = base + ((size_t)(R.lc[0][kx] * T1 + R.lc[1][ky]) * T2 + R.lc[2][kz]) * vstride;
               VecF<N> r = ldv<N>(a);
 #pragma unroll
               for (int i = 0; i < N; ++i) r.v[i] = fmaf(w, v.v[i], r.v[i]);
               stv<N>(a, r);
             }
-          }
-        }
-      } else if constexpr (NDIM == 2) {
-        for (int ky = L.ux; ky < P.n[1]; ky += L.UX) {
-          const int ly = tap_local(1, ky);
-          if (ly < 0 || ly >= g.T[1]) continue;
-          for (int kz = L.uz; kz < P.n[2]; kz += 4) {
-            const int lz = tap_local(2, kz);
-            if (lz < 0 || lz >= g.T[2]) continue;
-            const float w = tap_w(g, P, 0, ky, kz);
-            float* a = acc + ((size_t)ly * g.T[2] + lz) * vstride + L.cu * N;
-            VecF<N> r = ldv<N>(a);
-#pragma unroll
-            for (int i = 0; i < N; ++i) r.v[i] = fmaf(w, v.v[i], r.v[i]);
-            stv<N>(a, r);
-          }
-        }
-      } else {
-        for (int kz = L.uz + 4 * L.ux; kz < P.n[2]; kz += 4 * L.UX) {
-          const int lz = tap_local(2, kz);
-          if (lz < 0 || lz >= g.T[2]) continue;
-          const float w = tap_w(g, P, 0, 0, kz);
-          float* a = acc + (size_t)lz * vstride + L.cu * N;
-          VecF<N> r = ldv<N>(a);
-#pragma unroll
-          for (int i = 0; i < N; ++i) r.v[i] = fmaf(w, v.v[i], r.v[i]);
-          stv<N>(a, r);
-        }
       }
     }
   }
@@ -759,14 +772,13 @@ __global__ void __launch_bounds__(32) interp_adj_kernel(Geo g, const int4* __res
   }
   // write the tile: per (x, y) row, lanes over (z, batch entry), z fastest
   const long long gvol = (long long)g.N[0] * g.N[1] * g.N[2];
-  const int T2 = g.T[2];
   const bool p2 = (T2 & (T2 - 1)) == 0;
   const int lg2 = lg2i(T2);
-  for (int row = 0; row < g.T[0] * g.T[1]; ++row) {
-    const int x = row / g.T[1], y = row - x * g.T[1];
+  for (int row = 0; row < g.T[0] * T1; ++row) {
+    const int x = row / T1, y = row - x * T1;
     const int gx = o[0] + x, gy = o[1] + y;
     if (gx >= g.N[0] || gy >= g.N[1]) continue;
-    const float* srow = acc + (size_t)(x * g.T[1] + y) * T2 * vstride;
+    const float* srow = acc + (size_t)(x * T1 + y) * T2 * vstride;
     float* drow = gridv + (((long long)gx * g.N[1] + gy) * g.N[2] + o[2]) * es;
     for (int idx = lane; idx < T2 * ncoil; idx += 32) {
       const int cc = p2 ? (idx >> lg2) : idx / T2;
@@ -1064,7 +1076,9 @@ int ntb_for(const Geo& g) {
   if (m <= 5) return 5;
   return g.ndim == 3 ? 9 : 16;
 }
-size_t pt_bytes(int ntb) { return 24 + 12 * (size_t)ntb; }
+size_t pt_bytes(int ntb) {
+  return ntb == 5 ? sizeof(Rec<5>) : (ntb == 9 ? sizeof(Rec<9>) : sizeof(Rec<16>));
+}
 
 int64_t region_vol(const Geo& g) {
   return (int64_t)(g.T[0] + g.NT[0] - 1) * (g.T[1] + g.NT[1] - 1) * (g.T[2] + g.NT[2] - 1);
