@@ -115,6 +115,32 @@ int tlgb_interp_adjoint(const tlgb_interp_desc* d, const tlgb_interp_plan_info* 
                         const float* locs, const void* vals, void* grid, void* scratch, size_t scratch_bytes,
                         tlgb_stream_t stream);
 
+/* Gridding exactly as tlgb_interp_adjoint, for callers that cannot allocate
+ * device memory when they grid: a host framework that only hands out memory
+ * from a pool reserved at start-up (a real-time reconstruction loop, a
+ * service with a fixed memory budget), or an FFI caller (cgo, JNI) with no
+ * allocator of its own, for which cudaMalloc would also synchronise the
+ * device mid-pipeline. It allocates nothing: the partial tiles of dense
+ * output tiles go to one file-scope device buffer of
+ * TLGB_ADJOINT_FIXED_SCRATCH_BYTES bytes that the library holds on every GPU
+ * it is loaded on until the process exits. The caller still provides the
+ * plan, the inputs and the output.
+ *  - A plan whose partial tiles need more than the buffer (see
+ *    tlgb_interp_adjoint_scratch_size) is rejected with TLGB_ERR_WORKSPACE
+ *    before anything is launched.
+ *  - The first call on a device looks up the buffer's device address (with
+ *    that device current) and remembers it; make that first call before any
+ *    stream capture.
+ *  - Every call shares the one buffer and it keeps the last call's contents;
+ *    nothing in it has to start at zero, because every partial tile is
+ *    written in full before it is read. Calls whose work overlaps on the GPU
+ *    (other streams, other host threads) race on the buffer: serialise them.
+ * No counterpart in the reference: torchlinops allocates its outputs and has
+ * no scratch. */
+#define TLGB_ADJOINT_FIXED_SCRATCH_BYTES ((size_t)32 << 20)
+int tlgb_interp_adjoint_fixed(const tlgb_interp_desc* d, const tlgb_interp_plan_info* info, const void* plan,
+                              const float* locs, const void* vals, void* grid, tlgb_stream_t stream);
+
 /* grad_locs[p, e] = sum_b Re( conj(a[b, p]) * sum_taps dw(p, tap)/dx_e * grid[b, tap] )
  * -- the gradient w.r.t. the trajectory of sum Re(conj(a) * ungrid(grid)),
  * and (with grid := the output cotangent, a := the point values) of the

@@ -1,0 +1,79 @@
+"""tlgb_interp_adjoint_fixed: gridding that allocates no device memory.
+
+It exists for callers that cannot allocate device memory at the moment they
+grid, e.g. a host framework that only hands out memory from a pool reserved
+at start-up, or an FFI caller without an allocator of its own for which
+cudaMalloc would synchronise the device mid-pipeline. It must give the same
+grid as tlgb_interp_adjoint (which takes the caller's scratch) on every call,
+although all calls share one fixed device buffer for the partial tiles of
+dense output tiles. This file is collected last so that a run stopping at its
+first failure has already run every other test; it also passes on its own.
+"""
+
+import ctypes
+
+import pytest
+import torch
+
+from conftest import rel_l2
+
+import torchlinops_gb300 as T
+from torchlinops_gb300 import _ext, interp
+
+pytestmark = pytest.mark.gpu
+DEV = "cuda"
+TOL = 1e-5
+
+
+def _dense_case():
+    gen = torch.Generator().manual_seed(77)
+    n, npts, nb = 64, 200_000, 8
+    r = torch.rand(npts, generator=gen) * (n / 2)
+    u = torch.randn(npts, 3, generator=gen)
+    locs = (n / 2 + r[:, None] * u / u.norm(dim=-1, keepdim=True)).float().to(DEV)
+    vals = torch.randn(nb, npts, dtype=torch.complex64, generator=gen).to(DEV)
+    return n, locs, vals
+
+
+def _fixed_call(desc, plan, locs, vals, out):
+    L = _ext.lib()
+    with torch.cuda.device(out.device):
+        return L.tlgb_interp_adjoint_fixed(
+            ctypes.byref(desc), ctypes.byref(plan.info), _ext.ptr(plan.buffer), _ext.ptr(locs),
+            _ext.ptr(torch.view_as_real(vals)), _ext.ptr(torch.view_as_real(out)), _ext.stream_ptr(out.device),
+        )
+
+
+def test_fixed_scratch_gridding_matches_caller_scratch_gridding():
+    n, locs, vals = _dense_case()
+    beta = T.kaiser_bessel_beta(4.0, 1.25)
+    ref = T.grid(vals, locs, (n, n, n), 4.0, kernel_params=dict(beta=beta))
+    plan = interp.get_plan(locs, (n, n, n), 4.0, "kaiser_bessel", "circular")
+    assert plan.info.n_partials > 0, "the case must exercise the partial-tile scratch"
+    desc = interp._desc(3, (n, n, n), (4.0,) * 3, "kaiser_bessel", 1, "circular", beta, True, vals.shape[0],
+                        vals.shape[1])
+    for _ in range(2):  # the second call sees the first call's buffer contents
+        out = torch.full((vals.shape[0], n, n, n), float("nan"), dtype=torch.complex64, device=DEV)
+        assert _fixed_call(desc, plan, locs, vals, out) == _ext.TLGB_OK, _ext.lib().tlgb_last_error()
+        torch.cuda.synchronize()
+        assert rel_l2(out.cpu(), ref.cpu()) <= TOL
+        assert torch.equal(out, ref)  # same kernels, fixed summation order
+
+
+def test_fixed_scratch_rejects_plans_beyond_its_buffer():
+    n, locs, vals = _dense_case()
+    plan = interp.get_plan(locs, (n, n, n), 4.0, "kaiser_bessel", "circular")
+    desc = interp._desc(3, (n, n, n), (4.0,) * 3, "kaiser_bessel", 1, "circular", 1.0, True, vals.shape[0],
+                        vals.shape[1])
+    big = _ext.PlanInfo()
+    ctypes.memmove(ctypes.byref(big), ctypes.byref(plan.info), ctypes.sizeof(big))
+    big.n_partials = 1 << 20  # far more partial tiles than the fixed buffer holds
+    out = torch.zeros((vals.shape[0], n, n, n), dtype=torch.complex64, device=DEV)
+
+    class _P:
+        info = big
+        buffer = plan.buffer
+
+    st = _fixed_call(desc, _P, locs, vals, out)
+    assert st == _ext.TLGB_ERR_WORKSPACE
+    assert b"fixed" in _ext.lib().tlgb_last_error()

@@ -33,7 +33,9 @@
 
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 #include <numeric>
+#include <string>
 #include <vector>
 
 #include "common.cuh"
@@ -1402,4 +1404,71 @@ extern "C" int tlgb_interp_grad_locs(const tlgb_interp_desc* d, const tlgb_inter
                        : launch_grad<float2, 2>(g, info, P, locs, grid, a, grad_locs, s);
   return g.norm == 1 ? launch_grad<float, 1>(g, info, P, locs, grid, a, grad_locs, s)
                      : launch_grad<float, 2>(g, info, P, locs, grid, a, grad_locs, s);
+}
+
+// ------------------------------------------------ gridding without allocation
+//
+// Some callers cannot allocate device memory at the moment they grid: a
+// host framework that hands out memory only from a pool reserved at start-up
+// (a scanner's real-time reconstruction loop, a service with a fixed memory
+// budget), or an FFI caller (cgo, JNI) that has no allocator of its own and
+// for which cudaMalloc would synchronise the device in the middle of a
+// pipeline. For them tlgb_interp_adjoint_fixed takes the partial-tile scratch
+// of dense tiles from this file-scope device buffer instead of from the
+// caller. The buffer is part of the loaded module: every GPU that loads the
+// library holds it until the process exits.
+
+namespace tlgb {
+namespace {
+constexpr size_t kFixedScratchBytes = TLGB_ADJOINT_FIXED_SCRATCH_BYTES;
+}  // namespace
+}  // namespace tlgb
+
+static __device__ __align__(256) unsigned char g_adjoint_fixed_scratch[tlgb::kFixedScratchBytes];
+
+namespace tlgb {
+namespace {
+
+constexpr int kMaxDevices = 256;
+std::mutex g_fixed_mu;
+void* g_fixed_addr[kMaxDevices] = {};
+
+// Device address of the fixed buffer on the current device, looked up once
+// per device (with that device current) and remembered.
+int fixed_scratch_address(void** out) {
+  int dev = 0;
+  TLGB_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) TLGB_FAIL(TLGB_ERR_UNSUPPORTED, "device ordinal out of range");
+  std::lock_guard<std::mutex> lock(g_fixed_mu);
+  if (g_fixed_addr[dev] == nullptr) {
+    void* p = nullptr;
+    TLGB_CUDA(cudaGetSymbolAddress(&p, g_adjoint_fixed_scratch));
+    g_fixed_addr[dev] = p;
+  }
+  *out = g_fixed_addr[dev];
+  return TLGB_OK;
+}
+
+}  // namespace
+}  // namespace tlgb
+
+extern "C" int tlgb_interp_adjoint_fixed(const tlgb_interp_desc* d, const tlgb_interp_plan_info* info,
+                                         const void* plan, const float* locs, const void* vals, void* grid,
+                                         tlgb_stream_t stream) {
+  Geo g;
+  TLGB_TRY(make_geo(d, g));
+  TLGB_TRY(check_plan(g, info, plan));
+  if (g.nbatch == 0) return TLGB_OK;
+  if (!grid || (g.npts > 0 && (!locs || !vals))) TLGB_FAIL(TLGB_ERR_INVALID, "null pointer");
+  size_t need = 0;
+  TLGB_TRY(tlgb_interp_adjoint_scratch_size(d, info, &need));
+  if (need > kFixedScratchBytes)
+    TLGB_FAIL(TLGB_ERR_WORKSPACE, "this plan needs " + std::to_string(need) +
+                                      " bytes of partial-tile scratch, more than the fixed " +
+                                      std::to_string(kFixedScratchBytes) +
+                                      "-byte device buffer of tlgb_interp_adjoint_fixed; use "
+                                      "tlgb_interp_adjoint with caller scratch");
+  void* scratch = nullptr;
+  if (need > 0) TLGB_TRY(fixed_scratch_address(&scratch));
+  return launch_adj(g, info, (const char*)plan, locs, vals, grid, scratch, (cudaStream_t)stream);
 }

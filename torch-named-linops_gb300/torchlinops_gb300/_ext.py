@@ -88,6 +88,7 @@ _SIGNATURES = {
     "tlgb_interp_forward": ([_P, _P, _P, _P, _P, _P, _P], ctypes.c_int),
     "tlgb_interp_adjoint": ([_P, _P, _P, _P, _P, _P, _P, ctypes.c_size_t, _P], ctypes.c_int),
     "tlgb_interp_grad_locs": ([_P, _P, _P, _P, _P, _P, _P, _P], ctypes.c_int),
+    "tlgb_interp_adjoint_fixed": ([_P, _P, _P, _P, _P, _P, _P], ctypes.c_int),
     "tlgb_unfold": ([_P, _P, _P, _P], ctypes.c_int),
     "tlgb_fold": ([_P, _P, _P, _P], ctypes.c_int),
     "tlgb_cg_scratch_bytes": ([], ctypes.c_size_t),
