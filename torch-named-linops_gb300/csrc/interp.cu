@@ -56,6 +56,8 @@ struct Geo {
   int nt[3];  // tiles per dim
   int NT[3];  // taps per dim (inactive: 1)
   float r[3]; // kernel radius W/2 per dim
+  float rinv[3];  // 1/r, used when r is a power of two (the product is then exact)
+  int rpow2[3];
   int act[3];
   int kernel, norm, pad, cplx;
   float beta;
@@ -125,7 +127,8 @@ struct Tap {
 __device__ __forceinline__ Tap tap_eval(const Geo& g, int e, float x, int lower, int k) {
   Tap t;
   const float gk = (float)(lower + k);
-  t.d = __fdiv_rn(__fsub_rn(x, gk), g.r[e]);
+  const float diff = __fsub_rn(x, gk);
+  t.d = g.rpow2[e] ? __fmul_rn(diff, g.rinv[e]) : __fdiv_rn(diff, g.r[e]);
   const float ad = fabsf(t.d);
   bool v = ad <= g.r[e];
   if (g.kernel == TLGB_KERNEL_KAISER_BESSEL) v = v && (ad <= 1.0f);
@@ -370,6 +373,7 @@ struct Rec {
   short lc[3][NTB];
   float wv[3][NTB];
   int m[3];
+  int fast;  // every dim has <= 4 kept taps at consecutive local coordinates
 };
 
 // One lane builds the record of point p (coordinates x3) for the tile with
@@ -418,6 +422,12 @@ __device__ __forceinline__ void lane_rec(const Geo& g, const float (&x3)[3], con
     if (cnt == 0) ok = false;
   }
   if (!ok) R.m[0] = 0;
+  bool fast = ok;
+  for (int e = 0; e < 3 && fast; ++e) {
+    const int m = R.m[e];
+    fast = m <= 4 && (m == 0 || (int)R.lc[e][m - 1] - (int)R.lc[e][0] == m - 1);
+  }
+  R.fast = fast ? 1 : 0;
 }
 
 // N floats moved as one vector (a "coil unit": 1 or 2 batch entries)
@@ -506,7 +516,7 @@ __device__ __forceinline__ void for_lane_taps(const Geo& g, const Rec<NTB>& R, c
 
 // CTA = NW warps sharing one staged region (tile + halo, [x][y][z][batch]);
 // each warp interpolates 32 home points per batch.
-template <int N, int NDIM, int NTB, int NW>
+template <int N, int NDIM, int NTB, int NW, bool F3>
 __global__ void __launch_bounds__(NW * 32, 1) interp_fwd_kernel(Geo g, const int4* __restrict__ items,
                                                                 const int32_t* __restrict__ entries,
                                                                 const float* __restrict__ locs,
@@ -621,7 +631,41 @@ __global__ void __launch_bounds__(NW * 32, 1) interp_fwd_kernel(Geo g, const int
       VecF<N> acc;
 #pragma unroll
       for (int i = 0; i < N; ++i) acc.v[i] = 0.f;
-      if (L.cu < nunits) {
+      bool done = false;
+      if constexpr (F3) {
+        // 3D, 8^3 tile + 4-wide halo (12^3 region), 8 complex batch entries
+        // (16 floats per voxel), <= 4 taps per dim: unrolled, immediate offsets
+        if (R.fast) {
+          constexpr int SZ = 16, SY = 12 * 16, SX = 12 * 12 * 16;
+          const bool zin = L.uz < R.m[2];
+          const float wz = zin ? R.wv[2][L.uz] : 0.f;
+          float wy[4];
+#pragma unroll
+          for (int ky = 0; ky < 4; ++ky) wy[ky] = ky < R.m[1] ? R.wv[1][ky] : 0.f;
+          const float* base = reg + (R.lc[0][0] * SX + R.lc[1][0] * SY + (R.lc[2][0] + L.uz) * SZ) + L.cu * 4;
+#pragma unroll
+          for (int i = 0; i < 2; ++i) {
+            const int kx = L.ux + 2 * i;
+            if (zin && kx < R.m[0]) {
+              const float wxz = R.wv[0][kx] * wz;
+              const float* bx = base + kx * SX;
+#pragma unroll
+              for (int ky = 0; ky < 4; ++ky) {
+                if (ky < R.m[1]) {
+                  const float w = wxz * wy[ky];
+                  const float4 v = *reinterpret_cast<const float4*>(bx + ky * SY);
+                  acc.v[0] = fmaf(w, v.x, acc.v[0]);
+                  acc.v[1] = fmaf(w, v.y, acc.v[1]);
+                  acc.v[2] = fmaf(w, v.z, acc.v[2]);
+                  acc.v[3] = fmaf(w, v.w, acc.v[3]);
+                }
+              }
+            }
+          }
+          done = true;
+        }
+      }
+      if (!done && L.cu < nunits) {
         const float* base = reg + L.cu * N;
         for_lane_taps<NDIM, NTB>(g, R, L, [&](int lx, int ly, int lz, float w) {
           const VecF<N> v = ldv<N>(base + ((size_t)(lx * S[1] + ly) * S[2] + lz) * vstride);
@@ -654,7 +698,7 @@ __global__ void __launch_bounds__(NW * 32, 1) interp_fwd_kernel(Geo g, const int
 
 // One warp per CTA owns one output tile in shared memory ([x][y][z][batch]),
 // so every cell is updated by one warp in plan order: deterministic.
-template <int N, int NDIM, int NTB>
+template <int N, int NDIM, int NTB, bool F3>
 __global__ void __launch_bounds__(32) interp_adj_kernel(Geo g, const int4* __restrict__ items,
                                                         const int32_t* __restrict__ entries,
                                                         const float* __restrict__ locs,
@@ -740,6 +784,43 @@ __global__ void __launch_bounds__(32) interp_adj_kernel(Geo g, const int4* __res
       if (R.m[0] == 0 || L.cu >= nunits) continue;
       const VecF<N> v = ldv<N>(pv + jj * vstride + L.cu * N);
       float* base = acc + L.cu * N;
+      if constexpr (F3) {
+        // 3D, 8^3 tile, 8 complex batch entries (16 floats per cell), <= 4
+        // taps per dim at consecutive cells: unrolled, immediate offsets
+        if (R.fast && g.wrap_safe) {
+          constexpr int SZ = 16, SY = 8 * 16, SX = 8 * 8 * 16;
+          const bool zin = L.uz < R.m[2];
+          const float wz = zin ? R.wv[2][L.uz] : 0.f;
+          float wy[4];
+#pragma unroll
+          for (int ky = 0; ky < 4; ++ky) wy[ky] = ky < R.m[1] ? R.wv[1][ky] : 0.f;
+          float* b0 = base + (R.lc[0][0] * SX + R.lc[1][0] * SY + (R.lc[2][0] + L.uz) * SZ);
+#pragma unroll
+          for (int i = 0; i < 2; ++i) {
+            const int kx = L.ux + 2 * i;
+            if (zin && kx < R.m[0]) {
+              const float wxz = R.wv[0][kx] * wz;
+              float* bx = b0 + kx * SX;
+              float4 r[4];
+#pragma unroll
+              for (int ky = 0; ky < 4; ++ky)
+                if (ky < R.m[1]) r[ky] = *reinterpret_cast<const float4*>(bx + ky * SY);
+#pragma unroll
+              for (int ky = 0; ky < 4; ++ky) {
+                if (ky < R.m[1]) {
+                  const float w = wxz * wy[ky];
+                  r[ky].x = fmaf(w, v.v[0], r[ky].x);
+                  r[ky].y = fmaf(w, v.v[1], r[ky].y);
+                  r[ky].z = fmaf(w, v.v[2], r[ky].z);
+                  r[ky].w = fmaf(w, v.v[3], r[ky].w);
+                  *reinterpret_cast<float4*>(bx + ky * SY) = r[ky];
+                }
+              }
+            }
+          }
+          continue;
+        }
+      }
       if (g.wrap_safe) {
         for_lane_taps<NDIM, NTB>(g, R, L, [&](int lx, int ly, int lz, float w) {
           float* a = base + ((size_t)(lx * T1 + ly) * T2 + lz) * vstride;
@@ -772,20 +853,21 @@ __global__ void __launch_bounds__(32) interp_adj_kernel(Geo g, const int4* __res
       *reinterpret_cast<float4*>(dst + i) = *reinterpret_cast<const float4*>(acc + i);
     return;
   }
-  // write the tile: per (x, y) row, lanes over (z, batch entry), z fastest
+  // write the tile: per (x, y) row, lanes over (batch entry, z) with the
+  // batch entry fastest, so shared-memory reads are contiguous
   const long long gvol = (long long)g.N[0] * g.N[1] * g.N[2];
-  const bool p2 = (T2 & (T2 - 1)) == 0;
-  const int lg2 = lg2i(T2);
+  const int cgp = CG <= 1 ? 1 : (CG <= 2 ? 2 : (CG <= 4 ? 4 : 8));
+  const int lgc = lg2i(cgp);
   for (int row = 0; row < g.T[0] * T1; ++row) {
     const int x = row / T1, y = row - x * T1;
     const int gx = o[0] + x, gy = o[1] + y;
     if (gx >= g.N[0] || gy >= g.N[1]) continue;
     const float* srow = acc + (size_t)(x * T1 + y) * T2 * vstride;
     float* drow = gridv + (((long long)gx * g.N[1] + gy) * g.N[2] + o[2]) * es;
-    for (int idx = lane; idx < T2 * ncoil; idx += 32) {
-      const int cc = p2 ? (idx >> lg2) : idx / T2;
-      const int z = idx - cc * T2;
-      if (o[2] + z >= g.N[2]) continue;
+    for (int idx = lane; idx < T2 * cgp; idx += 32) {
+      const int cc = idx & (cgp - 1);
+      const int z = idx >> lgc;
+      if (cc >= ncoil || o[2] + z >= g.N[2]) continue;
       const float* sp = srow + z * vstride + cc * es;
       float* d = drow + ((long long)(c0 + cc) * gvol + z) * es;
       if (es == 2)
@@ -1001,6 +1083,12 @@ int make_geo(const tlgb_interp_desc* d, Geo& g) {
     g.N[e] = (int)n;
     g.NT[e] = nt;
     g.r[e] = w / 2.0f;
+    {
+      int ex = 0;
+      const float mant = frexpf(g.r[e], &ex);
+      g.rpow2[e] = (mant == 0.5f) ? 1 : 0;
+      g.rinv[e] = 1.0f / g.r[e];
+    }
     g.act[e] = 1;
     maxnt = std::max(maxnt, nt);
   }
@@ -1263,12 +1351,18 @@ extern "C" int tlgb_interp_adjoint_scratch_size(const tlgb_interp_desc* d, const
 namespace tlgb {
 namespace {
 
-template <int N, int NDIM, int NTB>
-int launch_fwd_t(const Geo& g, int cg, const tlgb_interp_plan_info* info, const char* P, const float* locs,
-                 const void* grid, void* out, cudaStream_t s) {
+// the unrolled paths: 3D, 8^3 tiles, 5 taps per dim (width in (3, 4]), 8 complex batch entries
+bool fast3(const Geo& g, int cg) {
+  return g.ndim == 3 && g.cplx && cg == 8 && g.T[0] == 8 && g.T[1] == 8 && g.T[2] == 8 && g.NT[0] == 5 &&
+         g.NT[1] == 5 && g.NT[2] == 5;
+}
+
+template <int N, int NDIM, int NTB, bool F3>
+int launch_fwd_t2(const Geo& g, int cg, const tlgb_interp_plan_info* info, const char* P, const float* locs,
+                  const void* grid, void* out, cudaStream_t s) {
   const int64_t ncg = cdiv(g.nbatch, cg);
   const size_t sm = fwd_smem(g, cg);
-  auto* k = interp_fwd_kernel<N, NDIM, NTB, NWF>;
+  auto* k = interp_fwd_kernel<N, NDIM, NTB, NWF, F3>;
   TLGB_TRY(set_smem(k, sm));
   dim3 grd((unsigned)info->n_fwd_items, (unsigned)ncg);
   k<<<grd, NWF * 32, sm, s>>>(g, (const int4*)(P + info->off_fwd_items), (const int32_t*)(P + info->off_entries),
@@ -1277,12 +1371,12 @@ int launch_fwd_t(const Geo& g, int cg, const tlgb_interp_plan_info* info, const 
   return TLGB_OK;
 }
 
-template <int N, int NDIM, int NTB>
-int launch_adj_t(const Geo& g, int cg, const tlgb_interp_plan_info* info, const char* P, const float* locs,
-                 const void* vals, void* grid, void* scratch, cudaStream_t s) {
+template <int N, int NDIM, int NTB, bool F3>
+int launch_adj_t2(const Geo& g, int cg, const tlgb_interp_plan_info* info, const char* P, const float* locs,
+                  const void* vals, void* grid, void* scratch, cudaStream_t s) {
   const int64_t ncg = cdiv(g.nbatch, cg);
   const size_t sm = adj_smem(g, cg);
-  auto* k = interp_adj_kernel<N, NDIM, NTB>;
+  auto* k = interp_adj_kernel<N, NDIM, NTB, F3>;
   TLGB_TRY(set_smem(k, sm));
   dim3 grd((unsigned)info->n_adj_items, (unsigned)ncg);
   k<<<grd, 32, sm, s>>>(g, (const int4*)(P + info->off_adj_items), (const int32_t*)(P + info->off_entries), locs,
@@ -1295,6 +1389,22 @@ int launch_adj_t(const Geo& g, int cg, const tlgb_interp_plan_info* info, const 
     TLGB_CHECK_LAUNCH();
   }
   return TLGB_OK;
+}
+
+template <int N, int NDIM, int NTB>
+int launch_fwd_t(const Geo& g, int cg, const tlgb_interp_plan_info* info, const char* P, const float* locs,
+                 const void* grid, void* out, cudaStream_t s) {
+  if constexpr (N == 4 && NDIM == 3 && NTB == 5)
+    if (fast3(g, cg)) return launch_fwd_t2<N, NDIM, NTB, true>(g, cg, info, P, locs, grid, out, s);
+  return launch_fwd_t2<N, NDIM, NTB, false>(g, cg, info, P, locs, grid, out, s);
+}
+
+template <int N, int NDIM, int NTB>
+int launch_adj_t(const Geo& g, int cg, const tlgb_interp_plan_info* info, const char* P, const float* locs,
+                 const void* vals, void* grid, void* scratch, cudaStream_t s) {
+  if constexpr (N == 4 && NDIM == 3 && NTB == 5)
+    if (fast3(g, cg)) return launch_adj_t2<N, NDIM, NTB, true>(g, cg, info, P, locs, vals, grid, scratch, s);
+  return launch_adj_t2<N, NDIM, NTB, false>(g, cg, info, P, locs, vals, grid, scratch, s);
 }
 
 // floats per coil unit: 2 batch entries per unit when the group size is even
