@@ -72,7 +72,7 @@ def test_array_to_blocks_linop():
     y = torch.randn(2, 13, 13, 13, 9, device=DEV)
     lhs = torch.vdot(A(x).flatten().double(), y.flatten().double())
     rhs = torch.vdot(x.flatten().double(), A.H(y).flatten().double())
-    assert abs(lhs - rhs) / abs(lhs) < 1e-6
+    assert abs(lhs - rhs) / abs(lhs) < 1e-4  # float32 outputs, cancelling sum
     torch.testing.assert_close(A.N(x), A.H(A(x)))
     assert isinstance(A.H, linops.BlocksToArray)
 

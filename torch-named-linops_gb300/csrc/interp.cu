@@ -360,6 +360,11 @@ __device__ __forceinline__ float kb_fast(float x, float beta) {
   return expf(z) * rsqrtf(z) * q;
 }
 
+__device__ __forceinline__ float kb_approx(float ax, float beta);
+__device__ __forceinline__ float kern_value_approx(int kernel, float ax, float beta) {
+  return kernel == TLGB_KERNEL_KAISER_BESSEL ? kb_approx(ax, beta) : fmaxf(1.0f - ax, 0.0f);
+}
+
 __device__ __forceinline__ float kern_fast(int kernel, float ax, float beta) {
   return kernel == TLGB_KERNEL_KAISER_BESSEL ? kb_fast(ax, beta) : fmaxf(1.0f - ax, 0.0f);
 }
@@ -878,6 +883,392 @@ __global__ void __launch_bounds__(32) interp_adj_kernel(Geo g, const int4* __res
   }
 }
 
+// ----------------------------------------- unrolled kernels of the 3D default
+//
+// 3D grids, 8^3 tiles, widths in (3, 4] (5 tap slots, <= 4 kept for
+// non-integer coordinates), 8 complex batch entries per CTA: the benchmark
+// configuration and the NUFFT default. Each point's taps are packed into a
+// 64-byte record read with vector loads; tap offsets are compile-time.
+
+// KB value for the weights only (the tap masks stay exact): the same A&S
+// expansions as kb_value evaluated with the approximate square root, divide
+// and exponential intrinsics; agrees with kb_value to ~3e-7 relative.
+__device__ __forceinline__ float kb_approx(float ax, float beta) {
+  const float u1 = __fsub_rn(1.0f, __fmul_rn(ax, ax));
+  const float z = beta * (u1 > 0.f ? u1 * rsqrtf(u1) : 0.f);
+  if (z < 3.75f) {
+    const float u = (z * (1.0f / 3.75f)) * (z * (1.0f / 3.75f));
+    return 1.0f + u * (3.5156229f + u * (3.0899424f + u * (1.2067492f + u * (0.2659732f +
+           u * (0.0360768f + u * 0.0045813f)))));
+  }
+  const float rz = __frcp_rn(z);
+  const float v = 3.75f * rz;
+  const float q = 0.39894228f + v * (0.01328592f + v * (0.00225319f + v * (-0.00157565f + v * (0.00916281f +
+                  v * (-0.02057706f + v * (0.02635537f + v * (-0.01647633f + v * 0.00392377f)))))));
+  return __expf(z) * rsqrtf(z) * q;
+}
+
+struct __align__(16) R3 {
+  float4 wx, wy, wz;  // weights of the kept taps, zero beyond the count
+  int base;           // local linear voxel offset of the first kept tap
+  int m;              // mx | my << 8 | mz << 16 | fast << 24
+  int p;              // point index
+  int pad;
+};
+
+// One lane packs the record of point p. region: gather mode (8^3 tile +
+// halo, 12^3 staged region, contiguous taps from the wrapped start); else
+// the 8^3 output tile, taps outside it dropped. fast = every dim keeps <= 4
+// taps at consecutive local coordinates.
+template <bool REGION>
+__device__ __forceinline__ void lane_rec3(const Geo& g, const float (&x3)[3], const int (&o)[3], long long p,
+                                          R3& R) {
+  constexpr int SD = REGION ? 12 : 8;
+  float4 w4[3];
+  int first[3], cnt[3];
+  bool ok = true, fast = true;
+#pragma unroll
+  for (int e = 0; e < 3; ++e) {
+    float w0 = 0.f, w1 = 0.f, w2 = 0.f, w3 = 0.f;  // kept-tap weights, in registers
+    first[e] = 0;
+    cnt[e] = 0;
+    const float x = x3[e];
+    if (ok && coord_ok(x)) {
+      const int lower = lower_of(g, e, x);
+      int s = -1, last = -100, c = 0;
+#pragma unroll
+      for (int k = 0; k < 5; ++k) {
+        const Tap t = tap_eval(g, e, x, lower, k);
+        if (t.valid) {
+          if (s < 0) s = k;
+          int l;
+          bool keep = true;
+          if (REGION) {
+            int st = lower + s;
+            if (g.pad == TLGB_PAD_CIRCULAR) st = wrapi(st, g.N[e]);
+            l = st - o[e] + (k - s);
+          } else {
+            int gg = lower + k;
+            if (g.pad == TLGB_PAD_CIRCULAR) gg = wrapi(gg, g.N[e]);
+            l = gg - o[e];
+            keep = l >= 0 && l < SD;
+          }
+          if (keep) {
+            if (c == 0) first[e] = l;
+            else if (l != last + 1) fast = false;
+            last = l;
+            const float v = kern_value_approx(g.kernel, fabsf(t.d), g.beta);
+            w0 = c == 0 ? v : w0;
+            w1 = c == 1 ? v : w1;
+            w2 = c == 2 ? v : w2;
+            w3 = c == 3 ? v : w3;
+            if (c >= 4) fast = false;
+            ++c;
+          }
+        }
+      }
+      cnt[e] = c;
+      if (c == 0) ok = false;
+    } else {
+      ok = false;
+    }
+    w4[e] = make_float4(w0, w1, w2, w3);
+  }
+  R.wx = w4[0];
+  R.wy = w4[1];
+  R.wz = w4[2];
+  R.base = (first[0] * SD + first[1]) * SD + first[2];
+  R.m = ok ? (min(cnt[0], 255) | (min(cnt[1], 255) << 8) | (min(cnt[2], 255) << 16) | ((fast ? 1 : 0) << 24)) : 0;
+  R.p = (int)p;
+  R.pad = 0;
+}
+
+__device__ __forceinline__ float pick4(const float4& v, int i) {
+  return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
+}
+
+// Gridding: CTA = 2 warps owning one 8^3 x 8-entry output tile; warp w owns
+// batch entries 4w..4w+3 (two float4 units), so the warps never touch the
+// same shared-memory word and each word is updated in plan order.
+__global__ void __launch_bounds__(64, 5) adj_f3_kernel(Geo g, const int4* __restrict__ items,
+                                                    const int32_t* __restrict__ entries,
+                                                    const float* __restrict__ locs, const float* __restrict__ vals,
+                                                    float* __restrict__ gridv, float* __restrict__ partial) {
+  constexpr int CG = 8, VS = 16, SZ = 16, SY = 8 * 16, SX = 8 * 8 * 16, TFL = 512 * 16, NB = 64;
+  extern __shared__ __align__(16) unsigned char smem[];
+  float* acc = reinterpret_cast<float*>(smem);                       // [8][8][8][16]
+  R3* rec = reinterpret_cast<R3*>(smem + TFL * sizeof(float));      // [64]
+  float* pv = reinterpret_cast<float*>(rec + NB);                   // [64][16]
+  Rec<5>* slow = reinterpret_cast<Rec<5>*>(pv + NB * VS);          // [2] generic records
+  const int4 it = items[blockIdx.x];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int cg = blockIdx.y;
+  const int c0 = cg * CG;
+  const int ncoil = (int)min((long long)CG, g.nbatch - c0);
+  int o[3];
+  {
+    int t = it.x;
+    o[2] = (t % g.nt[2]) * 8;
+    t /= g.nt[2];
+    o[1] = (t % g.nt[1]) * 8;
+    o[0] = (t / g.nt[1]) * 8;
+  }
+  for (int i = tid * 4; i < TFL; i += 256) *reinterpret_cast<float4*>(acc + i) = make_float4(0.f, 0.f, 0.f, 0.f);
+
+  // lane roles in a warp: cu (2 units of this warp), uz = z tap, ux = x tap
+  const int cu = lane & 1, uz = (lane >> 1) & 3, ux = lane >> 3;
+  const int unit = warp * 2 + cu;  // float4 unit = batch entries 2*unit, 2*unit+1
+  const int lofs = ux * SX + uz * SZ + unit * 4;
+
+  for (int b = it.y; b < it.z; b += NB) {
+    const int nb = min(NB, it.z - b);
+    __syncthreads();
+    if (tid < nb) {
+      const long long p = entries[b + tid];
+      float x3[3];
+      for (int e = 0; e < 3; ++e) x3[e] = load_coord(g, locs, p, e);
+      lane_rec3<false>(g, x3, o, p, rec[tid]);
+      float* d = pv + tid * VS;
+#pragma unroll
+      for (int c = 0; c < CG; ++c) {
+        float2 v = make_float2(0.f, 0.f);
+        if (c < ncoil) v = __ldg(reinterpret_cast<const float2*>(vals) + (long long)(c0 + c) * g.npts + p);
+        *reinterpret_cast<float2*>(d + 2 * c) = v;
+      }
+    }
+    __syncthreads();
+    for (int j = 0; j < nb; ++j) {
+      const R3& R = rec[j];
+      __syncwarp();
+      const int m = R.m;
+      if (m == 0) continue;
+      const float4 v = *reinterpret_cast<const float4*>(pv + j * VS + unit * 4);
+      if ((m >> 24) && g.wrap_safe) {
+        const int mx = m & 255, my = (m >> 8) & 255, mz = (m >> 16) & 255;
+        if (ux < mx && uz < mz) {
+          const float wxz = pick4(R.wx, ux) * pick4(R.wz, uz);
+          const float4 wy = R.wy;
+          float* a = acc + R.base * VS + lofs;
+          float4 r0 = *reinterpret_cast<float4*>(a);
+          float4 r1, r2, r3;
+          if (my > 1) r1 = *reinterpret_cast<float4*>(a + SY);
+          if (my > 2) r2 = *reinterpret_cast<float4*>(a + 2 * SY);
+          if (my > 3) r3 = *reinterpret_cast<float4*>(a + 3 * SY);
+          float w = wxz * wy.x;
+          r0.x = fmaf(w, v.x, r0.x); r0.y = fmaf(w, v.y, r0.y); r0.z = fmaf(w, v.z, r0.z); r0.w = fmaf(w, v.w, r0.w);
+          *reinterpret_cast<float4*>(a) = r0;
+          if (my > 1) {
+            w = wxz * wy.y;
+            r1.x = fmaf(w, v.x, r1.x); r1.y = fmaf(w, v.y, r1.y); r1.z = fmaf(w, v.z, r1.z); r1.w = fmaf(w, v.w, r1.w);
+            *reinterpret_cast<float4*>(a + SY) = r1;
+          }
+          if (my > 2) {
+            w = wxz * wy.z;
+            r2.x = fmaf(w, v.x, r2.x); r2.y = fmaf(w, v.y, r2.y); r2.z = fmaf(w, v.z, r2.z); r2.w = fmaf(w, v.w, r2.w);
+            *reinterpret_cast<float4*>(a + 2 * SY) = r2;
+          }
+          if (my > 3) {
+            w = wxz * wy.w;
+            r3.x = fmaf(w, v.x, r3.x); r3.y = fmaf(w, v.y, r3.y); r3.z = fmaf(w, v.z, r3.z); r3.w = fmaf(w, v.w, r3.w);
+            *reinterpret_cast<float4*>(a + 3 * SY) = r3;
+          }
+        }
+        continue;
+      }
+      // exact-integer coordinates (5 taps) or a window wrapping inside the
+      // tile: the generic record, taps in order
+      if (lane == 0) {
+        float x3[3];
+        for (int e = 0; e < 3; ++e) x3[e] = load_coord(g, locs, R.p, e);
+        lane_rec<5>(g, x3, o, false, slow[warp]);
+      }
+      __syncwarp();
+      const Rec<5>& S = slow[warp];
+      if (S.m[0] > 0 && lane < 2) {
+        float* base = acc + (warp * 2 + lane) * 4;
+        for (int kx = 0; kx < S.m[0]; ++kx)
+          for (int ky = 0; ky < S.m[1]; ++ky)
+            for (int kz = 0; kz < S.m[2]; ++kz) {
+              const float w = g.norm == 1 ? S.wv[0][kx] * S.wv[1][ky] * S.wv[2][kz]
+                                          : radial_w(g, S.wv[0][kx], S.wv[1][ky], S.wv[2][kz]);
+              float* a = base + ((S.lc[0][kx] * 8 + S.lc[1][ky]) * 8 + S.lc[2][kz]) * VS;
+              const float4 vv = *reinterpret_cast<const float4*>(pv + j * VS + (warp * 2 + lane) * 4);
+              float4 r = *reinterpret_cast<float4*>(a);
+              r.x = fmaf(w, vv.x, r.x); r.y = fmaf(w, vv.y, r.y); r.z = fmaf(w, vv.z, r.z); r.w = fmaf(w, vv.w, r.w);
+              *reinterpret_cast<float4*>(a) = r;
+            }
+      }
+    }
+  }
+  __syncthreads();
+  if (it.w >= 0) {
+    float* dst = partial + ((long long)it.w * gridDim.y + cg) * TFL;
+    for (int i = tid * 4; i < TFL; i += 256)
+      *reinterpret_cast<float4*>(dst + i) = *reinterpret_cast<const float4*>(acc + i);
+    return;
+  }
+  // write-out: per (x, y) row 8 z x 8 entries; lanes (entry fastest, z)
+  const long long gvol = (long long)g.N[0] * g.N[1] * g.N[2];
+  for (int row = warp; row < 64; row += 2) {
+    const int x = row >> 3, y = row & 7;
+    const int gx = o[0] + x, gy = o[1] + y;
+    if (gx >= g.N[0] || gy >= g.N[1]) continue;
+    const float* srow = acc + row * 8 * VS;
+    float* drow = gridv + (((long long)gx * g.N[1] + gy) * g.N[2] + o[2]) * 2;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int idx = lane + 32 * h;
+      const int c = idx & 7, z = idx >> 3;
+      if (c < ncoil && o[2] + z < g.N[2])
+        *reinterpret_cast<float2*>(drow + ((long long)(c0 + c) * gvol + z) * 2) =
+            *reinterpret_cast<const float2*>(srow + z * VS + c * 2);
+    }
+  }
+}
+
+// Gather: CTA = 16 warps sharing the staged 12^3 x 8-entry region
+// ([x][y][z][entry], entry fastest); warp = 32 points per batch, one at a
+// time, lanes (x-tap parity, z-tap, entry pair).
+__global__ void __launch_bounds__(512, 1) fwd_f3_kernel(Geo g, const int4* __restrict__ items,
+                                                        const int32_t* __restrict__ entries,
+                                                        const float* __restrict__ locs,
+                                                        const float* __restrict__ gridv, float* __restrict__ out) {
+  constexpr int CG = 8, VS = 16, S = 12, SZ = 16, SY = 12 * 16, SX = 12 * 12 * 16, RFL = S * S * S * VS, NW = 16;
+  extern __shared__ __align__(16) unsigned char smem[];
+  float* reg = reinterpret_cast<float*>(smem);                          // [12][12][12][16]
+  R3* recs = reinterpret_cast<R3*>(smem + RFL * sizeof(float));        // [16][32]
+  Rec<5>* slow = reinterpret_cast<Rec<5>*>(recs + NW * 32);            // [16]
+  const int4 it = items[blockIdx.x];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int c0 = blockIdx.y * CG;
+  const int ncoil = (int)min((long long)CG, g.nbatch - c0);
+  int o[3];
+  {
+    int t = it.x;
+    o[2] = (t % g.nt[2]) * 8;
+    t /= g.nt[2];
+    o[1] = (t % g.nt[1]) * 8;
+    o[0] = (t / g.nt[1]) * 8;
+  }
+  // stage: 144 (x, y) rows of 12 z x 8 entries = 96 float2; 3 loads per lane
+  const long long gvol = (long long)g.N[0] * g.N[1] * g.N[2];
+  for (int row = warp; row < S * S; row += NW) {
+    const int x = row / S, y = row - (row / S) * S;
+    int gx = o[0] + x, gy = o[1] + y;
+    bool rin = true;
+    if (g.pad == TLGB_PAD_CIRCULAR) {
+      gx = wrapi(gx, g.N[0]);
+      gy = wrapi(gy, g.N[1]);
+    } else {
+      rin = gx < g.N[0] && gy < g.N[1];
+    }
+    const long long rbase = ((long long)gx * g.N[1] + gy) * g.N[2];
+    float2 vv[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const int idx = lane + 32 * i;
+      const int c = idx & 7, z = idx >> 3;
+      int gz = o[2] + z;
+      bool in = rin && c < ncoil;
+      if (g.pad == TLGB_PAD_CIRCULAR) gz = wrapi(gz, g.N[2]);
+      else in = in && gz < g.N[2];
+      vv[i] = in ? __ldg(reinterpret_cast<const float2*>(gridv) + (long long)(c0 + c) * gvol + rbase + gz)
+                 : make_float2(0.f, 0.f);
+    }
+    float* rdst = reg + row * S * VS;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const int idx = lane + 32 * i;
+      *reinterpret_cast<float2*>(rdst + (idx >> 3) * VS + (idx & 7) * 2) = vv[i];
+    }
+  }
+  __syncthreads();
+
+  const int cu = lane & 3, uz = (lane >> 2) & 3, ux = lane >> 4;  // ux in {0, 1}: x taps ux, ux + 2
+  const int lofs = ux * SX + uz * SZ + cu * 4;
+  R3* rbuf = recs + warp * 32;
+  for (int b = it.y + warp * 32; b < it.z; b += NW * 32) {
+    const int nb = min(32, it.z - b);
+    if (lane < nb) {
+      const long long p = entries[b + lane];
+      float x3[3];
+      for (int e = 0; e < 3; ++e) x3[e] = load_coord(g, locs, p, e);
+      lane_rec3<true>(g, x3, o, p, rbuf[lane]);
+    }
+    __syncwarp();
+    for (int j = 0; j < nb; ++j) {
+      const R3& R = rbuf[j];
+      const int m = R.m;
+      if (m == 0) continue;  // warp-uniform
+      float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (m >> 24) {
+        const int mx = m & 255, my = (m >> 8) & 255, mz = (m >> 16) & 255;
+        if (uz < mz) {
+          const float wz = pick4(R.wz, uz);
+          const float4 wy = R.wy;
+          const float* a = reg + R.base * VS + lofs;
+#pragma unroll
+          for (int i = 0; i < 2; ++i) {
+            if (ux + 2 * i < mx) {
+              const float wxz = pick4(R.wx, ux + 2 * i) * wz;
+              const float* ax = a + 2 * i * SX;
+#pragma unroll
+              for (int ky = 0; ky < 4; ++ky) {
+                if (ky < my) {
+                  const float w = wxz * pick4(wy, ky);
+                  const float4 v = *reinterpret_cast<const float4*>(ax + ky * SY);
+                  acc.x = fmaf(w, v.x, acc.x);
+                  acc.y = fmaf(w, v.y, acc.y);
+                  acc.z = fmaf(w, v.z, acc.z);
+                  acc.w = fmaf(w, v.w, acc.w);
+                }
+              }
+            }
+          }
+        }
+      } else {
+        // exact-integer coordinates: generic record, lanes = (x, z taps, unit)
+        if (lane == 0) {
+          float x3[3];
+          for (int e = 0; e < 3; ++e) x3[e] = load_coord(g, locs, R.p, e);
+          lane_rec<5>(g, x3, o, true, slow[warp]);
+        }
+        __syncwarp();
+        const Rec<5>& Sr = slow[warp];
+        for (int kz = uz; kz < Sr.m[2]; kz += 4)
+          for (int kx = ux; kx < Sr.m[0]; kx += 2)
+            for (int ky = 0; ky < Sr.m[1]; ++ky) {
+              const float w = g.norm == 1 ? Sr.wv[0][kx] * Sr.wv[1][ky] * Sr.wv[2][kz]
+                                          : radial_w(g, Sr.wv[0][kx], Sr.wv[1][ky], Sr.wv[2][kz]);
+              const float4 v = *reinterpret_cast<const float4*>(
+                  reg + ((Sr.lc[0][kx] * S + Sr.lc[1][ky]) * S + Sr.lc[2][kz]) * VS + cu * 4);
+              acc.x = fmaf(w, v.x, acc.x);
+              acc.y = fmaf(w, v.y, acc.y);
+              acc.z = fmaf(w, v.z, acc.z);
+              acc.w = fmaf(w, v.w, acc.w);
+            }
+        __syncwarp();
+      }
+#pragma unroll
+      for (int mm = 4; mm < 32; mm <<= 1) {
+        acc.x += __shfl_xor_sync(0xffffffffu, acc.x, mm);
+        acc.y += __shfl_xor_sync(0xffffffffu, acc.y, mm);
+        acc.z += __shfl_xor_sync(0xffffffffu, acc.z, mm);
+        acc.w += __shfl_xor_sync(0xffffffffu, acc.w, mm);
+      }
+      if (lane < 4) {
+        const long long pj = R.p;
+        const int c = 2 * cu;
+        if (c < ncoil)
+          *reinterpret_cast<float2*>(out + ((long long)(c0 + c) * g.npts + pj) * 2) = make_float2(acc.x, acc.y);
+        if (c + 1 < ncoil)
+          *reinterpret_cast<float2*>(out + ((long long)(c0 + c + 1) * g.npts + pj) * 2) = make_float2(acc.z, acc.w);
+      }
+    }
+    __syncwarp();
+  }
+}
+
 // Sum the partial tiles of one split tile in slot order and write it out.
 __global__ void __launch_bounds__(NTHR) adj_reduce_kernel(Geo g, const int4* __restrict__ split,
                                                           const float* __restrict__ partial,
@@ -1051,7 +1442,7 @@ struct PlanLayout {
 };
 
 constexpr int64_t kFwdChunk = 512;
-constexpr int64_t kAdjChunk = 2048;
+constexpr int64_t kAdjChunk = 512;
 
 int make_geo(const tlgb_interp_desc* d, Geo& g) {
   if (!d) TLGB_FAIL(TLGB_ERR_INVALID, "null interp descriptor");
@@ -1353,7 +1744,7 @@ namespace {
 
 // the unrolled paths: 3D, 8^3 tiles, 5 taps per dim (width in (3, 4]), 8 complex batch entries
 bool fast3(const Geo& g, int cg) {
-  return g.ndim == 3 && g.cplx && cg == 8 && g.T[0] == 8 && g.T[1] == 8 && g.T[2] == 8 && g.NT[0] == 5 &&
+  return g.ndim == 3 && g.cplx && cg == 8 && g.norm == 1 && g.T[0] == 8 && g.T[1] == 8 && g.T[2] == 8 && g.NT[0] == 5 &&
          g.NT[1] == 5 && g.NT[2] == 5;
 }
 
@@ -1391,11 +1782,41 @@ int launch_adj_t2(const Geo& g, int cg, const tlgb_interp_plan_info* info, const
   return TLGB_OK;
 }
 
+int launch_fwd_f3(const Geo& g, const tlgb_interp_plan_info* info, const char* P, const float* locs,
+                  const void* grid, void* out, cudaStream_t s) {
+  const int64_t ncg = cdiv(g.nbatch, 8);
+  const size_t sm = 12 * 12 * 12 * 16 * sizeof(float) + 16 * 32 * sizeof(R3) + 16 * sizeof(Rec<5>);
+  TLGB_TRY(set_smem(fwd_f3_kernel, sm));
+  dim3 grd((unsigned)info->n_fwd_items, (unsigned)ncg);
+  fwd_f3_kernel<<<grd, 512, sm, s>>>(g, (const int4*)(P + info->off_fwd_items), (const int32_t*)(P + info->off_entries),
+                                     locs, (const float*)grid, (float*)out);
+  TLGB_CHECK_LAUNCH();
+  return TLGB_OK;
+}
+
+int launch_adj_f3(const Geo& g, const tlgb_interp_plan_info* info, const char* P, const float* locs,
+                  const void* vals, void* grid, void* scratch, cudaStream_t s) {
+  const int64_t ncg = cdiv(g.nbatch, 8);
+  const size_t sm = 512 * 16 * sizeof(float) + 64 * sizeof(R3) + 64 * 16 * sizeof(float) + 2 * sizeof(Rec<5>);
+  TLGB_TRY(set_smem(adj_f3_kernel, sm));
+  dim3 grd((unsigned)info->n_adj_items, (unsigned)ncg);
+  adj_f3_kernel<<<grd, 64, sm, s>>>(g, (const int4*)(P + info->off_adj_items), (const int32_t*)(P + info->off_entries),
+                                    locs, (const float*)vals, (float*)grid, (float*)scratch);
+  TLGB_CHECK_LAUNCH();
+  if (info->n_split_tiles > 0) {
+    dim3 g2((unsigned)info->n_split_tiles, (unsigned)ncg);
+    adj_reduce_kernel<<<g2, NTHR, 0, s>>>(g, (const int4*)(P + info->off_split), (const float*)scratch, (float*)grid,
+                                          8, (int)ncg);
+    TLGB_CHECK_LAUNCH();
+  }
+  return TLGB_OK;
+}
+
 template <int N, int NDIM, int NTB>
 int launch_fwd_t(const Geo& g, int cg, const tlgb_interp_plan_info* info, const char* P, const float* locs,
                  const void* grid, void* out, cudaStream_t s) {
   if constexpr (N == 4 && NDIM == 3 && NTB == 5)
-    if (fast3(g, cg)) return launch_fwd_t2<N, NDIM, NTB, true>(g, cg, info, P, locs, grid, out, s);
+    if (fast3(g, cg)) return launch_fwd_f3(g, info, P, locs, grid, out, s);
   return launch_fwd_t2<N, NDIM, NTB, false>(g, cg, info, P, locs, grid, out, s);
 }
 
@@ -1403,7 +1824,7 @@ template <int N, int NDIM, int NTB>
 int launch_adj_t(const Geo& g, int cg, const tlgb_interp_plan_info* info, const char* P, const float* locs,
                  const void* vals, void* grid, void* scratch, cudaStream_t s) {
   if constexpr (N == 4 && NDIM == 3 && NTB == 5)
-    if (fast3(g, cg)) return launch_adj_t2<N, NDIM, NTB, true>(g, cg, info, P, locs, vals, grid, scratch, s);
+    if (fast3(g, cg)) return launch_adj_f3(g, info, P, locs, vals, grid, scratch, s);
   return launch_adj_t2<N, NDIM, NTB, false>(g, cg, info, P, locs, vals, grid, scratch, s);
 }
 
