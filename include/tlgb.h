@@ -44,6 +44,13 @@ enum {
 const char* tlgb_last_error(void);
 int tlgb_version(void);
 
+/* Reads (and, if `clear`, resets) the device status word of the current
+ * device. Kernels whose internal waits are bounded (the TMA-staged gather)
+ * set it to a non-zero code instead of hanging when a wait gives up; their
+ * outputs are then incomplete. Synchronises the device. *status = 0 means no
+ * kernel has reported an error since the last clear. */
+int tlgb_device_status(int32_t* status, int32_t clear);
+
 /* ------------------------------------------------------------------------ */
 /* Interpolation: Kaiser-Bessel / spline ungridding and gridding, 1D-3D.      */
 /* ------------------------------------------------------------------------ */

@@ -38,6 +38,9 @@
 #include <string>
 #include <vector>
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "common.cuh"
 
 namespace tlgb {
@@ -987,21 +990,59 @@ __device__ __forceinline__ float pick4(const float4& v, int i) {
   return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
 }
 
-// Gridding: CTA = 2 warps owning one 8^3 x 8-entry output tile; warp w owns
-// batch entries 4w..4w+3 (two float4 units), so the warps never touch the
-// same shared-memory word and each word is updated in plan order.
-__global__ void __launch_bounds__(64, 5) adj_f3_kernel(Geo g, const int4* __restrict__ items,
-                                                    const int32_t* __restrict__ entries,
-                                                    const float* __restrict__ locs, const float* __restrict__ vals,
-                                                    float* __restrict__ gridv, float* __restrict__ partial) {
-  constexpr int CG = 8, VS = 16, SZ = 16, SY = 8 * 16, SX = 8 * 8 * 16, TFL = 512 * 16, NB = 64;
-  extern __shared__ __align__(16) unsigned char smem[];
-  float* acc = reinterpret_cast<float*>(smem);                       // [8][8][8][16]
-  R3* rec = reinterpret_cast<R3*>(smem + TFL * sizeof(float));      // [64]
-  float* pv = reinterpret_cast<float*>(rec + NB);                   // [64][16]
-  Rec<5>* slow = reinterpret_cast<Rec<5>*>(pv + NB * VS);          // [2] generic records
+// ---- TMA and mbarrier helpers (inline PTX)
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t phase) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(phase)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait: false after `limit` polls (the caller then records an error)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t phase, uint32_t limit) {
+  for (uint32_t i = 0; i < limit; ++i)
+    if (mbar_try_wait(bar, phase)) return true;
+  return false;
+}
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, uint64_t* bar, int x0, int x1, int x2,
+                                            int x3) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+      "[%6];" ::"r"(smem_u32(dst)),
+      "l"(map), "r"(x0), "r"(x1), "r"(x2), "r"(x3), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// device status word: set when a bounded wait gave up (see tlgb_interp_forward)
+__device__ int g_tlgb_status;
+
+// Gridding: one warp per CTA owns one 8^3 x 8-entry output tile
+// ([x][y][z][entry], 16 floats per cell); lanes = (x-tap parity, z-tap,
+// entry pair). Each cell is updated by that warp in plan order.
+__global__ void __launch_bounds__(32, 6) adj_f3_kernel(Geo g, const int4* __restrict__ items,
+                                                       const int32_t* __restrict__ entries,
+                                                       const float* __restrict__ locs, const float* __restrict__ vals,
+                                                       float* __restrict__ gridv, float* __restrict__ partial) {
+  constexpr int CG = 8, VS = 16, SZ = 16, SY = 8 * 16, SX = 8 * 8 * 16, TFL = 512 * 16;
+  extern __shared__ __align__(128) unsigned char smem[];
+  float* acc = reinterpret_cast<float*>(smem);                  // [8][8][8][16]
+  R3* rec = reinterpret_cast<R3*>(smem + TFL * sizeof(float)); // [32]
+  float* pv = reinterpret_cast<float*>(rec + 32);              // [32][16]
+  Rec<5>* slow = reinterpret_cast<Rec<5>*>(pv + 32 * VS);     // [1]
   const int4 it = items[blockIdx.x];
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int lane = threadIdx.x;
   const int cg = blockIdx.y;
   const int c0 = cg * CG;
   const int ncoil = (int)min((long long)CG, g.nbatch - c0);
@@ -1013,86 +1054,91 @@ __global__ void __launch_bounds__(64, 5) adj_f3_kernel(Geo g, const int4* __rest
     o[1] = (t % g.nt[1]) * 8;
     o[0] = (t / g.nt[1]) * 8;
   }
-  for (int i = tid * 4; i < TFL; i += 256) *reinterpret_cast<float4*>(acc + i) = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int i = lane * 4; i < TFL; i += 128) *reinterpret_cast<float4*>(acc + i) = make_float4(0.f, 0.f, 0.f, 0.f);
+  const int cu = lane & 3, uz = (lane >> 2) & 3, kxp = lane >> 4;
+  const int lofs = kxp * SX + uz * SZ + cu * 4;
 
-  // lane roles in a warp: cu (2 units of this warp), uz = z tap, ux = x tap
-  const int cu = lane & 1, uz = (lane >> 1) & 3, ux = lane >> 3;
-  const int unit = warp * 2 + cu;  // float4 unit = batch entries 2*unit, 2*unit+1
-  const int lofs = ux * SX + uz * SZ + unit * 4;
-
-  for (int b = it.y; b < it.z; b += NB) {
-    const int nb = min(NB, it.z - b);
-    __syncthreads();
-    if (tid < nb) {
-      const long long p = entries[b + tid];
-      float x3[3];
-      for (int e = 0; e < 3; ++e) x3[e] = load_coord(g, locs, p, e);
-      lane_rec3<false>(g, x3, o, p, rec[tid]);
-      float* d = pv + tid * VS;
+  // prefetched coordinates / values of the next batch of 32 entries
+  long long np_ = -1;
+  float nx3[3] = {0.f, 0.f, 0.f};
+  float2 nv[CG];
+  auto prefetch = [&](int b) {
+    np_ = -1;
+    if (b + lane < it.z) {
+      np_ = entries[b + lane];
+      for (int e = 0; e < 3; ++e) nx3[e] = load_coord(g, locs, np_, e);
 #pragma unroll
-      for (int c = 0; c < CG; ++c) {
-        float2 v = make_float2(0.f, 0.f);
-        if (c < ncoil) v = __ldg(reinterpret_cast<const float2*>(vals) + (long long)(c0 + c) * g.npts + p);
-        *reinterpret_cast<float2*>(d + 2 * c) = v;
-      }
+      for (int c = 0; c < CG; ++c)
+        nv[c] = c < ncoil ? __ldg(reinterpret_cast<const float2*>(vals) + (long long)(c0 + c) * g.npts + np_)
+                          : make_float2(0.f, 0.f);
     }
-    __syncthreads();
+  };
+  if (it.y < it.z) prefetch(it.y);
+  for (int b = it.y; b < it.z; b += 32) {
+    const int nb = min(32, it.z - b);
+    __syncwarp();
+    if (np_ >= 0) {
+      lane_rec3<false>(g, nx3, o, np_, rec[lane]);
+      float4* d = reinterpret_cast<float4*>(pv + lane * VS);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) d[q] = make_float4(nv[2 * q].x, nv[2 * q].y, nv[2 * q + 1].x, nv[2 * q + 1].y);
+    }
+    __syncwarp();
+    if (b + 32 < it.z) prefetch(b + 32);
     for (int j = 0; j < nb; ++j) {
+      __syncwarp();  // lanes update cells of consecutive points: order them
       const R3& R = rec[j];
-      __syncwarp();
       const int m = R.m;
       if (m == 0) continue;
-      const float4 v = *reinterpret_cast<const float4*>(pv + j * VS + unit * 4);
       if ((m >> 24) && g.wrap_safe) {
         const int mx = m & 255, my = (m >> 8) & 255, mz = (m >> 16) & 255;
-        if (ux < mx && uz < mz) {
-          const float wxz = pick4(R.wx, ux) * pick4(R.wz, uz);
+        if (uz < mz) {
+          const float4 v = *reinterpret_cast<const float4*>(pv + j * VS + cu * 4);
+          const float wz = pick4(R.wz, uz);
           const float4 wy = R.wy;
-          float* a = acc + R.base * VS + lofs;
-          float4 r0 = *reinterpret_cast<float4*>(a);
-          float4 r1, r2, r3;
-          if (my > 1) r1 = *reinterpret_cast<float4*>(a + SY);
-          if (my > 2) r2 = *reinterpret_cast<float4*>(a + 2 * SY);
-          if (my > 3) r3 = *reinterpret_cast<float4*>(a + 3 * SY);
-          float w = wxz * wy.x;
-          r0.x = fmaf(w, v.x, r0.x); r0.y = fmaf(w, v.y, r0.y); r0.z = fmaf(w, v.z, r0.z); r0.w = fmaf(w, v.w, r0.w);
-          *reinterpret_cast<float4*>(a) = r0;
-          if (my > 1) {
-            w = wxz * wy.y;
-            r1.x = fmaf(w, v.x, r1.x); r1.y = fmaf(w, v.y, r1.y); r1.z = fmaf(w, v.z, r1.z); r1.w = fmaf(w, v.w, r1.w);
-            *reinterpret_cast<float4*>(a + SY) = r1;
-          }
-          if (my > 2) {
-            w = wxz * wy.z;
-            r2.x = fmaf(w, v.x, r2.x); r2.y = fmaf(w, v.y, r2.y); r2.z = fmaf(w, v.z, r2.z); r2.w = fmaf(w, v.w, r2.w);
-            *reinterpret_cast<float4*>(a + 2 * SY) = r2;
-          }
-          if (my > 3) {
-            w = wxz * wy.w;
-            r3.x = fmaf(w, v.x, r3.x); r3.y = fmaf(w, v.y, r3.y); r3.z = fmaf(w, v.z, r3.z); r3.w = fmaf(w, v.w, r3.w);
-            *reinterpret_cast<float4*>(a + 3 * SY) = r3;
+          float* a0 = acc + R.base * VS + lofs;
+#pragma unroll
+          for (int i = 0; i < 2; ++i) {
+            const int kx = kxp + 2 * i;
+            if (kx < mx) {
+              const float wxz = pick4(R.wx, kx) * wz;
+              float* a = a0 + 2 * i * SX;
+              float4 r[4];
+#pragma unroll
+              for (int ky = 0; ky < 4; ++ky)
+                if (ky < my) r[ky] = *reinterpret_cast<const float4*>(a + ky * SY);
+#pragma unroll
+              for (int ky = 0; ky < 4; ++ky)
+                if (ky < my) {
+                  const float w = wxz * pick4(wy, ky);
+                  r[ky].x = fmaf(w, v.x, r[ky].x);
+                  r[ky].y = fmaf(w, v.y, r[ky].y);
+                  r[ky].z = fmaf(w, v.z, r[ky].z);
+                  r[ky].w = fmaf(w, v.w, r[ky].w);
+                  *reinterpret_cast<float4*>(a + ky * SY) = r[ky];
+                }
+            }
           }
         }
         continue;
       }
       // exact-integer coordinates (5 taps) or a window wrapping inside the
-      // tile: the generic record, taps in order
+      // tile: generic record, taps in order by the lanes of each entry pair
       if (lane == 0) {
         float x3[3];
         for (int e = 0; e < 3; ++e) x3[e] = load_coord(g, locs, R.p, e);
-        lane_rec<5>(g, x3, o, false, slow[warp]);
+        lane_rec<5>(g, x3, o, false, slow[0]);
       }
       __syncwarp();
-      const Rec<5>& S = slow[warp];
-      if (S.m[0] > 0 && lane < 2) {
-        float* base = acc + (warp * 2 + lane) * 4;
+      const Rec<5>& S = slow[0];
+      if (S.m[0] > 0 && lane < 4) {
+        const float4 vv = *reinterpret_cast<const float4*>(pv + j * VS + lane * 4);
         for (int kx = 0; kx < S.m[0]; ++kx)
           for (int ky = 0; ky < S.m[1]; ++ky)
             for (int kz = 0; kz < S.m[2]; ++kz) {
               const float w = g.norm == 1 ? S.wv[0][kx] * S.wv[1][ky] * S.wv[2][kz]
                                           : radial_w(g, S.wv[0][kx], S.wv[1][ky], S.wv[2][kz]);
-              float* a = base + ((S.lc[0][kx] * 8 + S.lc[1][ky]) * 8 + S.lc[2][kz]) * VS;
-              const float4 vv = *reinterpret_cast<const float4*>(pv + j * VS + (warp * 2 + lane) * 4);
+              float* a = acc + ((S.lc[0][kx] * 8 + S.lc[1][ky]) * 8 + S.lc[2][kz]) * VS + lane * 4;
               float4 r = *reinterpret_cast<float4*>(a);
               r.x = fmaf(w, vv.x, r.x); r.y = fmaf(w, vv.y, r.y); r.z = fmaf(w, vv.z, r.z); r.w = fmaf(w, vv.w, r.w);
               *reinterpret_cast<float4*>(a) = r;
@@ -1100,16 +1146,16 @@ __global__ void __launch_bounds__(64, 5) adj_f3_kernel(Geo g, const int4* __rest
       }
     }
   }
-  __syncthreads();
+  __syncwarp();
   if (it.w >= 0) {
     float* dst = partial + ((long long)it.w * gridDim.y + cg) * TFL;
-    for (int i = tid * 4; i < TFL; i += 256)
+    for (int i = lane * 4; i < TFL; i += 128)
       *reinterpret_cast<float4*>(dst + i) = *reinterpret_cast<const float4*>(acc + i);
     return;
   }
   // write-out: per (x, y) row 8 z x 8 entries; lanes (entry fastest, z)
   const long long gvol = (long long)g.N[0] * g.N[1] * g.N[2];
-  for (int row = warp; row < 64; row += 2) {
+  for (int row = 0; row < 64; ++row) {
     const int x = row >> 3, y = row & 7;
     const int gx = o[0] + x, gy = o[1] + y;
     if (gx >= g.N[0] || gy >= g.N[1]) continue;
@@ -1126,18 +1172,22 @@ __global__ void __launch_bounds__(64, 5) adj_f3_kernel(Geo g, const int4* __rest
   }
 }
 
-// Gather: CTA = 16 warps sharing the staged 12^3 x 8-entry region
-// ([x][y][z][entry], entry fastest); warp = 32 points per batch, one at a
-// time, lanes (x-tap parity, z-tap, entry pair).
-__global__ void __launch_bounds__(512, 1) fwd_f3_kernel(Geo g, const int4* __restrict__ items,
+// Gather: CTA = 16 warps sharing one 12^3 x 8-entry region ([entry][x][y][z],
+// loaded by one TMA bulk tensor copy when the region needs no wrap); lanes =
+// (x-tap parity, y-tap, z-tap), entries looped, reduced by shuffles.
+__global__ void __launch_bounds__(512, 1) fwd_f3_kernel(const __grid_constant__ CUtensorMap tmap, int use_tma, Geo g,
+                                                        const int4* __restrict__ items,
                                                         const int32_t* __restrict__ entries,
                                                         const float* __restrict__ locs,
                                                         const float* __restrict__ gridv, float* __restrict__ out) {
-  constexpr int CG = 8, VS = 16, S = 12, SZ = 16, SY = 12 * 16, SX = 12 * 12 * 16, RFL = S * S * S * VS, NW = 16;
-  extern __shared__ __align__(16) unsigned char smem[];
-  float* reg = reinterpret_cast<float*>(smem);                          // [12][12][12][16]
-  R3* recs = reinterpret_cast<R3*>(smem + RFL * sizeof(float));        // [16][32]
-  Rec<5>* slow = reinterpret_cast<Rec<5>*>(recs + NW * 32);            // [16]
+  constexpr int CG = 8, S = 12, PLANE = S * S, VOL = S * S * S, NW = 16;
+  constexpr uint32_t RBYTES = VOL * CG * 8;
+  extern __shared__ __align__(1024) unsigned char smem[];
+  float2* reg = reinterpret_cast<float2*>(smem);                     // [8][12][12][12]
+  R3* recs = reinterpret_cast<R3*>(smem + RBYTES);                   // [16][32]
+  Rec<5>* slow = reinterpret_cast<Rec<5>*>(recs + NW * 32);          // [16]
+  static_assert((NW * 32 * sizeof(R3) + NW * sizeof(Rec<5>)) % 8 == 0, "mbarrier alignment");
+  uint64_t* bar = reinterpret_cast<uint64_t*>(slow + NW);
   const int4 it = items[blockIdx.x];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int c0 = blockIdx.y * CG;
@@ -1150,46 +1200,63 @@ __global__ void __launch_bounds__(512, 1) fwd_f3_kernel(Geo g, const int4* __res
     o[1] = (t % g.nt[1]) * 8;
     o[0] = (t / g.nt[1]) * 8;
   }
-  // stage: 144 (x, y) rows of 12 z x 8 entries = 96 float2; 3 loads per lane
-  const long long gvol = (long long)g.N[0] * g.N[1] * g.N[2];
-  for (int row = warp; row < S * S; row += NW) {
-    const int x = row / S, y = row - (row / S) * S;
-    int gx = o[0] + x, gy = o[1] + y;
-    bool rin = true;
-    if (g.pad == TLGB_PAD_CIRCULAR) {
-      gx = wrapi(gx, g.N[0]);
-      gy = wrapi(gy, g.N[1]);
-    } else {
-      rin = gx < g.N[0] && gy < g.N[1];
+  // the region needs wrap in circular mode when it crosses the upper edge
+  const bool wraps = g.pad == TLGB_PAD_CIRCULAR && (o[0] + S > g.N[0] || o[1] + S > g.N[1] || o[2] + S > g.N[2]);
+  const bool tma = use_tma && !wraps;
+  if (tma) {
+    if (threadIdx.x == 0) {
+      mbar_init(bar, 1);
+      fence_mbar_init();
     }
-    const long long rbase = ((long long)gx * g.N[1] + gy) * g.N[2];
-    float2 vv[3];
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-      const int idx = lane + 32 * i;
-      const int c = idx & 7, z = idx >> 3;
-      int gz = o[2] + z;
-      bool in = rin && c < ncoil;
-      if (g.pad == TLGB_PAD_CIRCULAR) gz = wrapi(gz, g.N[2]);
-      else in = in && gz < g.N[2];
-      vv[i] = in ? __ldg(reinterpret_cast<const float2*>(gridv) + (long long)(c0 + c) * gvol + rbase + gz)
-                 : make_float2(0.f, 0.f);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      mbar_arrive_expect_tx(bar, RBYTES);
+      tma_load_4d(reg, &tmap, bar, o[2], o[1], o[0], c0);
     }
-    float* rdst = reg + row * S * VS;
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-      const int idx = lane + 32 * i;
-      *reinterpret_cast<float2*>(rdst + (idx >> 3) * VS + (idx & 7) * 2) = vv[i];
+  } else {
+    // manual staging with wrap / zero fill: rows (entry, x, y) of 12 z
+    const long long gvol = (long long)g.N[0] * g.N[1] * g.N[2];
+    for (int idx = threadIdx.x; idx < CG * VOL; idx += NW * 32) {
+      const int z = idx % S;
+      const int r = idx / S;
+      const int y = r % S, x = (r / S) % S, c = r / PLANE;
+      int gx = o[0] + x, gy = o[1] + y, gz = o[2] + z;
+      bool in = c < ncoil;
+      if (g.pad == TLGB_PAD_CIRCULAR) {
+        gx = wrapi(gx, g.N[0]);
+        gy = wrapi(gy, g.N[1]);
+        gz = wrapi(gz, g.N[2]);
+      } else {
+        in = in && gx < g.N[0] && gy < g.N[1] && gz < g.N[2];
+      }
+      reg[idx] = in ? __ldg(reinterpret_cast<const float2*>(gridv) + (long long)(c0 + c) * gvol +
+                           ((long long)gx * g.N[1] + gy) * g.N[2] + gz)
+                    : make_float2(0.f, 0.f);
     }
   }
-  __syncthreads();
-
-  const int cu = lane & 3, uz = (lane >> 2) & 3, ux = lane >> 4;  // ux in {0, 1}: x taps ux, ux + 2
-  const int lofs = ux * SX + uz * SZ + cu * 4;
+  // tap records of this warp's first batch while the copy is in flight
   R3* rbuf = recs + warp * 32;
-  for (int b = it.y + warp * 32; b < it.z; b += NW * 32) {
+  int b = it.y + warp * 32;
+  if (b + lane < it.z) {
+    const long long p = entries[b + lane];
+    float x3[3];
+    for (int e = 0; e < 3; ++e) x3[e] = load_coord(g, locs, p, e);
+    lane_rec3<true>(g, x3, o, p, rbuf[lane]);
+  }
+  if (tma) {
+    if (!mbar_wait_bounded(bar, 0, 1u << 24)) {
+      if (lane == 0) atomicExch(&g_tlgb_status, 1);
+      // the copy never completed: give up on this item without reading it
+      return;
+    }
+  } else {
+    __syncthreads();
+  }
+
+  const int kz = lane & 3, ky = (lane >> 2) & 3, kxp = lane >> 4;
+  for (; b < it.z; b += NW * 32) {
     const int nb = min(32, it.z - b);
-    if (lane < nb) {
+    if (b != it.y + warp * 32 && b + lane < it.z) {
       const long long p = entries[b + lane];
       float x3[3];
       for (int e = 0; e < 3; ++e) x3[e] = load_coord(g, locs, p, e);
@@ -1200,34 +1267,24 @@ __global__ void __launch_bounds__(512, 1) fwd_f3_kernel(Geo g, const int4* __res
       const R3& R = rbuf[j];
       const int m = R.m;
       if (m == 0) continue;  // warp-uniform
-      float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+      float acc[2 * CG];
+#pragma unroll
+      for (int i = 0; i < 2 * CG; ++i) acc[i] = 0.f;
       if (m >> 24) {
         const int mx = m & 255, my = (m >> 8) & 255, mz = (m >> 16) & 255;
-        if (uz < mz) {
-          const float wz = pick4(R.wz, uz);
-          const float4 wy = R.wy;
-          const float* a = reg + R.base * VS + lofs;
+        const float wyz = (ky < my && kz < mz) ? pick4(R.wy, ky) * pick4(R.wz, kz) : 0.f;
+        const float w0 = kxp < mx ? pick4(R.wx, kxp) * wyz : 0.f;
+        const float w1 = kxp + 2 < mx ? pick4(R.wx, kxp + 2) * wyz : 0.f;
+        const float2* a = reg + R.base + kxp * PLANE + ky * S + kz;
 #pragma unroll
-          for (int i = 0; i < 2; ++i) {
-            if (ux + 2 * i < mx) {
-              const float wxz = pick4(R.wx, ux + 2 * i) * wz;
-              const float* ax = a + 2 * i * SX;
-#pragma unroll
-              for (int ky = 0; ky < 4; ++ky) {
-                if (ky < my) {
-                  const float w = wxz * pick4(wy, ky);
-                  const float4 v = *reinterpret_cast<const float4*>(ax + ky * SY);
-                  acc.x = fmaf(w, v.x, acc.x);
-                  acc.y = fmaf(w, v.y, acc.y);
-                  acc.z = fmaf(w, v.z, acc.z);
-                  acc.w = fmaf(w, v.w, acc.w);
-                }
-              }
-            }
-          }
+        for (int c = 0; c < CG; ++c) {
+          const float2 v0 = a[c * VOL];
+          const float2 v1 = a[c * VOL + 2 * PLANE];
+          acc[2 * c] = fmaf(w0, v0.x, fmaf(w1, v1.x, acc[2 * c]));
+          acc[2 * c + 1] = fmaf(w0, v0.y, fmaf(w1, v1.y, acc[2 * c + 1]));
         }
       } else {
-        // exact-integer coordinates: generic record, lanes = (x, z taps, unit)
+        // exact-integer coordinates: generic record
         if (lane == 0) {
           float x3[3];
           for (int e = 0; e < 3; ++e) x3[e] = load_coord(g, locs, R.p, e);
@@ -1235,34 +1292,51 @@ __global__ void __launch_bounds__(512, 1) fwd_f3_kernel(Geo g, const int4* __res
         }
         __syncwarp();
         const Rec<5>& Sr = slow[warp];
-        for (int kz = uz; kz < Sr.m[2]; kz += 4)
-          for (int kx = ux; kx < Sr.m[0]; kx += 2)
-            for (int ky = 0; ky < Sr.m[1]; ++ky) {
-              const float w = g.norm == 1 ? Sr.wv[0][kx] * Sr.wv[1][ky] * Sr.wv[2][kz]
-                                          : radial_w(g, Sr.wv[0][kx], Sr.wv[1][ky], Sr.wv[2][kz]);
-              const float4 v = *reinterpret_cast<const float4*>(
-                  reg + ((Sr.lc[0][kx] * S + Sr.lc[1][ky]) * S + Sr.lc[2][kz]) * VS + cu * 4);
-              acc.x = fmaf(w, v.x, acc.x);
-              acc.y = fmaf(w, v.y, acc.y);
-              acc.z = fmaf(w, v.z, acc.z);
-              acc.w = fmaf(w, v.w, acc.w);
+        for (int kzz = kz; kzz < Sr.m[2]; kzz += 4)
+          for (int kyy = ky; kyy < Sr.m[1]; kyy += 4)
+            for (int kx = kxp; kx < Sr.m[0]; kx += 2) {
+              const float w = g.norm == 1 ? Sr.wv[0][kx] * Sr.wv[1][kyy] * Sr.wv[2][kzz]
+                                          : radial_w(g, Sr.wv[0][kx], Sr.wv[1][kyy], Sr.wv[2][kzz]);
+              const float2* a = reg + (Sr.lc[0][kx] * S + Sr.lc[1][kyy]) * S + Sr.lc[2][kzz];
+#pragma unroll
+              for (int c = 0; c < CG; ++c) {
+                const float2 v = a[c * VOL];
+                acc[2 * c] = fmaf(w, v.x, acc[2 * c]);
+                acc[2 * c + 1] = fmaf(w, v.y, acc[2 * c + 1]);
+              }
             }
         __syncwarp();
       }
+      // reduce-scatter the 16 partial sums over the 32 lanes: lane L ends
+      // with the sum of value L >> 1 (entry (L >> 2), re if L & 2 == 0)
+      float s8[8], s4[4], s2[2];
+      const bool b4 = lane & 16, b3 = lane & 8, b2 = lane & 4, b1 = lane & 2;
 #pragma unroll
-      for (int mm = 4; mm < 32; mm <<= 1) {
-        acc.x += __shfl_xor_sync(0xffffffffu, acc.x, mm);
-        acc.y += __shfl_xor_sync(0xffffffffu, acc.y, mm);
-        acc.z += __shfl_xor_sync(0xffffffffu, acc.z, mm);
-        acc.w += __shfl_xor_sync(0xffffffffu, acc.w, mm);
+      for (int i = 0; i < 8; ++i) {
+        const float send = b4 ? acc[i] : acc[i + 8];
+        s8[i] = (b4 ? acc[i + 8] : acc[i]) + __shfl_xor_sync(0xffffffffu, send, 16);
       }
-      if (lane < 4) {
-        const long long pj = R.p;
-        const int c = 2 * cu;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const float send = b3 ? s8[i] : s8[i + 4];
+        s4[i] = (b3 ? s8[i + 4] : s8[i]) + __shfl_xor_sync(0xffffffffu, send, 8);
+      }
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        const float send = b2 ? s4[i] : s4[i + 2];
+        s2[i] = (b2 ? s4[i + 2] : s4[i]) + __shfl_xor_sync(0xffffffffu, send, 4);
+      }
+      float s1;
+      {
+        const float send = b1 ? s2[0] : s2[1];
+        s1 = (b1 ? s2[1] : s2[0]) + __shfl_xor_sync(0xffffffffu, send, 2);
+      }
+      s1 += __shfl_xor_sync(0xffffffffu, s1, 1);
+      const float im = __shfl_down_sync(0xffffffffu, s1, 2);
+      if ((lane & 3) == 0) {
+        const int c = lane >> 2;
         if (c < ncoil)
-          *reinterpret_cast<float2*>(out + ((long long)(c0 + c) * g.npts + pj) * 2) = make_float2(acc.x, acc.y);
-        if (c + 1 < ncoil)
-          *reinterpret_cast<float2*>(out + ((long long)(c0 + c + 1) * g.npts + pj) * 2) = make_float2(acc.z, acc.w);
+          *reinterpret_cast<float2*>(out + ((long long)(c0 + c) * g.npts + R.p) * 2) = make_float2(s1, im);
       }
     }
     __syncwarp();
@@ -1442,7 +1516,7 @@ struct PlanLayout {
 };
 
 constexpr int64_t kFwdChunk = 512;
-constexpr int64_t kAdjChunk = 512;
+constexpr int64_t kAdjChunk = 1024;
 
 int make_geo(const tlgb_interp_desc* d, Geo& g) {
   if (!d) TLGB_FAIL(TLGB_ERR_INVALID, "null interp descriptor");
@@ -1782,14 +1856,44 @@ int launch_adj_t2(const Geo& g, int cg, const tlgb_interp_plan_info* info, const
   return TLGB_OK;
 }
 
+// cuTensorMapEncodeTiled from the driver, looked up once (no -lcuda)
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
 int launch_fwd_f3(const Geo& g, const tlgb_interp_plan_info* info, const char* P, const float* locs,
                   const void* grid, void* out, cudaStream_t s) {
   const int64_t ncg = cdiv(g.nbatch, 8);
-  const size_t sm = 12 * 12 * 12 * 16 * sizeof(float) + 16 * 32 * sizeof(R3) + 16 * sizeof(Rec<5>);
+  const size_t sm = 12 * 12 * 12 * 8 * 8 + 16 * 32 * sizeof(R3) + 16 * sizeof(Rec<5>) + 16;
+  // 4D tensor map over [batch][X][Y][Z] complex64 (8-byte elements), box 12^3 x 8
+  CUtensorMap tmap;
+  memset(&tmap, 0, sizeof(tmap));
+  int use_tma = 0;
+  auto enc = tensor_map_encoder();
+  const uint64_t zb = (uint64_t)g.N[2] * 8;
+  if (enc && (zb % 16) == 0 && ((uintptr_t)grid % 16) == 0) {
+    const cuuint64_t dims[4] = {(cuuint64_t)g.N[2], (cuuint64_t)g.N[1], (cuuint64_t)g.N[0], (cuuint64_t)g.nbatch};
+    const cuuint64_t strides[3] = {zb, zb * g.N[1], zb * g.N[1] * g.N[0]};
+    const cuuint32_t box[4] = {12, 12, 12, 8};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    const CUresult r = enc(&tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4, const_cast<void*>(grid), dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    use_tma = (r == CUDA_SUCCESS) ? 1 : 0;
+  }
   TLGB_TRY(set_smem(fwd_f3_kernel, sm));
   dim3 grd((unsigned)info->n_fwd_items, (unsigned)ncg);
-  fwd_f3_kernel<<<grd, 512, sm, s>>>(g, (const int4*)(P + info->off_fwd_items), (const int32_t*)(P + info->off_entries),
-                                     locs, (const float*)grid, (float*)out);
+  fwd_f3_kernel<<<grd, 512, sm, s>>>(tmap, use_tma, g, (const int4*)(P + info->off_fwd_items),
+                                     (const int32_t*)(P + info->off_entries), locs, (const float*)grid, (float*)out);
   TLGB_CHECK_LAUNCH();
   return TLGB_OK;
 }
@@ -1797,10 +1901,10 @@ int launch_fwd_f3(const Geo& g, const tlgb_interp_plan_info* info, const char* P
 int launch_adj_f3(const Geo& g, const tlgb_interp_plan_info* info, const char* P, const float* locs,
                   const void* vals, void* grid, void* scratch, cudaStream_t s) {
   const int64_t ncg = cdiv(g.nbatch, 8);
-  const size_t sm = 512 * 16 * sizeof(float) + 64 * sizeof(R3) + 64 * 16 * sizeof(float) + 2 * sizeof(Rec<5>);
+  const size_t sm = 512 * 16 * sizeof(float) + 32 * sizeof(R3) + 32 * 16 * sizeof(float) + sizeof(Rec<5>);
   TLGB_TRY(set_smem(adj_f3_kernel, sm));
   dim3 grd((unsigned)info->n_adj_items, (unsigned)ncg);
-  adj_f3_kernel<<<grd, 64, sm, s>>>(g, (const int4*)(P + info->off_adj_items), (const int32_t*)(P + info->off_entries),
+  adj_f3_kernel<<<grd, 32, sm, s>>>(g, (const int4*)(P + info->off_adj_items), (const int32_t*)(P + info->off_entries),
                                     locs, (const float*)vals, (float*)grid, (float*)scratch);
   TLGB_CHECK_LAUNCH();
   if (info->n_split_tiles > 0) {
@@ -2002,4 +2106,17 @@ extern "C" int tlgb_interp_adjoint_fixed(const tlgb_interp_desc* d, const tlgb_i
   void* scratch = nullptr;
   if (need > 0) TLGB_TRY(fixed_scratch_address(&scratch));
   return launch_adj(g, info, (const char*)plan, locs, vals, grid, scratch, (cudaStream_t)stream);
+}
+
+extern "C" int tlgb_device_status(int32_t* status, int32_t clear) {
+  if (status == nullptr) TLGB_FAIL(TLGB_ERR_INVALID, "status is NULL");
+  int v = 0;
+  TLGB_CUDA(cudaDeviceSynchronize());
+  TLGB_CUDA(cudaMemcpyFromSymbol(&v, tlgb::g_tlgb_status, sizeof(int)));
+  if (clear) {
+    const int z = 0;
+    TLGB_CUDA(cudaMemcpyToSymbol(tlgb::g_tlgb_status, &z, sizeof(int)));
+  }
+  *status = v;
+  return TLGB_OK;
 }

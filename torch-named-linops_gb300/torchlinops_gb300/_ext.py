@@ -82,6 +82,7 @@ _P = ctypes.c_void_p
 _SIGNATURES = {
     "tlgb_last_error": ([], ctypes.c_char_p),
     "tlgb_version": ([], ctypes.c_int),
+    "tlgb_device_status": ([ctypes.POINTER(ctypes.c_int32), ctypes.c_int32], ctypes.c_int),
     "tlgb_interp_plan_size": ([_P, _P, _P], ctypes.c_int),
     "tlgb_interp_plan_build": ([_P, _P, _P, ctypes.c_size_t, _P, ctypes.c_size_t, _P, _P], ctypes.c_int),
     "tlgb_interp_adjoint_scratch_size": ([_P, _P, _P], ctypes.c_int),
@@ -141,6 +142,13 @@ def check(status: int, what: str) -> None:
     if status in (TLGB_ERR_INVALID, TLGB_ERR_UNSUPPORTED):
         raise ValueError(text)
     raise RuntimeError(text)
+
+
+def device_status(clear: bool = False) -> int:
+    """The device status word (0 = no kernel gave up a bounded wait); synchronises."""
+    v = ctypes.c_int32(0)
+    check(lib().tlgb_device_status(ctypes.byref(v), 1 if clear else 0), "tlgb_device_status")
+    return int(v.value)
 
 
 def check_cuda(*tensors: torch.Tensor) -> torch.device:
