@@ -911,79 +911,135 @@ __device__ __forceinline__ float kb_approx(float ax, float beta) {
   return __expf(z) * rsqrtf(z) * q;
 }
 
+// Packed tap record of one (point, tile) entry for the 3D 8-entry kernels,
+// built one dimension per thread. Per dimension: the weights of the kept taps
+// (zero beyond the count) and an info word first | count << 4 | ok << 8 |
+// fast << 9, with first the local position of the first kept tap (in the
+// 12^3 gather region, or in the 8^3 tile for gridding), ok = a finite
+// coordinate with at least one kept tap, fast = at most 4 kept taps at
+// consecutive local positions.
 struct __align__(16) R3 {
-  float4 wx, wy, wz;  // weights of the kept taps, zero beyond the count
-  int base;           // local linear voxel offset of the first kept tap
-  int m;              // mx | my << 8 | mz << 16 | fast << 24
-  int p;              // point index
-  int pad;
+  float4 w[3];
+  int info[3];
+  int p;  // point index
 };
 
-// One lane packs the record of point p. region: gather mode (8^3 tile +
-// halo, 12^3 staged region, contiguous taps from the wrapped start); else
-// the 8^3 output tile, taps outside it dropped. fast = every dim keeps <= 4
-// taps at consecutive local coordinates.
+// The constants of one dimension, selected by a runtime index (keeps a
+// per-thread dimension out of local memory).
+struct Axis {
+  int N;
+  float r, rinv;
+  int rpow2;
+};
+
+__device__ __forceinline__ Axis axis_of(const Geo& g, int e) {
+  Axis a;
+  a.N = e == 0 ? g.N[0] : (e == 1 ? g.N[1] : g.N[2]);
+  a.r = e == 0 ? g.r[0] : (e == 1 ? g.r[1] : g.r[2]);
+  a.rinv = e == 0 ? g.rinv[0] : (e == 1 ? g.rinv[1] : g.rinv[2]);
+  a.rpow2 = e == 0 ? g.rpow2[0] : (e == 1 ? g.rpow2[1] : g.rpow2[2]);
+  return a;
+}
+
+// tap_eval for one dimension given by its constants (same operations)
+__device__ __forceinline__ Tap tap_eval_ax(const Geo& g, const Axis& a, float x, int lower, int k) {
+  Tap t;
+  const float gk = (float)(lower + k);
+  const float diff = __fsub_rn(x, gk);
+  t.d = a.rpow2 ? __fmul_rn(diff, a.rinv) : __fdiv_rn(diff, a.r);
+  const float ad = fabsf(t.d);
+  bool v = ad <= a.r;
+  if (g.kernel == TLGB_KERNEL_KAISER_BESSEL) v = v && (ad <= 1.0f);
+  if (g.pad == TLGB_PAD_ZERO) v = v && (lower + k >= 0) && (lower + k < a.N);
+  t.valid = v;
+  return t;
+}
+
+// One dimension of a record (5 candidate taps). REGION: gather mode, the
+// window is contiguous from its first valid tap (the region is staged with
+// wrap); otherwise gridding mode, only the taps inside the tile are kept.
 template <bool REGION>
-__device__ __forceinline__ void lane_rec3(const Geo& g, const float (&x3)[3], const int (&o)[3], long long p,
-                                          R3& R) {
+__device__ __forceinline__ int rec3_dim(const Geo& g, const Axis& a, float x, int oe, float4& w4) {
   constexpr int SD = REGION ? 12 : 8;
-  float4 w4[3];
-  int first[3], cnt[3];
-  bool ok = true, fast = true;
+  float w0 = 0.f, w1 = 0.f, w2 = 0.f, w3 = 0.f;
+  int first = 0, c = 0;
+  bool fast = true;
+  if (coord_ok(x)) {
+    const int lower = (int)ceilf(__fsub_rn(x, a.r));
+    int s = -1, last = -100;
 #pragma unroll
-  for (int e = 0; e < 3; ++e) {
-    float w0 = 0.f, w1 = 0.f, w2 = 0.f, w3 = 0.f;  // kept-tap weights, in registers
-    first[e] = 0;
-    cnt[e] = 0;
-    const float x = x3[e];
-    if (ok && coord_ok(x)) {
-      const int lower = lower_of(g, e, x);
-      int s = -1, last = -100, c = 0;
-#pragma unroll
-      for (int k = 0; k < 5; ++k) {
-        const Tap t = tap_eval(g, e, x, lower, k);
-        if (t.valid) {
-          if (s < 0) s = k;
-          int l;
-          bool keep = true;
-          if (REGION) {
-            int st = lower + s;
-            if (g.pad == TLGB_PAD_CIRCULAR) st = wrapi(st, g.N[e]);
-            l = st - o[e] + (k - s);
-          } else {
-            int gg = lower + k;
-            if (g.pad == TLGB_PAD_CIRCULAR) gg = wrapi(gg, g.N[e]);
-            l = gg - o[e];
-            keep = l >= 0 && l < SD;
-          }
-          if (keep) {
-            if (c == 0) first[e] = l;
-            else if (l != last + 1) fast = false;
-            last = l;
-            const float v = kern_value_approx(g.kernel, fabsf(t.d), g.beta);
-            w0 = c == 0 ? v : w0;
-            w1 = c == 1 ? v : w1;
-            w2 = c == 2 ? v : w2;
-            w3 = c == 3 ? v : w3;
-            if (c >= 4) fast = false;
-            ++c;
-          }
+    for (int k = 0; k < 5; ++k) {
+      const Tap t = tap_eval_ax(g, a, x, lower, k);
+      if (t.valid) {
+        if (s < 0) s = k;
+        int l;
+        bool keep = true;
+        if (REGION) {
+          int st = lower + s;
+          if (g.pad == TLGB_PAD_CIRCULAR) st = wrapi(st, a.N);
+          l = st - oe + (k - s);
+        } else {
+          int gg = lower + k;
+          if (g.pad == TLGB_PAD_CIRCULAR) gg = wrapi(gg, a.N);
+          l = gg - oe;
+          keep = l >= 0 && l < SD;
+        }
+        if (keep) {
+          if (c == 0) first = l;
+          else if (l != last + 1) fast = false;
+          last = l;
+          const float v = kern_value_approx(g.kernel, fabsf(t.d), g.beta);
+          w0 = c == 0 ? v : w0;
+          w1 = c == 1 ? v : w1;
+          w2 = c == 2 ? v : w2;
+          w3 = c == 3 ? v : w3;
+          if (c >= 4) fast = false;
+          ++c;
         }
       }
-      cnt[e] = c;
-      if (c == 0) ok = false;
-    } else {
-      ok = false;
     }
-    w4[e] = make_float4(w0, w1, w2, w3);
   }
-  R.wx = w4[0];
-  R.wy = w4[1];
-  R.wz = w4[2];
-  R.base = (first[0] * SD + first[1]) * SD + first[2];
-  R.m = ok ? (min(cnt[0], 255) | (min(cnt[1], 255) << 8) | (min(cnt[2], 255) << 16) | ((fast ? 1 : 0) << 24)) : 0;
-  R.p = (int)p;
-  R.pad = 0;
+  w4 = make_float4(w0, w1, w2, w3);
+  if (first < 0 || first >= SD) fast = false;  // never for plan entries; keeps the fast paths in bounds
+  return (first & 15) | (c << 4) | ((c > 0 ? 1 : 0) << 8) | ((fast ? 1 : 0) << 9);
+}
+
+// Thread task (entry j, dimension d) of a record batch: d = task / span.
+template <bool REGION>
+__device__ __forceinline__ void rec3_task(const Geo& g, const float* __restrict__ locs,
+                                          const int32_t* __restrict__ entries, int b, int j, int d,
+                                          const int (&o)[3], R3* rec) {
+  const long long p = entries[b + j];
+  const float x = load_coord(g, locs, p, d);
+  const int oe = d == 0 ? o[0] : (d == 1 ? o[1] : o[2]);
+  float4 w4;
+  const int info = rec3_dim<REGION>(g, axis_of(g, d), x, oe, w4);
+  rec[j].w[d] = w4;
+  rec[j].info[d] = info;
+  if (d == 0) rec[j].p = (int)p;
+}
+
+struct R3v {
+  int base, mx, my, mz, fx, fy, fz, p;
+  bool ok, fast;
+};
+
+template <int SD>
+__device__ __forceinline__ R3v rec3_view(const R3& R) {
+  const int4 q = *reinterpret_cast<const int4*>(R.info);
+  R3v v;
+  const int all = q.x & q.y & q.z;
+  v.ok = (all >> 8) & 1;
+  v.fast = (all >> 9) & 1;
+  v.fx = q.x & 15;
+  v.fy = q.y & 15;
+  v.fz = q.z & 15;
+  v.mx = (q.x >> 4) & 15;
+  v.my = (q.y >> 4) & 15;
+  v.mz = (q.z >> 4) & 15;
+  v.base = (v.fx * SD + v.fy) * SD + v.fz;
+  v.p = q.w;
+  return v;
 }
 
 __device__ __forceinline__ float pick4(const float4& v, int i) {
@@ -1028,21 +1084,28 @@ __device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, u
 // device status word: set when a bounded wait gave up (see tlgb_interp_forward)
 __device__ int g_tlgb_status;
 
-// Gridding: one warp per CTA owns one 8^3 x 8-entry output tile
-// ([x][y][z][entry], 16 floats per cell); lanes = (x-tap parity, z-tap,
-// entry pair). Each cell is updated by that warp in plan order.
-__global__ void __launch_bounds__(32, 6) adj_f3_kernel(Geo g, const int4* __restrict__ items,
-                                                       const int32_t* __restrict__ entries,
-                                                       const float* __restrict__ locs, const float* __restrict__ vals,
-                                                       float* __restrict__ gridv, float* __restrict__ partial) {
-  constexpr int CG = 8, VS = 16, SZ = 16, SY = 8 * 16, SX = 8 * 8 * 16, TFL = 512 * 16;
+// Gridding: CTA = 8 warps owning one 8^3 x 8-entry output tile
+// ([x][y][z][entry], 16 floats per cell); warp w owns the cells of x-plane w,
+// so no two warps write the same cell. Entries are staged in batches of kAB
+// (records built one dimension per thread, point values, and per plane a
+// bitmask of the entries with taps in it); each warp applies its plane's
+// entries in plan order, so every cell is updated in the same order on every
+// run. Lanes = (entry pair, z-tap parity, y-tap).
+constexpr int kAB = 128;
+
+__global__ void __launch_bounds__(256, 4) adj_f3_kernel(Geo g, const int4* __restrict__ items,
+                                                        const int32_t* __restrict__ entries,
+                                                        const float* __restrict__ locs, const float* __restrict__ vals,
+                                                        float* __restrict__ gridv, float* __restrict__ partial) {
+  constexpr int CG = 8, VS = 16, TFL = 512 * 16, NW = 8, MW = kAB / 32;
   extern __shared__ __align__(128) unsigned char smem[];
-  float* acc = reinterpret_cast<float*>(smem);                  // [8][8][8][16]
-  R3* rec = reinterpret_cast<R3*>(smem + TFL * sizeof(float)); // [32]
-  float* pv = reinterpret_cast<float*>(rec + 32);              // [32][16]
-  Rec<5>* slow = reinterpret_cast<Rec<5>*>(pv + 32 * VS);     // [1]
+  float* acc = reinterpret_cast<float*>(smem);                   // [8][8][8][16]
+  R3* rec = reinterpret_cast<R3*>(smem + TFL * sizeof(float));  // [kAB]
+  float* pv = reinterpret_cast<float*>(rec + kAB);              // [kAB][16]
+  Rec<5>* slow = reinterpret_cast<Rec<5>*>(pv + kAB * VS);      // [NW]
+  unsigned* pmask = reinterpret_cast<unsigned*>(slow + NW);     // [NW][MW]
   const int4 it = items[blockIdx.x];
-  const int lane = threadIdx.x;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int cg = blockIdx.y;
   const int c0 = cg * CG;
   const int ncoil = (int)min((long long)CG, g.nbatch - c0);
@@ -1054,112 +1117,124 @@ __global__ void __launch_bounds__(32, 6) adj_f3_kernel(Geo g, const int4* __rest
     o[1] = (t % g.nt[1]) * 8;
     o[0] = (t / g.nt[1]) * 8;
   }
-  for (int i = lane * 4; i < TFL; i += 128) *reinterpret_cast<float4*>(acc + i) = make_float4(0.f, 0.f, 0.f, 0.f);
-  const int cu = lane & 3, uz = (lane >> 2) & 3, kxp = lane >> 4;
-  const int lofs = kxp * SX + uz * SZ + cu * 4;
-
-  // prefetched coordinates / values of the next batch of 32 entries
-  long long np_ = -1;
-  float nx3[3] = {0.f, 0.f, 0.f};
-  float2 nv[CG];
-  auto prefetch = [&](int b) {
-    np_ = -1;
-    if (b + lane < it.z) {
-      np_ = entries[b + lane];
-      for (int e = 0; e < 3; ++e) nx3[e] = load_coord(g, locs, np_, e);
+  for (int i = tid * 4; i < TFL; i += 256 * 4) *reinterpret_cast<float4*>(acc + i) = make_float4(0.f, 0.f, 0.f, 0.f);
+  const int cu = lane & 3, kzl = (lane >> 2) & 1, ky = lane >> 3;
+  for (int b = it.y; b < it.z; b += kAB) {
+    const int nb = min(kAB, it.z - b);
+    __syncthreads();  // the previous batch has been applied
+    // tasks: (entry j, dim d) for j < kAB, d < 3; warps 0..3 take dimension 0
+    for (int task = tid; task < 3 * kAB; task += 256) {
+      const int j = task % kAB, d = task / kAB;
+      int info = 0;
+      if (j < nb) {
+        rec3_task<false>(g, locs, entries, b, j, d, o, rec);
+        info = rec[j].info[d];
+      }
+      if (d == 0) {
+        // planes touched by the entry's x taps; all planes when the x window
+        // is not a plain run (the generic path checks each tap)
+        const bool okx = (info >> 8) & 1;
+        const bool fx = ((info >> 9) & 1) && g.wrap_safe;
+        const int f = info & 15, n = (info >> 4) & 15;
 #pragma unroll
-      for (int c = 0; c < CG; ++c)
-        nv[c] = c < ncoil ? __ldg(reinterpret_cast<const float2*>(vals) + (long long)(c0 + c) * g.npts + np_)
-                          : make_float2(0.f, 0.f);
+        for (int w = 0; w < NW; ++w) {
+          const unsigned bal = __ballot_sync(0xffffffffu, okx && (!fx || (w >= f && w < f + n)));
+          if (lane == 0) pmask[w * MW + (task >> 5)] = bal;
+        }
+      }
     }
-  };
-  if (it.y < it.z) prefetch(it.y);
-  for (int b = it.y; b < it.z; b += 32) {
-    const int nb = min(32, it.z - b);
-    __syncwarp();
-    if (np_ >= 0) {
-      lane_rec3<false>(g, nx3, o, np_, rec[lane]);
-      float4* d = reinterpret_cast<float4*>(pv + lane * VS);
+    for (int j = tid >> 1; j < nb; j += 128) {
+      // point values of the batch: two threads per entry, 4 entries each
+      const long long p = entries[b + j];
+      const int h = tid & 1;
+      float4* d = reinterpret_cast<float4*>(pv + j * VS) + 2 * h;
 #pragma unroll
-      for (int q = 0; q < 4; ++q) d[q] = make_float4(nv[2 * q].x, nv[2 * q].y, nv[2 * q + 1].x, nv[2 * q + 1].y);
+      for (int q = 0; q < 2; ++q) {
+        const int c = 4 * h + 2 * q;
+        const float2 v0 = c < ncoil ? __ldg(reinterpret_cast<const float2*>(vals) + (long long)(c0 + c) * g.npts + p)
+                                    : make_float2(0.f, 0.f);
+        const float2 v1 = c + 1 < ncoil
+                              ? __ldg(reinterpret_cast<const float2*>(vals) + (long long)(c0 + c + 1) * g.npts + p)
+                              : make_float2(0.f, 0.f);
+        d[q] = make_float4(v0.x, v0.y, v1.x, v1.y);
+      }
     }
-    __syncwarp();
-    if (b + 32 < it.z) prefetch(b + 32);
-    for (int j = 0; j < nb; ++j) {
-      __syncwarp();  // lanes update cells of consecutive points: order them
-      const R3& R = rec[j];
-      const int m = R.m;
-      if (m == 0) continue;
-      if ((m >> 24) && g.wrap_safe) {
-        const int mx = m & 255, my = (m >> 8) & 255, mz = (m >> 16) & 255;
-        if (uz < mz) {
-          const float4 v = *reinterpret_cast<const float4*>(pv + j * VS + cu * 4);
-          const float wz = pick4(R.wz, uz);
-          const float4 wy = R.wy;
-          float* a0 = acc + R.base * VS + lofs;
-#pragma unroll
-          for (int i = 0; i < 2; ++i) {
-            const int kx = kxp + 2 * i;
-            if (kx < mx) {
-              const float wxz = pick4(R.wx, kx) * wz;
-              float* a = a0 + 2 * i * SX;
-              float4 r[4];
-#pragma unroll
-              for (int ky = 0; ky < 4; ++ky)
-                if (ky < my) r[ky] = *reinterpret_cast<const float4*>(a + ky * SY);
-#pragma unroll
-              for (int ky = 0; ky < 4; ++ky)
-                if (ky < my) {
-                  const float w = wxz * pick4(wy, ky);
-                  r[ky].x = fmaf(w, v.x, r[ky].x);
-                  r[ky].y = fmaf(w, v.y, r[ky].y);
-                  r[ky].z = fmaf(w, v.z, r[ky].z);
-                  r[ky].w = fmaf(w, v.w, r[ky].w);
-                  *reinterpret_cast<float4*>(a + ky * SY) = r[ky];
-                }
+    __syncthreads();
+#pragma unroll 1
+    for (int mw = 0; mw < MW; ++mw) {
+      unsigned bits = pmask[warp * MW + mw];
+      while (bits) {
+        const int j = mw * 32 + __ffs(bits) - 1;
+        bits &= bits - 1;
+        __syncwarp();  // consecutive entries may share cells of this plane
+        const R3& R = rec[j];
+        const R3v V = rec3_view<8>(R);
+        if (!V.ok) continue;
+        if (V.fast && g.wrap_safe) {
+          const int t = warp - V.fx;  // in [0, mx) by the mask
+          if (ky < V.my) {
+            const float wxy = (&R.w[0].x)[t] * (&R.w[1].x)[ky];
+            const float4 v = *reinterpret_cast<const float4*>(pv + j * VS + cu * 4);
+            float* a = acc + ((V.base + t * 64 + ky * 8 + kzl) * VS) + cu * 4;
+            const bool z0 = kzl < V.mz, z1 = kzl + 2 < V.mz;
+            float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = r0;
+            if (z0) r0 = *reinterpret_cast<const float4*>(a);
+            if (z1) r1 = *reinterpret_cast<const float4*>(a + 2 * VS);
+            if (z0) {
+              const float w = wxy * (&R.w[2].x)[kzl];
+              r0.x = fmaf(w, v.x, r0.x); r0.y = fmaf(w, v.y, r0.y); r0.z = fmaf(w, v.z, r0.z); r0.w = fmaf(w, v.w, r0.w);
+              *reinterpret_cast<float4*>(a) = r0;
+            }
+            if (z1) {
+              const float w = wxy * (&R.w[2].x)[kzl + 2];
+              r1.x = fmaf(w, v.x, r1.x); r1.y = fmaf(w, v.y, r1.y); r1.z = fmaf(w, v.z, r1.z); r1.w = fmaf(w, v.w, r1.w);
+              *reinterpret_cast<float4*>(a + 2 * VS) = r1;
             }
           }
+          continue;
         }
-        continue;
-      }
-      // exact-integer coordinates (5 taps) or a window wrapping inside the
-      // tile: generic record, taps in order by the lanes of each entry pair
-      if (lane == 0) {
-        float x3[3];
-        for (int e = 0; e < 3; ++e) x3[e] = load_coord(g, locs, R.p, e);
-        lane_rec<5>(g, x3, o, false, slow[0]);
-      }
-      __syncwarp();
-      const Rec<5>& S = slow[0];
-      if (S.m[0] > 0 && lane < 4) {
-        const float4 vv = *reinterpret_cast<const float4*>(pv + j * VS + lane * 4);
-        for (int kx = 0; kx < S.m[0]; ++kx)
-          for (int ky = 0; ky < S.m[1]; ++ky)
-            for (int kz = 0; kz < S.m[2]; ++kz) {
-              const float w = g.norm == 1 ? S.wv[0][kx] * S.wv[1][ky] * S.wv[2][kz]
-                                          : radial_w(g, S.wv[0][kx], S.wv[1][ky], S.wv[2][kz]);
-              float* a = acc + ((S.lc[0][kx] * 8 + S.lc[1][ky]) * 8 + S.lc[2][kz]) * VS + lane * 4;
-              float4 r = *reinterpret_cast<float4*>(a);
-              r.x = fmaf(w, vv.x, r.x); r.y = fmaf(w, vv.y, r.y); r.z = fmaf(w, vv.z, r.z); r.w = fmaf(w, vv.w, r.w);
-              *reinterpret_cast<float4*>(a) = r;
-            }
+        // exact-integer coordinates (5 taps) or a window wrapping inside the
+        // tile: generic record, this plane's taps in order by 4 lanes
+        if (lane == 0) {
+          float x3[3];
+          for (int e = 0; e < 3; ++e) x3[e] = load_coord(g, locs, V.p, e);
+          lane_rec<5>(g, x3, o, false, slow[warp]);
+        }
+        __syncwarp();
+        const Rec<5>& S = slow[warp];
+        if (lane < 4) {
+          const float4 vv = *reinterpret_cast<const float4*>(pv + j * VS + lane * 4);
+          for (int kx = 0; kx < S.m[0]; ++kx) {
+            if (S.lc[0][kx] != warp) continue;
+            for (int kyy = 0; kyy < S.m[1]; ++kyy)
+              for (int kz = 0; kz < S.m[2]; ++kz) {
+                const float w = g.norm == 1 ? S.wv[0][kx] * S.wv[1][kyy] * S.wv[2][kz]
+                                            : radial_w(g, S.wv[0][kx], S.wv[1][kyy], S.wv[2][kz]);
+                float* a = acc + ((warp * 8 + S.lc[1][kyy]) * 8 + S.lc[2][kz]) * VS + lane * 4;
+                float4 r = *reinterpret_cast<float4*>(a);
+                r.x = fmaf(w, vv.x, r.x); r.y = fmaf(w, vv.y, r.y); r.z = fmaf(w, vv.z, r.z); r.w = fmaf(w, vv.w, r.w);
+                *reinterpret_cast<float4*>(a) = r;
+              }
+          }
+        }
       }
     }
   }
-  __syncwarp();
+  __syncthreads();
   if (it.w >= 0) {
     float* dst = partial + ((long long)it.w * gridDim.y + cg) * TFL;
-    for (int i = lane * 4; i < TFL; i += 128)
+    for (int i = tid * 4; i < TFL; i += 256 * 4)
       *reinterpret_cast<float4*>(dst + i) = *reinterpret_cast<const float4*>(acc + i);
     return;
   }
-  // write-out: per (x, y) row 8 z x 8 entries; lanes (entry fastest, z)
+  // write-out: warp = x plane, per (x, y) row 8 z x 8 entries; lanes (entry fastest, z)
   const long long gvol = (long long)g.N[0] * g.N[1] * g.N[2];
-  for (int row = 0; row < 64; ++row) {
-    const int x = row >> 3, y = row & 7;
-    const int gx = o[0] + x, gy = o[1] + y;
-    if (gx >= g.N[0] || gy >= g.N[1]) continue;
-    const float* srow = acc + row * 8 * VS;
+  const int gx = o[0] + warp;
+  if (gx >= g.N[0]) return;
+  for (int y = 0; y < 8; ++y) {
+    const int gy = o[1] + y;
+    if (gy >= g.N[1]) break;
+    const float* srow = acc + (warp * 8 + y) * 8 * VS;
     float* drow = gridv + (((long long)gx * g.N[1] + gy) * g.N[2] + o[2]) * 2;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
@@ -1172,26 +1247,29 @@ __global__ void __launch_bounds__(32, 6) adj_f3_kernel(Geo g, const int4* __rest
   }
 }
 
-// Gather: CTA = 16 warps sharing one 12^3 x 8-entry region ([entry][x][y][z],
-// loaded by one TMA bulk tensor copy when the region needs no wrap); lanes =
-// (x-tap parity, y-tap, z-tap), entries looped, reduced by shuffles.
-__global__ void __launch_bounds__(512, 1) fwd_f3_kernel(const __grid_constant__ CUtensorMap tmap, int use_tma, Geo g,
+// Gather: CTA = 8 warps sharing one 12^3 x 8-entry region ([entry][x][y][z],
+// loaded by one TMA bulk tensor copy when the region needs no wrap), two CTAs
+// per SM. Records of kGB entries are built per batch, one per thread; each
+// warp then takes every 8th point. Lanes = (z-tap, y-tap, entry half): a lane
+// sums 4 x-taps x 4 entries, then 8 values are reduced over 16 lanes.
+constexpr int kGB = 64;
+
+__global__ void __launch_bounds__(256, 2) fwd_f3_kernel(const __grid_constant__ CUtensorMap tmap, int use_tma, Geo g,
                                                         const int4* __restrict__ items,
                                                         const int32_t* __restrict__ entries,
                                                         const float* __restrict__ locs,
                                                         const float* __restrict__ gridv, float* __restrict__ out) {
-  constexpr int CG = 8, S = 12, PLANE = S * S, VOL = S * S * S, NW = 16;
+  constexpr int CG = 8, S = 12, PLANE = S * S, VOL = S * S * S, NW = 8;
   constexpr uint32_t RBYTES = VOL * CG * 8;
-  extern __shared__ __align__(1024) unsigned char smem[];
-  float2* reg = reinterpret_cast<float2*>(smem);                     // [8][12][12][12]
-  R3* recs = reinterpret_cast<R3*>(smem + RBYTES);                   // [16][32]
-  Rec<5>* slow = reinterpret_cast<Rec<5>*>(recs + NW * 32);          // [16]
-  static_assert((NW * 32 * sizeof(R3) + NW * sizeof(Rec<5>)) % 8 == 0, "mbarrier alignment");
+  extern __shared__ __align__(128) unsigned char smem[];
+  float2* reg = reinterpret_cast<float2*>(smem);               // [8][12][12][12]
+  R3* rec = reinterpret_cast<R3*>(smem + RBYTES);              // [kGB]
+  Rec<5>* slow = reinterpret_cast<Rec<5>*>(rec + kGB);         // [NW]
+  static_assert((kGB * sizeof(R3) + NW * sizeof(Rec<5>)) % 8 == 0, "mbarrier alignment");
   uint64_t* bar = reinterpret_cast<uint64_t*>(slow + NW);
   const int4 it = items[blockIdx.x];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int c0 = blockIdx.y * CG;
-  const int ncoil = (int)min((long long)CG, g.nbatch - c0);
   int o[3];
   {
     int t = it.x;
@@ -1204,19 +1282,20 @@ __global__ void __launch_bounds__(512, 1) fwd_f3_kernel(const __grid_constant__ 
   const bool wraps = g.pad == TLGB_PAD_CIRCULAR && (o[0] + S > g.N[0] || o[1] + S > g.N[1] || o[2] + S > g.N[2]);
   const bool tma = use_tma && !wraps;
   if (tma) {
-    if (threadIdx.x == 0) {
+    if (tid == 0) {
       mbar_init(bar, 1);
       fence_mbar_init();
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (tid == 0) {
       mbar_arrive_expect_tx(bar, RBYTES);
       tma_load_4d(reg, &tmap, bar, o[2], o[1], o[0], c0);
     }
   } else {
-    // manual staging with wrap / zero fill: rows (entry, x, y) of 12 z
+    // plain loads with wrap / zero fill: rows (entry, x, y) of 12 z
+    const int ncoil = (int)min((long long)CG, g.nbatch - c0);
     const long long gvol = (long long)g.N[0] * g.N[1] * g.N[2];
-    for (int idx = threadIdx.x; idx < CG * VOL; idx += NW * 32) {
+    for (int idx = tid; idx < CG * VOL; idx += NW * 32) {
       const int z = idx % S;
       const int r = idx / S;
       const int y = r % S, x = (r / S) % S, c = r / PLANE;
@@ -1234,72 +1313,69 @@ __global__ void __launch_bounds__(512, 1) fwd_f3_kernel(const __grid_constant__ 
                     : make_float2(0.f, 0.f);
     }
   }
-  // tap records of this warp's first batch while the copy is in flight
-  R3* rbuf = recs + warp * 32;
-  int b = it.y + warp * 32;
-  if (b + lane < it.z) {
-    const long long p = entries[b + lane];
-    float x3[3];
-    for (int e = 0; e < 3; ++e) x3[e] = load_coord(g, locs, p, e);
-    lane_rec3<true>(g, x3, o, p, rbuf[lane]);
-  }
-  if (tma) {
-    if (!mbar_wait_bounded(bar, 0, 1u << 24)) {
-      if (lane == 0) atomicExch(&g_tlgb_status, 1);
-      // the copy never completed: give up on this item without reading it
+  const int kz = lane & 3, ky = (lane >> 2) & 3, ch = lane >> 4;
+  auto build_records = [&](int b) {
+    // tasks (entry j, dim d): warps 2d, 2d + 1 take dimension d
+    const int j = tid & (kGB - 1), d = tid / kGB;
+    if (d < 3 && j < min(kGB, it.z - b)) rec3_task<true>(g, locs, entries, b, j, d, o, rec);
+  };
+  build_records(it.y);  // while the region copy is in flight
+  {
+    // the copy must have landed: bounded wait, then a CTA-wide vote
+    bool ok = true;
+    if (tma) ok = mbar_wait_bounded(bar, 0, 1u << 22);
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) atomicExch(&g_tlgb_status, 1);
       return;
     }
-  } else {
-    __syncthreads();
   }
-
-  const int kz = lane & 3, ky = (lane >> 2) & 3, kxp = lane >> 4;
-  for (; b < it.z; b += NW * 32) {
-    const int nb = min(32, it.z - b);
-    if (b != it.y + warp * 32 && b + lane < it.z) {
-      const long long p = entries[b + lane];
-      float x3[3];
-      for (int e = 0; e < 3; ++e) x3[e] = load_coord(g, locs, p, e);
-      lane_rec3<true>(g, x3, o, p, rbuf[lane]);
+  for (int b = it.y; b < it.z; b += kGB) {
+    const int nb = min(kGB, it.z - b);
+    if (b != it.y) {
+      __syncthreads();  // the previous batch has been read
+      build_records(b);
+      __syncthreads();
     }
-    __syncwarp();
-    for (int j = 0; j < nb; ++j) {
-      const R3& R = rbuf[j];
-      const int m = R.m;
-      if (m == 0) continue;  // warp-uniform
-      float acc[2 * CG];
+    for (int j = warp; j < nb; j += NW) {
+      const R3& R = rec[j];
+      const R3v V = rec3_view<S>(R);
+      if (!V.ok) continue;  // warp-uniform
+      float acc[8];
 #pragma unroll
-      for (int i = 0; i < 2 * CG; ++i) acc[i] = 0.f;
-      if (m >> 24) {
-        const int mx = m & 255, my = (m >> 8) & 255, mz = (m >> 16) & 255;
-        const float wyz = (ky < my && kz < mz) ? pick4(R.wy, ky) * pick4(R.wz, kz) : 0.f;
-        const float w0 = kxp < mx ? pick4(R.wx, kxp) * wyz : 0.f;
-        const float w1 = kxp + 2 < mx ? pick4(R.wx, kxp + 2) * wyz : 0.f;
-        const float2* a = reg + R.base + kxp * PLANE + ky * S + kz;
+      for (int i = 0; i < 8; ++i) acc[i] = 0.f;
+      if (V.fast) {
+        const float wyz = (ky < V.my && kz < V.mz) ? (&R.w[1].x)[ky] * (&R.w[2].x)[kz] : 0.f;
+        const float2* a = reg + ch * 4 * VOL + V.base + ky * S + kz;
+        const float4 wx = R.w[0];
 #pragma unroll
-        for (int c = 0; c < CG; ++c) {
-          const float2 v0 = a[c * VOL];
-          const float2 v1 = a[c * VOL + 2 * PLANE];
-          acc[2 * c] = fmaf(w0, v0.x, fmaf(w1, v1.x, acc[2 * c]));
-          acc[2 * c + 1] = fmaf(w0, v0.y, fmaf(w1, v1.y, acc[2 * c + 1]));
+        for (int kx = 0; kx < 4; ++kx) {
+          if (kx < V.mx) {
+            const float w = (kx == 0 ? wx.x : kx == 1 ? wx.y : kx == 2 ? wx.z : wx.w) * wyz;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+              const float2 v = a[c * VOL + kx * PLANE];
+              acc[2 * c] = fmaf(w, v.x, acc[2 * c]);
+              acc[2 * c + 1] = fmaf(w, v.y, acc[2 * c + 1]);
+            }
+          }
         }
       } else {
         // exact-integer coordinates: generic record
         if (lane == 0) {
           float x3[3];
-          for (int e = 0; e < 3; ++e) x3[e] = load_coord(g, locs, R.p, e);
+          for (int e = 0; e < 3; ++e) x3[e] = load_coord(g, locs, V.p, e);
           lane_rec<5>(g, x3, o, true, slow[warp]);
         }
         __syncwarp();
         const Rec<5>& Sr = slow[warp];
         for (int kzz = kz; kzz < Sr.m[2]; kzz += 4)
           for (int kyy = ky; kyy < Sr.m[1]; kyy += 4)
-            for (int kx = kxp; kx < Sr.m[0]; kx += 2) {
+            for (int kx = 0; kx < Sr.m[0]; ++kx) {
               const float w = g.norm == 1 ? Sr.wv[0][kx] * Sr.wv[1][kyy] * Sr.wv[2][kzz]
                                           : radial_w(g, Sr.wv[0][kx], Sr.wv[1][kyy], Sr.wv[2][kzz]);
-              const float2* a = reg + (Sr.lc[0][kx] * S + Sr.lc[1][kyy]) * S + Sr.lc[2][kzz];
+              const float2* a = reg + ch * 4 * VOL + (Sr.lc[0][kx] * S + Sr.lc[1][kyy]) * S + Sr.lc[2][kzz];
 #pragma unroll
-              for (int c = 0; c < CG; ++c) {
+              for (int c = 0; c < 4; ++c) {
                 const float2 v = a[c * VOL];
                 acc[2 * c] = fmaf(w, v.x, acc[2 * c]);
                 acc[2 * c + 1] = fmaf(w, v.y, acc[2 * c + 1]);
@@ -1307,19 +1383,15 @@ __global__ void __launch_bounds__(512, 1) fwd_f3_kernel(const __grid_constant__ 
             }
         __syncwarp();
       }
-      // reduce-scatter the 16 partial sums over the 32 lanes: lane L ends
-      // with the sum of value L >> 1 (entry (L >> 2), re if L & 2 == 0)
-      float s8[8], s4[4], s2[2];
-      const bool b4 = lane & 16, b3 = lane & 8, b2 = lane & 4, b1 = lane & 2;
-#pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        const float send = b4 ? acc[i] : acc[i + 8];
-        s8[i] = (b4 ? acc[i + 8] : acc[i]) + __shfl_xor_sync(0xffffffffu, send, 16);
-      }
+      // reduce-scatter 8 values over the 16 lanes of each entry half: lane L
+      // ends with value (L >> 1) & 7 (entry (L >> 2) & 3 of its half, re if
+      // L & 2 == 0)
+      float s4[4], s2[2];
+      const bool b3 = lane & 8, b2 = lane & 4, b1 = lane & 2;
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
-        const float send = b3 ? s8[i] : s8[i + 4];
-        s4[i] = (b3 ? s8[i + 4] : s8[i]) + __shfl_xor_sync(0xffffffffu, send, 8);
+        const float send = b3 ? acc[i] : acc[i + 4];
+        s4[i] = (b3 ? acc[i + 4] : acc[i]) + __shfl_xor_sync(0xffffffffu, send, 8);
       }
 #pragma unroll
       for (int i = 0; i < 2; ++i) {
@@ -1333,13 +1405,10 @@ __global__ void __launch_bounds__(512, 1) fwd_f3_kernel(const __grid_constant__ 
       }
       s1 += __shfl_xor_sync(0xffffffffu, s1, 1);
       const float im = __shfl_down_sync(0xffffffffu, s1, 2);
-      if ((lane & 3) == 0) {
-        const int c = lane >> 2;
-        if (c < ncoil)
-          *reinterpret_cast<float2*>(out + ((long long)(c0 + c) * g.npts + R.p) * 2) = make_float2(s1, im);
-      }
+      const int c = c0 + ch * 4 + ((lane >> 2) & 3);
+      if ((lane & 3) == 0 && c < g.nbatch)
+        *reinterpret_cast<float2*>(out + ((long long)c * g.npts + V.p) * 2) = make_float2(s1, im);
     }
-    __syncwarp();
   }
 }
 
@@ -1684,6 +1753,7 @@ int check_plan(const Geo& g, const tlgb_interp_plan_info* info, const void* plan
 template <typename F>
 int set_smem(F* kernel, size_t bytes) {
   TLGB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  TLGB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   return TLGB_OK;
 }
 
@@ -1873,7 +1943,7 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 int launch_fwd_f3(const Geo& g, const tlgb_interp_plan_info* info, const char* P, const float* locs,
                   const void* grid, void* out, cudaStream_t s) {
   const int64_t ncg = cdiv(g.nbatch, 8);
-  const size_t sm = 12 * 12 * 12 * 8 * 8 + 16 * 32 * sizeof(R3) + 16 * sizeof(Rec<5>) + 16;
+  const size_t sm = 12 * 12 * 12 * 8 * 8 + kGB * sizeof(R3) + 8 * sizeof(Rec<5>) + 8;
   // 4D tensor map over [batch][X][Y][Z] complex64 (8-byte elements), box 12^3 x 8
   CUtensorMap tmap;
   memset(&tmap, 0, sizeof(tmap));
@@ -1892,7 +1962,7 @@ int launch_fwd_f3(const Geo& g, const tlgb_interp_plan_info* info, const char* P
   }
   TLGB_TRY(set_smem(fwd_f3_kernel, sm));
   dim3 grd((unsigned)info->n_fwd_items, (unsigned)ncg);
-  fwd_f3_kernel<<<grd, 512, sm, s>>>(tmap, use_tma, g, (const int4*)(P + info->off_fwd_items),
+  fwd_f3_kernel<<<grd, 256, sm, s>>>(tmap, use_tma, g, (const int4*)(P + info->off_fwd_items),
                                      (const int32_t*)(P + info->off_entries), locs, (const float*)grid, (float*)out);
   TLGB_CHECK_LAUNCH();
   return TLGB_OK;
@@ -1901,10 +1971,11 @@ int launch_fwd_f3(const Geo& g, const tlgb_interp_plan_info* info, const char* P
 int launch_adj_f3(const Geo& g, const tlgb_interp_plan_info* info, const char* P, const float* locs,
                   const void* vals, void* grid, void* scratch, cudaStream_t s) {
   const int64_t ncg = cdiv(g.nbatch, 8);
-  const size_t sm = 512 * 16 * sizeof(float) + 32 * sizeof(R3) + 32 * 16 * sizeof(float) + sizeof(Rec<5>);
+  const size_t sm = 512 * 16 * sizeof(float) + kAB * (sizeof(R3) + 16 * sizeof(float)) + 8 * sizeof(Rec<5>) +
+                    8 * (kAB / 32) * sizeof(unsigned);
   TLGB_TRY(set_smem(adj_f3_kernel, sm));
   dim3 grd((unsigned)info->n_adj_items, (unsigned)ncg);
-  adj_f3_kernel<<<grd, 32, sm, s>>>(g, (const int4*)(P + info->off_adj_items), (const int32_t*)(P + info->off_entries),
+  adj_f3_kernel<<<grd, 256, sm, s>>>(g, (const int4*)(P + info->off_adj_items), (const int32_t*)(P + info->off_entries),
                                     locs, (const float*)vals, (float*)grid, (float*)scratch);
   TLGB_CHECK_LAUNCH();
   if (info->n_split_tiles > 0) {
