@@ -226,6 +226,56 @@ int tlgb_cg_set_pap(const float* p, const float* ap, int64_t n, int is_complex, 
 int tlgb_cg_step(float* x, float* r, float* p, const float* ap, int64_t n, int is_complex, double* state,
                  void* scratch, size_t scratch_bytes, tlgb_stream_t stream);
 
+/* ------------------------------------------------------------------------ */
+/* 3^3 convolution on the tensor cores (BF16 operands, FP32 accumulation):    */
+/* the layers of the learned CG preconditioner. No counterpart in the         */
+/* reference (torchlinops has no learned preconditioner).                     */
+/* ------------------------------------------------------------------------ */
+
+/* Epilogue of tlgb_conv3d_fwd. */
+enum {
+  TLGB_CONV_PLAIN = 0, /* y = conv(x, w)                                     */
+  TLGB_CONV_RELU = 1,  /* y = max(conv(x, w), 0)                             */
+  TLGB_CONV_MASK = 2   /* y = conv(x, w) * (aux > 0): data gradient through a
+                          ReLU whose output is aux                           */
+};
+
+typedef struct tlgb_conv3d_desc {
+  int32_t D, H, W;   /* spatial size, the same in and out (zero padding 1)  */
+  int32_t cin, cout; /* 16 and 16: pad narrower layers with zero channels    */
+  int32_t mode;      /* TLGB_CONV_*                                          */
+  int32_t out_f32;   /* 1: float32 output [D][H][W][16], else bfloat16       */
+  int32_t reserved;
+} tlgb_conv3d_desc;
+
+/* y[v][co] = sum_{t, ci} w[t][co][ci] x[v + off(t)][ci], activations
+ * channels-last [D][H][W][16] bfloat16, weights [27][16][16] bfloat16 with
+ * tap t = (kd*3 + kh)*3 + kw reading input offset (kd-1, kh-1, kw-1).
+ * The data gradient is this call with w'[26 - t][ci][co] = w[t][co][ci].
+ * Buffers 16-byte aligned. */
+int tlgb_conv3d_fwd(const tlgb_conv3d_desc* d, const void* x, const void* w, const void* aux, void* y,
+                    tlgb_stream_t stream);
+
+/* Device scratch for tlgb_conv3d_wgrad. */
+int tlgb_conv3d_wgrad_scratch_size(const tlgb_conv3d_desc* d, size_t* bytes);
+
+/* dw[t][co][ci] = sum_v gy[v][co] x[v + off(t)][ci] (float32), summed in a
+ * fixed order (bit-identical run to run). */
+int tlgb_conv3d_wgrad(const tlgb_conv3d_desc* d, const void* x, const void* gy, float* dw, void* scratch,
+                      size_t scratch_bytes, tlgb_stream_t stream);
+
+/* complex64 z[V] times *scale (device float; NULL = 1) -> bfloat16 [V][16]
+ * with channels 0, 1 = real, imaginary rounded to bfloat16 and, if hilo,
+ * channels 2, 3 = their rounding remainders (a two-term split with 16
+ * significant bits); the other channels zero. */
+int tlgb_conv3d_pack(const void* z, int64_t nvox, const float* scale, int32_t hilo, void* out,
+                     tlgb_stream_t stream);
+
+/* out[v] = *scale * (y[v][0] + i y[v][1]) + skip * z[v] (z may be NULL):
+ * float32 [V][16] network output back to complex64. */
+int tlgb_conv3d_unpack(const float* y, const void* z, int64_t nvox, const float* scale, float skip, void* out,
+                       tlgb_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,341 @@
+// 3^3 convolution, 16 -> 16 channels, BF16 operands with FP32 accumulation, on
+// the tensor cores: the layers of the learned CG preconditioner (no
+// counterpart in the reference; it replaces nothing there).
+//
+// Layout: activations channels-last [D][H][W][16] bf16, zero padding 1, same
+// spatial size in and out. Weights [27][16 out][16 in] bf16, tap t = (kd*3 +
+// kh)*3 + kw. Forward and data-gradient are one implicit-GEMM kernel (the
+// data gradient is the forward with flipped, transposed weights); the weight
+// gradient is a second kernel with a fixed-order cross-CTA reduction.
+
+#include <cuda_bf16.h>
+
+#include "common.cuh"
+
+namespace tlgb {
+namespace {
+
+constexpr int kTileW = 64;               // output voxels along W per CTA (4 warps x 16)
+constexpr int kHaloW = kTileW + 2;       // input voxels along W per (kd, kh) row
+constexpr int kHaloRows = 9;             // (kd, kh) rows
+constexpr int kVoxBytes = 32;            // 16 bf16 channels
+constexpr int kTaps = 27;
+
+// 16-byte chunk c of row j in a 32-byte-row tile, XOR-swizzled so that the 8
+// row addresses of one ldmatrix phase fall in distinct banks
+__device__ __forceinline__ uint32_t swz(int j, int c) { return (uint32_t)(j * 32 + ((c ^ ((j >> 2) & 1)) << 4)); }
+
+__device__ __forceinline__ void ldsm_x4(uint32_t addr, uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];"
+               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+               : "r"(addr));
+}
+__device__ __forceinline__ void ldsm_x4_t(uint32_t addr, uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0, %1, %2, %3}, [%4];"
+               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+               : "r"(addr));
+}
+// D(16x8, f32) += A(16x16, bf16, row) * B(16x8, bf16, col)
+__device__ __forceinline__ void mma_bf16(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t b0,
+                                         uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+      "{%0, %1, %2, %3};"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// The 9 (kd, kh) input rows of kHaloW voxels around output row (d, h, w0..):
+// zero outside the volume. Row r = kd*3 + kh, voxel j = input w0 - 1 + j.
+__device__ __forceinline__ void load_halo(unsigned char* halo, const uint4* __restrict__ x, int D, int H, int W, int d,
+                                          int h, int w0) {
+  for (int i = threadIdx.x; i < kHaloRows * kHaloW * 2; i += blockDim.x) {
+    const int c = i & 1;
+    const int j = (i >> 1) % kHaloW;
+    const int r = (i >> 1) / kHaloW;
+    const int di = d + r / 3 - 1, hi = h + r % 3 - 1, wi = w0 - 1 + j;
+    uint4 v = make_uint4(0u, 0u, 0u, 0u);
+    if (di >= 0 && di < D && hi >= 0 && hi < H && wi >= 0 && wi < W)
+      v = __ldg(x + ((((long long)di * H + hi) * W + wi) * 2 + c));
+    *reinterpret_cast<uint4*>(halo + r * kHaloW * kVoxBytes + swz(j, c)) = v;
+  }
+}
+
+// MODE 0: plain; 1: ReLU; 2: multiply by (aux > 0) (the ReLU mask of a
+// forward output, for the data gradient). OUTF32: float32 output.
+template <int MODE, bool OUTF32>
+__global__ void __launch_bounds__(128) conv3d_fwd_kernel(int D, int H, int W, const uint4* __restrict__ x,
+                                                         const uint4* __restrict__ wts,
+                                                         const __nv_bfloat16* __restrict__ aux, void* __restrict__ y) {
+  __shared__ __align__(128) unsigned char halo[kHaloRows * kHaloW * kVoxBytes];
+  __shared__ __align__(128) unsigned char wsm[kTaps * 16 * kVoxBytes];
+  const int w0 = blockIdx.x * kTileW, h = blockIdx.y, d = blockIdx.z;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  load_halo(halo, x, D, H, W, d, h, w0);
+  for (int i = threadIdx.x; i < kTaps * 16 * 2; i += blockDim.x) {
+    const int c = i & 1, n = (i >> 1) & 15, t = i >> 5;
+    *reinterpret_cast<uint4*>(wsm + t * 16 * kVoxBytes + swz(n, c)) = __ldg(wts + i);
+  }
+  __syncthreads();
+
+  float acc[2][4];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int k = 0; k < 4; ++k) acc[i][k] = 0.f;
+  // ldmatrix row roles: A (16 voxels x 16 ch): row = voxel, chunk = k half;
+  // B (16 out x 16 in, stored [n][k]): row = n
+  const int a_row = (lane & 7) + 8 * ((lane >> 3) & 1), a_chunk = lane >> 4;
+  const int b_row = (lane & 7) + 8 * (lane >> 4), b_chunk = (lane >> 3) & 1;
+  const uint32_t hbase = smem_addr(halo), wbase = smem_addr(wsm);
+#pragma unroll 1
+  for (int t = 0; t < kTaps; ++t) {
+    const int r = t / 3, kw = t % 3;
+    uint32_t a0, a1, a2, a3, b0, b1, b2, b3;
+    ldsm_x4(hbase + r * kHaloW * kVoxBytes + swz(warp * 16 + kw + a_row, a_chunk), a0, a1, a2, a3);
+    ldsm_x4(wbase + t * 16 * kVoxBytes + swz(b_row, b_chunk), b0, b1, b2, b3);
+    mma_bf16(acc[0], a0, a1, a2, a3, b0, b1);
+    mma_bf16(acc[1], a0, a1, a2, a3, b2, b3);
+  }
+  // D fragment: rows gid, gid + 8 (voxels), columns 2*tig, 2*tig + 1 (+ 8 for chunk 1)
+  const int gid = lane >> 2, tig = lane & 3;
+#pragma unroll
+  for (int hr = 0; hr < 2; ++hr) {
+    const int w = w0 + warp * 16 + gid + 8 * hr;
+    if (w >= W) continue;
+    const long long v = ((long long)d * H + h) * W + w;
+#pragma unroll
+    for (int ch = 0; ch < 2; ++ch) {
+      const int co = ch * 8 + 2 * tig;
+      float y0 = acc[ch][2 * hr], y1 = acc[ch][2 * hr + 1];
+      if (MODE == 1) {
+        y0 = fmaxf(y0, 0.f);
+        y1 = fmaxf(y1, 0.f);
+      } else if (MODE == 2) {
+        const __nv_bfloat162 m = *reinterpret_cast<const __nv_bfloat162*>(aux + v * 16 + co);
+        y0 = __bfloat162float(m.x) > 0.f ? y0 : 0.f;
+        y1 = __bfloat162float(m.y) > 0.f ? y1 : 0.f;
+      }
+      if (OUTF32) {
+        *reinterpret_cast<float2*>(reinterpret_cast<float*>(y) + v * 16 + co) = make_float2(y0, y1);
+      } else {
+        *reinterpret_cast<__nv_bfloat162*>(reinterpret_cast<__nv_bfloat16*>(y) + v * 16 + co) =
+            __floats2bfloat162_rn(y0, y1);
+      }
+    }
+  }
+}
+
+// Weight gradient: dW[t][co][ci] = sum over output voxels v of gy[v][co] *
+// x[v + offset(t)][ci]. CTA b takes output rows b, b + grid, ... (fixed), warp
+// w the taps w, w + 4, ...; partial sums per CTA are reduced in CTA order.
+constexpr int kWgTapsPerWarp = 7;
+
+__global__ void __launch_bounds__(128) conv3d_wgrad_kernel(int D, int H, int W, const uint4* __restrict__ x,
+                                                           const uint4* __restrict__ gy, float* __restrict__ partial) {
+  __shared__ __align__(128) unsigned char halo[kHaloRows * kHaloW * kVoxBytes];
+  __shared__ __align__(128) unsigned char gsm[kTileW * kVoxBytes];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int ntw = (W + kTileW - 1) / kTileW;
+  const long long nrows = (long long)D * H * ntw;
+  float acc[kWgTapsPerWarp][2][4];
+#pragma unroll
+  for (int i = 0; i < kWgTapsPerWarp; ++i)
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+      for (int k = 0; k < 4; ++k) acc[i][j][k] = 0.f;
+  // ldmatrix.trans roles. A = gy^T (16 out x 16 voxels) from gsm [voxel][co]:
+  // matrix q holds voxels 8*(q >> 1).., channels 8*(q & 1)..
+  const int ga_row = (lane & 7) + 8 * (lane >> 4), ga_chunk = (lane >> 3) & 1;
+  // B = x (16 voxels x 8 in) from the halo [voxel][ci]: matrix q holds
+  // voxels 8*(q & 1).., channels 8*(q >> 1)..
+  const int xb_row = (lane & 7) + 8 * ((lane >> 3) & 1), xb_chunk = lane >> 4;
+  const uint32_t hbase = smem_addr(halo), gbase = smem_addr(gsm);
+  for (long long row = blockIdx.x; row < nrows; row += gridDim.x) {
+    const int wt = (int)(row % ntw);
+    const long long dh = row / ntw;
+    const int h = (int)(dh % H), d = (int)(dh / H);
+    const int w0 = wt * kTileW;
+    __syncthreads();  // the previous row's tiles have been read
+    load_halo(halo, x, D, H, W, d, h, w0);
+    for (int i = threadIdx.x; i < kTileW * 2; i += blockDim.x) {
+      const int c = i & 1, j = i >> 1;
+      const int w = w0 + j;
+      uint4 v = make_uint4(0u, 0u, 0u, 0u);
+      if (w < W) v = __ldg(gy + ((((long long)d * H + h) * W + w) * 2 + c));
+      *reinterpret_cast<uint4*>(gsm + swz(j, c)) = v;
+    }
+    __syncthreads();
+#pragma unroll 1
+    for (int ks = 0; ks < kTileW / 16; ++ks) {
+      uint32_t a0, a1, a2, a3;
+      ldsm_x4_t(gbase + swz(ks * 16 + ga_row, ga_chunk), a0, a1, a2, a3);
+      // A fragment order: (co 0-7, v 0-7), (co 8-15, v 0-7), (co 0-7, v 8-15), (co 8-15, v 8-15)
+      // = stored blocks (v lo, c lo), (v lo, c hi), (v hi, c lo), (v hi, c hi): a0, a1, a2, a3
+#pragma unroll
+      for (int i = 0; i < kWgTapsPerWarp; ++i) {
+        const int t = warp + 4 * i;
+        if (t < kTaps) {
+          const int r = t / 3, kw = t % 3;
+          uint32_t b0, b1, b2, b3;
+          ldsm_x4_t(hbase + r * kHaloW * kVoxBytes + swz(ks * 16 + kw + xb_row, xb_chunk), b0, b1, b2, b3);
+          // b0: (v lo, ci lo), b1: (v hi, ci lo), b2: (v lo, ci hi), b3: (v hi, ci hi)
+          mma_bf16(acc[i][0], a0, a1, a2, a3, b0, b1);
+          mma_bf16(acc[i][1], a0, a1, a2, a3, b2, b3);
+        }
+      }
+    }
+  }
+  const int gid = lane >> 2, tig = lane & 3;
+  float* dst = partial + (long long)blockIdx.x * kTaps * 256;
+#pragma unroll
+  for (int i = 0; i < kWgTapsPerWarp; ++i) {
+    const int t = warp + 4 * i;
+    if (t >= kTaps) continue;
+#pragma unroll
+    for (int ch = 0; ch < 2; ++ch)
+#pragma unroll
+      for (int hr = 0; hr < 2; ++hr) {
+        const int co = gid + 8 * hr, ci = ch * 8 + 2 * tig;
+        *reinterpret_cast<float2*>(dst + t * 256 + co * 16 + ci) = make_float2(acc[i][ch][2 * hr], acc[i][ch][2 * hr + 1]);
+      }
+  }
+}
+
+__global__ void wgrad_reduce_kernel(const float* __restrict__ partial, int nparts, float* __restrict__ dw) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= kTaps * 256) return;
+  float s = 0.f;
+  for (int b = 0; b < nparts; ++b) s += partial[(long long)b * kTaps * 256 + i];
+  dw[i] = s;
+}
+
+// complex64 [V] * scale -> bf16 [V][16]: channels 0, 1 = re, im rounded to
+// bf16; with hilo, channels 2, 3 = the rounding remainders (a two-term bf16
+// split carrying 16 mantissa bits); the rest 0
+__global__ void pack_c64_kernel(const float2* __restrict__ z, long long nvox, const float* __restrict__ scale,
+                                int hilo, uint4* __restrict__ out) {
+  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nvox) return;
+  const float s = scale ? *scale : 1.f;
+  const float2 a = z[v];
+  const float re = a.x * s, im = a.y * s;
+  const __nv_bfloat162 p = __floats2bfloat162_rn(re, im);
+  uint32_t q = 0u;
+  if (hilo) {
+    const __nv_bfloat162 r = __floats2bfloat162_rn(re - __bfloat162float(p.x), im - __bfloat162float(p.y));
+    q = *reinterpret_cast<const uint32_t*>(&r);
+  }
+  out[2 * v] = make_uint4(*reinterpret_cast<const uint32_t*>(&p), q, 0u, 0u);
+  out[2 * v + 1] = make_uint4(0u, 0u, 0u, 0u);
+}
+
+// float32 [V][16] channels 0, 1 -> complex64 [V]: out = scale * y + skip * z
+__global__ void unpack_c64_kernel(const float* __restrict__ y, const float2* __restrict__ z, long long nvox,
+                                  const float* __restrict__ scale, float skip, float2* __restrict__ out) {
+  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nvox) return;
+  const float s = scale ? *scale : 1.f;
+  const float2 a = *reinterpret_cast<const float2*>(y + v * 16);
+  float2 r = make_float2(a.x * s, a.y * s);
+  if (z) {
+    const float2 b = z[v];
+    r.x = fmaf(skip, b.x, r.x);
+    r.y = fmaf(skip, b.y, r.y);
+  }
+  out[v] = r;
+}
+
+int check_conv(const tlgb_conv3d_desc* d) {
+  if (!d) TLGB_FAIL(TLGB_ERR_INVALID, "null conv descriptor");
+  if (d->D < 1 || d->H < 1 || d->W < 1) TLGB_FAIL(TLGB_ERR_INVALID, "conv3d: spatial sizes must be >= 1");
+  if (d->H > 65535 || d->D > 65535) TLGB_FAIL(TLGB_ERR_UNSUPPORTED, "conv3d: D and H must be <= 65535");
+  if (d->cin != 16 || d->cout != 16) TLGB_FAIL(TLGB_ERR_UNSUPPORTED, "conv3d: 16 input and 16 output channels (pad)");
+  if (d->mode < 0 || d->mode > 2) TLGB_FAIL(TLGB_ERR_INVALID, "conv3d: unknown epilogue mode");
+  return TLGB_OK;
+}
+
+int wgrad_parts(const tlgb_conv3d_desc* d) {
+  const long long rows = (long long)d->D * d->H * ((d->W + kTileW - 1) / kTileW);
+  return (int)std::min<long long>(rows, 4 * 152);
+}
+
+}  // namespace
+}  // namespace tlgb
+
+using namespace tlgb;
+
+extern "C" int tlgb_conv3d_fwd(const tlgb_conv3d_desc* d, const void* x, const void* w, const void* aux, void* y,
+                               tlgb_stream_t stream) {
+  TLGB_TRY(check_conv(d));
+  if (!x || !w || !y || (d->mode == 2 && !aux)) TLGB_FAIL(TLGB_ERR_INVALID, "null pointer");
+  if (((uintptr_t)x | (uintptr_t)w | (uintptr_t)y | (uintptr_t)aux) & 15)
+    TLGB_FAIL(TLGB_ERR_INVALID, "conv3d: buffers must be 16-byte aligned");
+  cudaStream_t s = (cudaStream_t)stream;
+  dim3 grid((unsigned)((d->W + kTileW - 1) / kTileW), (unsigned)d->H, (unsigned)d->D);
+  const uint4* xp = (const uint4*)x;
+  const uint4* wp = (const uint4*)w;
+  const __nv_bfloat16* ap = (const __nv_bfloat16*)aux;
+#define TLGB_CONV_LAUNCH(M, F) conv3d_fwd_kernel<M, F><<<grid, 128, 0, s>>>(d->D, d->H, d->W, xp, wp, ap, y)
+  if (d->out_f32) {
+    if (d->mode == 0) TLGB_CONV_LAUNCH(0, true);
+    else if (d->mode == 1) TLGB_CONV_LAUNCH(1, true);
+    else TLGB_CONV_LAUNCH(2, true);
+  } else {
+    if (d->mode == 0) TLGB_CONV_LAUNCH(0, false);
+    else if (d->mode == 1) TLGB_CONV_LAUNCH(1, false);
+    else TLGB_CONV_LAUNCH(2, false);
+  }
+#undef TLGB_CONV_LAUNCH
+  TLGB_CHECK_LAUNCH();
+  return TLGB_OK;
+}
+
+extern "C" int tlgb_conv3d_wgrad_scratch_size(const tlgb_conv3d_desc* d, size_t* bytes) {
+  TLGB_TRY(check_conv(d));
+  if (!bytes) TLGB_FAIL(TLGB_ERR_INVALID, "null pointer");
+  *bytes = (size_t)wgrad_parts(d) * kTaps * 256 * sizeof(float);
+  return TLGB_OK;
+}
+
+extern "C" int tlgb_conv3d_wgrad(const tlgb_conv3d_desc* d, const void* x, const void* gy, float* dw, void* scratch,
+                                 size_t scratch_bytes, tlgb_stream_t stream) {
+  TLGB_TRY(check_conv(d));
+  if (!x || !gy || !dw || !scratch) TLGB_FAIL(TLGB_ERR_INVALID, "null pointer");
+  if (((uintptr_t)x | (uintptr_t)gy | (uintptr_t)scratch) & 15)
+    TLGB_FAIL(TLGB_ERR_INVALID, "conv3d: buffers must be 16-byte aligned");
+  size_t need = 0;
+  TLGB_TRY(tlgb_conv3d_wgrad_scratch_size(d, &need));
+  if (scratch_bytes < need) TLGB_FAIL(TLGB_ERR_WORKSPACE, "conv3d wgrad scratch too small");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int parts = wgrad_parts(d);
+  conv3d_wgrad_kernel<<<parts, 128, 0, s>>>(d->D, d->H, d->W, (const uint4*)x, (const uint4*)gy, (float*)scratch);
+  TLGB_CHECK_LAUNCH();
+  wgrad_reduce_kernel<<<(kTaps * 256 + 255) / 256, 256, 0, s>>>((const float*)scratch, parts, dw);
+  TLGB_CHECK_LAUNCH();
+  return TLGB_OK;
+}
+
+extern "C" int tlgb_conv3d_pack(const void* z, int64_t nvox, const float* scale, int32_t hilo, void* out,
+                                tlgb_stream_t stream) {
+  if (nvox < 0 || (nvox > 0 && (!z || !out))) TLGB_FAIL(TLGB_ERR_INVALID, "null pointer or negative size");
+  if (nvox == 0) return TLGB_OK;
+  if ((uintptr_t)out & 15) TLGB_FAIL(TLGB_ERR_INVALID, "pack: output must be 16-byte aligned");
+  pack_c64_kernel<<<(unsigned)cdiv(nvox, 256), 256, 0, (cudaStream_t)stream>>>((const float2*)z, nvox, scale, hilo,
+                                                                               (uint4*)out);
+  TLGB_CHECK_LAUNCH();
+  return TLGB_OK;
+}
+
+extern "C" int tlgb_conv3d_unpack(const float* y, const void* z, int64_t nvox, const float* scale, float skip,
+                                  void* out, tlgb_stream_t stream) {
+  if (nvox < 0 || (nvox > 0 && (!y || !out))) TLGB_FAIL(TLGB_ERR_INVALID, "null pointer or negative size");
+  if (nvox == 0) return TLGB_OK;
+  unpack_c64_kernel<<<(unsigned)cdiv(nvox, 256), 256, 0, (cudaStream_t)stream>>>(y, (const float2*)z, nvox, scale,
+                                                                                 skip, (float2*)out);
+  TLGB_CHECK_LAUNCH();
+  return TLGB_OK;
+}

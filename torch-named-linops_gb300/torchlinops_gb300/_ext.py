@@ -78,6 +78,19 @@ class BlocksDesc(ctypes.Structure):
     ]
 
 
+class ConvDesc(ctypes.Structure):
+    _fields_ = [
+        ("D", ctypes.c_int32),
+        ("H", ctypes.c_int32),
+        ("W", ctypes.c_int32),
+        ("cin", ctypes.c_int32),
+        ("cout", ctypes.c_int32),
+        ("mode", ctypes.c_int32),
+        ("out_f32", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+    ]
+
+
 _P = ctypes.c_void_p
 _SIGNATURES = {
     "tlgb_last_error": ([], ctypes.c_char_p),
@@ -96,7 +109,15 @@ _SIGNATURES = {
     "tlgb_dot_f64": ([_P, _P, ctypes.c_int64, ctypes.c_int, _P, _P, ctypes.c_size_t, _P], ctypes.c_int),
     "tlgb_cg_set_pap": ([_P, _P, ctypes.c_int64, ctypes.c_int, _P, _P, ctypes.c_size_t, _P], ctypes.c_int),
     "tlgb_cg_step": ([_P, _P, _P, _P, ctypes.c_int64, ctypes.c_int, _P, _P, ctypes.c_size_t, _P], ctypes.c_int),
+    "tlgb_conv3d_fwd": ([_P, _P, _P, _P, _P, _P], ctypes.c_int),
+    "tlgb_conv3d_wgrad_scratch_size": ([_P, ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
+    "tlgb_conv3d_wgrad": ([_P, _P, _P, _P, _P, ctypes.c_size_t, _P], ctypes.c_int),
+    "tlgb_conv3d_pack": ([_P, ctypes.c_int64, _P, ctypes.c_int32, _P, _P], ctypes.c_int),
+    "tlgb_conv3d_unpack": ([_P, _P, ctypes.c_int64, _P, ctypes.c_float, _P, _P], ctypes.c_int),
 }
+
+# conv3d epilogue modes (include/tlgb.h)
+TLGB_CONV_PLAIN, TLGB_CONV_RELU, TLGB_CONV_MASK = 0, 1, 2
 
 # float64 CG state vector slots (include/tlgb.h)
 CG_RS, CG_RS_OLD, CG_PAP, CG_ALPHA, CG_BETA, CG_ITERS, CG_TMP, CG_STATE_LEN = 0, 1, 2, 3, 4, 5, 6, 8
@@ -106,7 +127,7 @@ _lock = threading.Lock()
 
 
 def lib_path() -> str:
-    return os.environ.get("TLGB_LIBRARY", LIB_PATH)
+    return os.environ.get("TLGB_LIBRARY") or LIB_PATH
 
 
 def lib() -> ctypes.CDLL:
