@@ -348,6 +348,9 @@ def run_gpu(args, world, rank, local):
         cpu = None
         if world == 1 and not args.skip_cpu:
             cpu = cpu_baseline(args.ref_sample)
+        cg = None
+        if world == 1 and not args.skip_cg:
+            cg = bench_cg(dev, args)
         line = {
             "metric": "3D multicoil gridding+ungridding throughput (256^3 x 8 coils, 2^21 points, KB W=4)",
             "value": value,
@@ -394,6 +397,7 @@ def run_gpu(args, world, rank, local):
             "clocks": clocks,
             "gpu_launches": launches_per_step * args.steps,
             "kernels": kernels,
+            "cg": cg,
         }
         print(json.dumps(line), flush=True)
     return line
@@ -434,6 +438,65 @@ def bench_blocks(dev, peak, args):
     }
 
 
+def bench_cg(dev, args):
+    """Learned-preconditioned vs plain CG to relative residual 1e-4 on 3D
+    SENSE: 128^3 image, 8 Gaussian coil maps, 3D radial 2048 spokes x 512
+    readouts (2^20 points), lam = 1e-3, A normalised by the power method.
+    Wall time of each solve (float64 true residual included); the
+    preconditioner is trained here first, on the GPU, by the package's own
+    convolution kernels (its time is reported separately)."""
+    from torchlinops_gb300 import alg, mri, precond
+
+    n, ncoil, nspokes, nread, lam = 128, 8, 2048, 512, 1e-3
+    locs = mri.radial_trajectory_3d(nspokes, nread, n, dev)
+    maps = mri.gaussian_coil_maps_3d(ncoil, n, device=dev)
+    A = mri.SenseNormal(locs, maps, lam=lam)
+    xt = mri.ellipsoid_phantom_3d(n, 10, torch.Generator().manual_seed(1234), dev)
+    b = A(xt)
+
+    def timed(fn, reps=5):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / reps * 1e3
+
+    def solve(M):
+        alg.cg_solve(A, b, rtol=1e-4, max_iters=500, M=M)  # warm-up
+        runs = [alg.cg_solve(A, b, rtol=1e-4, max_iters=500, M=M)[1] for _ in range(3)]
+        best = min(runs, key=lambda i: i.seconds)
+        return {"iters": best.iters, "seconds": best.seconds, "converged": best.converged,
+                "true_rel_residual": best.true_rel_residual, "fallback": best.fallback}
+
+    normal_ms = timed(lambda: A(b))
+    plain = solve(None)
+    M = precond.CNNPreconditioner(dev, seed=1, init="laplacian", c0=0.02)
+    warm = solve(M)
+    gen = torch.Generator().manual_seed(0)
+    batch = 4
+    log = M.fit(lambda step: mri.training_batch(A, n, gen, batch, dev), args.cg_steps, lr=1e-3,
+                log_every=max(args.cg_steps // 10, 1))
+    learned = solve(M)
+    m_ms = timed(lambda: M(b))
+    return {
+        "workload": f"sense3d_{n}cube_{ncoil}coil_{nspokes}x{nread}radial_lam{lam:g}",
+        "rtol": 1e-4,
+        "normal_op_ms": normal_ms,
+        "preconditioner_ms": m_ms,
+        "plain": plain,
+        "warm_start": warm,
+        "learned": learned,
+        "speedup_wall": plain["seconds"] / learned["seconds"],
+        "speedup_iters": plain["iters"] / learned["iters"],
+        "train": {"steps": args.cg_steps, "samples": args.cg_steps * batch, "seconds": log.seconds,
+                  "loss_first": log.losses[0][1] if log.losses else None,
+                  "loss_last": log.losses[-1][1] if log.losses else None},
+        "data": "synthetic: ellipsoid phantom, Gaussian coil maps, Fibonacci-sphere radial trajectory, seeded",
+    }
+
+
 def _resize(grid: int, points: int) -> None:
     global N_GRID, N_PTS, ALGO_BYTES
     N_GRID, N_PTS = grid, points
@@ -449,6 +512,8 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=1 << 16, help="points in the CPU baseline sample")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-blocks", action="store_true")
+    ap.add_argument("--skip-cg", action="store_true", help="skip the learned vs plain CG comparison")
+    ap.add_argument("--cg-steps", type=int, default=300, help="preconditioner training steps (4 samples each)")
     ap.add_argument("--grid", type=int, default=N_GRID, help="grid edge (smaller cases for profiling)")
     ap.add_argument("--points", type=int, default=N_PTS, help="number of points (smaller cases for profiling)")
     args = ap.parse_args()
