@@ -106,7 +106,10 @@ int tlgb_interp_plan_size(const tlgb_interp_desc* d, size_t* plan_bytes, size_t*
 int tlgb_interp_plan_build(const tlgb_interp_desc* d, const float* locs, void* plan, size_t plan_bytes,
                            void* tmp, size_t tmp_bytes, tlgb_interp_plan_info* info, tlgb_stream_t stream);
 
-/* Scratch bytes tlgb_interp_adjoint needs for the partial tiles of this plan. */
+/* Scratch bytes tlgb_interp_adjoint needs for this plan: the partial tiles of
+ * split output tiles and, for 3D gridding of 8-entry groups, a point-major
+ * copy of the point values (64 bytes per point and group of 8 entries), so
+ * that each (point, tile) pair reads its values in one contiguous run. */
 int tlgb_interp_adjoint_scratch_size(const tlgb_interp_desc* d, const tlgb_interp_plan_info* info,
                                      size_t* bytes);
 
@@ -132,9 +135,10 @@ int tlgb_interp_adjoint(const tlgb_interp_desc* d, const tlgb_interp_plan_info* 
  * TLGB_ADJOINT_FIXED_SCRATCH_BYTES bytes that the library holds on every GPU
  * it is loaded on until the process exits. The caller still provides the
  * plan, the inputs and the output.
- *  - A plan whose partial tiles need more than the buffer (see
- *    tlgb_interp_adjoint_scratch_size) is rejected with TLGB_ERR_WORKSPACE
- *    before anything is launched.
+ *  - A plan whose partial tiles alone need more than the buffer is rejected
+ *    with TLGB_ERR_WORKSPACE before anything is launched. The point-major
+ *    copy of the values is made only when it fits beside them; otherwise
+ *    the values are read in place (same result, bit for bit).
  *  - The first call on a device looks up the buffer's device address (with
  *    that device current) and remembers it; make that first call before any
  *    stream capture.

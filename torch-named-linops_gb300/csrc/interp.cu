@@ -66,6 +66,7 @@ struct Geo {
   float beta;
   long long npts, nbatch;
   int wrap_safe;  // every active N >= NT: a window never overlaps itself
+  long long tv_off;  // gridding: byte offset in scratch of the point-major values, -1 = none
 };
 
 // ---------------------------------------------------------------- kernels math
@@ -1084,6 +1085,28 @@ __device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, u
 // device status word: set when a bounded wait gave up (see tlgb_interp_forward)
 __device__ int g_tlgb_status;
 
+// Point values [batch][npts] (complex) -> point-major [group][npts][8]: the
+// gridding reads 64 contiguous bytes per (point, tile) pair instead of 8
+// scattered 8-byte values. CTA = 32 points x 8 entries of one group.
+__global__ void __launch_bounds__(256) transpose_vals_kernel(const float2* __restrict__ vals, long long npts,
+                                                             long long nbatch, float2* __restrict__ tv) {
+  __shared__ float2 sm[32][9];
+  const int grp = blockIdx.y;
+  const long long p0 = (long long)blockIdx.x * 32;
+  const int t = threadIdx.x;
+  {
+    const int c = t >> 5, i = t & 31;
+    const long long p = p0 + i, cc = (long long)grp * 8 + c;
+    sm[i][c] = (p < npts && cc < nbatch) ? __ldg(vals + cc * npts + p) : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  {
+    const int i = t >> 3, c = t & 7;
+    const long long p = p0 + i;
+    if (p < npts) tv[((long long)grp * npts + p) * 8 + c] = sm[i][c];
+  }
+}
+
 // Gridding: CTA = 8 warps owning one 8^3 x 8-entry output tile
 // ([x][y][z][entry], 16 floats per cell); warp w owns the cells of x-plane w,
 // so no two warps write the same cell. Entries are staged in batches of kAB
@@ -1096,7 +1119,8 @@ constexpr int kAB = 128;
 __global__ void __launch_bounds__(256, 4) adj_f3_kernel(Geo g, const int4* __restrict__ items,
                                                         const int32_t* __restrict__ entries,
                                                         const float* __restrict__ locs, const float* __restrict__ vals,
-                                                        float* __restrict__ gridv, float* __restrict__ partial) {
+                                                        const float4* __restrict__ tv, float* __restrict__ gridv,
+                                                        float* __restrict__ partial) {
   constexpr int CG = 8, VS = 16, TFL = 512 * 16, NW = 8, MW = kAB / 32;
   extern __shared__ __align__(128) unsigned char smem[];
   float* acc = reinterpret_cast<float*>(smem);                   // [8][8][8][16]
@@ -1148,6 +1172,12 @@ __global__ void __launch_bounds__(256, 4) adj_f3_kernel(Geo g, const int4* __res
       const long long p = entries[b + j];
       const int h = tid & 1;
       float4* d = reinterpret_cast<float4*>(pv + j * VS) + 2 * h;
+      if (tv) {
+        const float4* src = tv + ((long long)cg * g.npts + p) * 4 + 2 * h;
+        d[0] = __ldg(src);
+        d[1] = __ldg(src + 1);
+        continue;
+      }
 #pragma unroll
       for (int q = 0; q < 2; ++q) {
         const int c = 4 * h + 2 * q;
@@ -1630,6 +1660,7 @@ int make_geo(const tlgb_interp_desc* d, Geo& g) {
   const int T3[3] = {8, 8, 8}, T2[3] = {1, 32, 32}, T1[3] = {1, 1, 512};
   const int* T = d->ndim == 3 ? T3 : (d->ndim == 2 ? T2 : T1);
   g.wrap_safe = 1;
+  g.tv_off = -1;
   for (int e = 0; e < 3; ++e) {
     g.T[e] = std::min(T[e], g.N[e]);
     g.nt[e] = (int)cdiv(g.N[e], g.T[e]);
@@ -1872,14 +1903,29 @@ extern "C" int tlgb_interp_plan_build(const tlgb_interp_desc* d, const float* lo
   return TLGB_OK;
 }
 
+namespace tlgb {
+namespace {
+bool fast3(const Geo& g, int cg);
+
+// Gridding scratch: the partial tiles of split tiles, then (3D 8-entry path
+// only) the point values transposed to point-major order.
+void adj_scratch_parts(const Geo& g, const tlgb_interp_plan_info* info, size_t& partial_bytes, size_t& tv_bytes) {
+  const int cg = adj_cg(g);
+  const int64_t ncg = cdiv(std::max<long long>(g.nbatch, 1), cg);
+  partial_bytes = align_up((size_t)info->n_partials * ncg * tile_floats(g, cg) * sizeof(float), 256);
+  tv_bytes = fast3(g, cg) ? (size_t)ncg * g.npts * 8 * 8 : 0;
+}
+}  // namespace
+}  // namespace tlgb
+
 extern "C" int tlgb_interp_adjoint_scratch_size(const tlgb_interp_desc* d, const tlgb_interp_plan_info* info,
                                                 size_t* bytes) {
   Geo g;
   TLGB_TRY(make_geo(d, g));
   if (!info || !bytes) TLGB_FAIL(TLGB_ERR_INVALID, "null pointer");
-  const int cg = adj_cg(g);
-  const int64_t ncg = cdiv(std::max<long long>(g.nbatch, 1), cg);
-  *bytes = (size_t)info->n_partials * ncg * tile_floats(g, cg) * sizeof(float);
+  size_t pb = 0, tb = 0;
+  adj_scratch_parts(g, info, pb, tb);
+  *bytes = pb + tb;
   return TLGB_OK;
 }
 
@@ -1974,9 +2020,17 @@ int launch_adj_f3(const Geo& g, const tlgb_interp_plan_info* info, const char* P
   const size_t sm = 512 * 16 * sizeof(float) + kAB * (sizeof(R3) + 16 * sizeof(float)) + 8 * sizeof(Rec<5>) +
                     8 * (kAB / 32) * sizeof(unsigned);
   TLGB_TRY(set_smem(adj_f3_kernel, sm));
+  const float4* tv = nullptr;
+  if (g.tv_off >= 0 && g.npts > 0) {
+    float2* t = reinterpret_cast<float2*>(static_cast<char*>(scratch) + g.tv_off);
+    dim3 gt((unsigned)cdiv(g.npts, 32), (unsigned)ncg);
+    transpose_vals_kernel<<<gt, 256, 0, s>>>((const float2*)vals, g.npts, g.nbatch, t);
+    TLGB_CHECK_LAUNCH();
+    tv = reinterpret_cast<const float4*>(t);
+  }
   dim3 grd((unsigned)info->n_adj_items, (unsigned)ncg);
   adj_f3_kernel<<<grd, 256, sm, s>>>(g, (const int4*)(P + info->off_adj_items), (const int32_t*)(P + info->off_entries),
-                                    locs, (const float*)vals, (float*)grid, (float*)scratch);
+                                    locs, (const float*)vals, tv, (float*)grid, (float*)scratch);
   TLGB_CHECK_LAUNCH();
   if (info->n_split_tiles > 0) {
     dim3 g2((unsigned)info->n_split_tiles, (unsigned)ncg);
@@ -2084,9 +2138,10 @@ extern "C" int tlgb_interp_adjoint(const tlgb_interp_desc* d, const tlgb_interp_
   TLGB_TRY(check_plan(g, info, plan));
   if (g.nbatch == 0) return TLGB_OK;
   if (!grid || (g.npts > 0 && (!locs || !vals))) TLGB_FAIL(TLGB_ERR_INVALID, "null pointer");
-  size_t need = 0;
-  TLGB_TRY(tlgb_interp_adjoint_scratch_size(d, info, &need));
-  if (scratch_bytes < need || (need > 0 && !scratch)) TLGB_FAIL(TLGB_ERR_WORKSPACE, "adjoint scratch too small");
+  size_t pb = 0, tb = 0;
+  adj_scratch_parts(g, info, pb, tb);
+  if (scratch_bytes < pb + tb || (pb + tb > 0 && !scratch)) TLGB_FAIL(TLGB_ERR_WORKSPACE, "adjoint scratch too small");
+  g.tv_off = tb > 0 ? (long long)pb : -1;
   cudaStream_t s = (cudaStream_t)stream;
   const char* P = (const char*)plan;
   return launch_adj(g, info, P, locs, vals, grid, scratch, s);
@@ -2166,16 +2221,18 @@ extern "C" int tlgb_interp_adjoint_fixed(const tlgb_interp_desc* d, const tlgb_i
   TLGB_TRY(check_plan(g, info, plan));
   if (g.nbatch == 0) return TLGB_OK;
   if (!grid || (g.npts > 0 && (!locs || !vals))) TLGB_FAIL(TLGB_ERR_INVALID, "null pointer");
-  size_t need = 0;
-  TLGB_TRY(tlgb_interp_adjoint_scratch_size(d, info, &need));
+  size_t need = 0, tb = 0;
+  adj_scratch_parts(g, info, need, tb);
   if (need > kFixedScratchBytes)
     TLGB_FAIL(TLGB_ERR_WORKSPACE, "this plan needs " + std::to_string(need) +
                                       " bytes of partial-tile scratch, more than the fixed " +
                                       std::to_string(kFixedScratchBytes) +
                                       "-byte device buffer of tlgb_interp_adjoint_fixed; use "
                                       "tlgb_interp_adjoint with caller scratch");
+  // the point-major copy of the values is used only when it fits as well
+  g.tv_off = (tb > 0 && need + tb <= kFixedScratchBytes) ? (long long)need : -1;
   void* scratch = nullptr;
-  if (need > 0) TLGB_TRY(fixed_scratch_address(&scratch));
+  if (need + (g.tv_off >= 0 ? tb : 0) > 0) TLGB_TRY(fixed_scratch_address(&scratch));
   return launch_adj(g, info, (const char*)plan, locs, vals, grid, scratch, (cudaStream_t)stream);
 }
 
