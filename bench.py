@@ -261,7 +261,7 @@ def run_gpu(args, world, rank, local):
     # plan (one-time per trajectory), timed separately
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    plan = get_plan(locs, (N_GRID,) * 3, WIDTH, "kaiser_bessel", "circular")
+    plan = get_plan(locs, (N_GRID,) * 3, WIDTH, "kaiser_bessel", "circular", beta)
     torch.cuda.synchronize()
     plan_ms = (time.perf_counter() - t0) * 1e3
     launches_per_step = 2 + (1 if plan.info.n_split_tiles > 0 else 0)

@@ -93,7 +93,10 @@ typedef struct tlgb_interp_plan_info {
   int64_t off_adj_items;
   int64_t off_split;
   int64_t plan_bytes;
-  int64_t reserved[4];
+  int64_t n_home;         /* points with at least one valid tap (home pairs) */
+  int64_t off_records;    /* byte offset of the per-point tap records, 0 = none */
+  int64_t kernel_key;     /* kernel, norm and beta the records were built for */
+  int64_t reserved;
 } tlgb_interp_plan_info;
 
 /* Bytes of device memory needed by a plan for this description (worst case)

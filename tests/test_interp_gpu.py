@@ -278,3 +278,29 @@ def test_plan_cache_follows_inplace_edits():
     b = T.ungrid(img, locs, 4.0)
     ref = OI.ungrid(img.cpu(), locs.cpu(), 4.0)
     assert rel_l2(b.cpu(), ref) < TOL and not torch.allclose(a, b)
+
+
+def test_plan_records_are_tied_to_the_kernel_parameters():
+    """3D plans store each point's tap weights, so a plan is valid for the
+    kernel, norm and beta it was built with; the C ABI rejects another beta."""
+    import ctypes
+
+    from torchlinops_gb300 import _ext, interp
+
+    gen = torch.Generator().manual_seed(12)
+    locs = (torch.rand(5000, 3, generator=gen) * 32).to(DEV)
+    img = torch.randn(8, 32, 32, 32, dtype=torch.complex64, generator=gen).to(DEV)
+    b1, b2 = 6.99666, 5.0
+    plan = interp.get_plan(locs, (32, 32, 32), 4.0, "kaiser_bessel", "circular", b1)
+    assert plan.info.off_records > 0
+    d = interp._desc(3, (32, 32, 32), (4.0,) * 3, "kaiser_bessel", 1, "circular", b2, True, 8, 5000)
+    out = torch.empty(8, 5000, dtype=torch.complex64, device=DEV)
+    st = _ext.lib().tlgb_interp_forward(ctypes.byref(d), ctypes.byref(plan.info), _ext.ptr(plan.buffer),
+                                         _ext.ptr(locs), _ext.ptr(torch.view_as_real(img)),
+                                         _ext.ptr(torch.view_as_real(out)), _ext.stream_ptr(locs.device))
+    assert st == _ext.TLGB_ERR_INVALID and b"beta" in _ext.lib().tlgb_last_error()
+    # the Python layer keys its plan cache by beta, so both betas just work
+    y1 = T.ungrid(img, locs, 4.0, kernel_params=dict(beta=b1)).cpu()
+    y2 = T.ungrid(img, locs, 4.0, kernel_params=dict(beta=b2)).cpu()
+    assert rel_l2(y2, OI.ungrid(img.cpu(), locs.cpu(), 4.0, beta=b2)) < TOL
+    assert rel_l2(y1, OI.ungrid(img.cpu(), locs.cpu(), 4.0, beta=b1)) < TOL

@@ -48,7 +48,7 @@ def test_fixed_scratch_gridding_matches_caller_scratch_gridding():
     n, locs, vals = _dense_case()
     beta = T.kaiser_bessel_beta(4.0, 1.25)
     ref = T.grid(vals, locs, (n, n, n), 4.0, kernel_params=dict(beta=beta))
-    plan = interp.get_plan(locs, (n, n, n), 4.0, "kaiser_bessel", "circular")
+    plan = interp.get_plan(locs, (n, n, n), 4.0, "kaiser_bessel", "circular", beta)
     assert plan.info.n_partials > 0, "the case must exercise the partial-tile scratch"
     desc = interp._desc(3, (n, n, n), (4.0,) * 3, "kaiser_bessel", 1, "circular", beta, True, vals.shape[0],
                         vals.shape[1])

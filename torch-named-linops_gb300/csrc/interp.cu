@@ -912,135 +912,138 @@ __device__ __forceinline__ float kb_approx(float ax, float beta) {
   return __expf(z) * rsqrtf(z) * q;
 }
 
-// Packed tap record of one (point, tile) entry for the 3D 8-entry kernels,
-// built one dimension per thread. Per dimension: the weights of the kept taps
-// (zero beyond the count) and an info word first | count << 4 | ok << 8 |
-// fast << 9, with first the local position of the first kept tap (in the
-// 12^3 gather region, or in the 8^3 tile for gridding), ok = a finite
-// coordinate with at least one kept tap, fast = at most 4 kept taps at
-// consecutive local positions.
+// A staged entry of the 3D 8-entry kernels in shared memory: the point's
+// weights, its view word (grid_view or region_view) and the point index.
 struct __align__(16) R3 {
   float4 w[3];
-  int info[3];
+  unsigned view;
+  int pad0, pad1;
   int p;  // point index
 };
 
-// The constants of one dimension, selected by a runtime index (keeps a
-// per-thread dimension out of local memory).
-struct Axis {
-  int N;
-  float r, rinv;
-  int rpow2;
+// Per-point tap record, built with the plan for 3D geometries with 8^3 tiles
+// and at most 5 taps per dimension: the kernel weights of the first 4 valid
+// taps of each dimension (zero beyond), the position of the first valid tap
+// (wrapped into [0, N) in circular mode) and the number of valid taps per
+// dimension (cnt_x | cnt_y << 4 | cnt_z << 8; a zero count marks a point
+// without taps). Valid taps form one run of tap indices: |x - g| <= W/2 is
+// an interval, and so is [0, N) for zero padding.
+struct __align__(16) PRec {
+  float4 w[3];
+  int st[3];
+  int cnt;
 };
+static_assert(sizeof(PRec) == 64, "64-byte point records");
 
-__device__ __forceinline__ Axis axis_of(const Geo& g, int e) {
-  Axis a;
-  a.N = e == 0 ? g.N[0] : (e == 1 ? g.N[1] : g.N[2]);
-  a.r = e == 0 ? g.r[0] : (e == 1 ? g.r[1] : g.r[2]);
-  a.rinv = e == 0 ? g.rinv[0] : (e == 1 ? g.rinv[1] : g.rinv[2]);
-  a.rpow2 = e == 0 ? g.rpow2[0] : (e == 1 ? g.rpow2[1] : g.rpow2[2]);
-  return a;
-}
-
-// tap_eval for one dimension given by its constants (same operations)
-__device__ __forceinline__ Tap tap_eval_ax(const Geo& g, const Axis& a, float x, int lower, int k) {
-  Tap t;
-  const float gk = (float)(lower + k);
-  const float diff = __fsub_rn(x, gk);
-  t.d = a.rpow2 ? __fmul_rn(diff, a.rinv) : __fdiv_rn(diff, a.r);
-  const float ad = fabsf(t.d);
-  bool v = ad <= a.r;
-  if (g.kernel == TLGB_KERNEL_KAISER_BESSEL) v = v && (ad <= 1.0f);
-  if (g.pad == TLGB_PAD_ZERO) v = v && (lower + k >= 0) && (lower + k < a.N);
-  t.valid = v;
-  return t;
-}
-
-// One dimension of a record (5 candidate taps). REGION: gather mode, the
-// window is contiguous from its first valid tap (the region is staged with
-// wrap); otherwise gridding mode, only the taps inside the tile are kept.
-template <bool REGION>
-__device__ __forceinline__ int rec3_dim(const Geo& g, const Axis& a, float x, int oe, float4& w4) {
-  constexpr int SD = REGION ? 12 : 8;
-  float w0 = 0.f, w1 = 0.f, w2 = 0.f, w3 = 0.f;
-  int first = 0, c = 0;
-  bool fast = true;
-  if (coord_ok(x)) {
-    const int lower = (int)ceilf(__fsub_rn(x, a.r));
-    int s = -1, last = -100;
+__global__ void point_records_kernel(Geo g, const float* __restrict__ locs, PRec* __restrict__ out) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= g.npts) return;
+  PRec R;
+  int cnt = 0;
 #pragma unroll
-    for (int k = 0; k < 5; ++k) {
-      const Tap t = tap_eval_ax(g, a, x, lower, k);
-      if (t.valid) {
-        if (s < 0) s = k;
-        int l;
-        bool keep = true;
-        if (REGION) {
-          int st = lower + s;
-          if (g.pad == TLGB_PAD_CIRCULAR) st = wrapi(st, a.N);
-          l = st - oe + (k - s);
-        } else {
-          int gg = lower + k;
-          if (g.pad == TLGB_PAD_CIRCULAR) gg = wrapi(gg, a.N);
-          l = gg - oe;
-          keep = l >= 0 && l < SD;
-        }
-        if (keep) {
-          if (c == 0) first = l;
-          else if (l != last + 1) fast = false;
-          last = l;
+  for (int e = 0; e < 3; ++e) {
+    float w0 = 0.f, w1 = 0.f, w2 = 0.f, w3 = 0.f;
+    int c = 0, st = 0;
+    const float x = load_coord(g, locs, p, e);
+    if (coord_ok(x)) {
+      const int lower = lower_of(g, e, x);
+      int s = -1;
+#pragma unroll
+      for (int k = 0; k < 5; ++k) {
+        const Tap t = tap_eval(g, e, x, lower, k);
+        if (t.valid) {
+          if (s < 0) s = k;
           const float v = kern_value_approx(g.kernel, fabsf(t.d), g.beta);
           w0 = c == 0 ? v : w0;
           w1 = c == 1 ? v : w1;
           w2 = c == 2 ? v : w2;
           w3 = c == 3 ? v : w3;
-          if (c >= 4) fast = false;
           ++c;
         }
       }
+      if (c > 0) {
+        st = lower + s;
+        if (g.pad == TLGB_PAD_CIRCULAR) st = wrapi(st, g.N[e]);
+      }
     }
+    R.w[e] = make_float4(w0, w1, w2, w3);
+    R.st[e] = st;
+    cnt |= c << (4 * e);
   }
-  w4 = make_float4(w0, w1, w2, w3);
-  if (first < 0 || first >= SD) fast = false;  // never for plan entries; keeps the fast paths in bounds
-  return (first & 15) | (c << 4) | ((c > 0 ? 1 : 0) << 8) | ((fast ? 1 : 0) << 9);
+  R.cnt = cnt;
+  out[p] = R;
 }
 
-// Thread task (entry j, dimension d) of a record batch: d = task / span.
-template <bool REGION>
-__device__ __forceinline__ void rec3_task(const Geo& g, const float* __restrict__ locs,
-                                          const int32_t* __restrict__ entries, int b, int j, int d,
-                                          const int (&o)[3], R3* rec) {
-  const long long p = entries[b + j];
-  const float x = load_coord(g, locs, p, d);
-  const int oe = d == 0 ? o[0] : (d == 1 ? o[1] : o[2]);
-  float4 w4;
-  const int info = rec3_dim<REGION>(g, axis_of(g, d), x, oe, w4);
-  rec[j].w[d] = w4;
-  rec[j].info[d] = info;
-  if (d == 0) rec[j].p = (int)p;
+// View of one dimension of a record from the tile at o (8 wide, grid N):
+// f = first local position, m = taps inside the tile, k0 = index of the
+// first of them in the record; packed f | m << 3 | k0 << 6. fast is cleared
+// when the window has 5 taps or, in circular mode on a grid below 16, could
+// meet the tile twice.
+__device__ __forceinline__ int tile_view(int st, int c, int o, int N, bool circ, bool& fast) {
+  const int te = min(8, N - o);
+  int d = st - o;
+  if (circ && d < 0) d += N;
+  int f, k0, m;
+  if (d >= 0 && d < te) {
+    f = d;
+    k0 = 0;
+    m = min(c, te - d);
+  } else {
+    f = 0;
+    k0 = circ ? N - d : -d;  // the window enters from below (wrapping around in circular mode)
+    m = (d >= te && !circ) ? 0 : min(c - k0, te);
+  }
+  if (m < 0 || k0 < 0) m = 0, k0 = 0;
+  if (c > 4 || (circ && N < 16)) fast = false;
+  return f | (m << 3) | (min(k0, 7) << 6);
 }
 
-struct R3v {
-  int base, mx, my, mz, fx, fy, fz, p;
-  bool ok, fast;
-};
+// The gridding view of a point record in the tile at o, as one word: three
+// 9-bit tile views (x, y, z) | fast << 27 | ok << 28.
+__device__ __forceinline__ unsigned grid_view(const Geo& g, const PRec& R, const int (&o)[3]) {
+  bool fast = true;
+  const bool circ = g.pad == TLGB_PAD_CIRCULAR;
+  const int c = R.cnt;
+  const bool ok = (c & 15) && ((c >> 4) & 15) && ((c >> 8) & 15);
+  unsigned v = 0;
+#pragma unroll
+  for (int e = 0; e < 3; ++e) v |= (unsigned)tile_view(R.st[e], (c >> (4 * e)) & 15, o[e], g.N[e], circ, fast) << (9 * e);
+  return v | ((fast ? 1u : 0u) << 27) | ((ok ? 1u : 0u) << 28);
+}
 
-template <int SD>
-__device__ __forceinline__ R3v rec3_view(const R3& R) {
-  const int4 q = *reinterpret_cast<const int4*>(R.info);
-  R3v v;
-  const int all = q.x & q.y & q.z;
-  v.ok = (all >> 8) & 1;
-  v.fast = (all >> 9) & 1;
-  v.fx = q.x & 15;
-  v.fy = q.y & 15;
-  v.fz = q.z & 15;
-  v.mx = (q.x >> 4) & 15;
-  v.my = (q.y >> 4) & 15;
-  v.mz = (q.z >> 4) & 15;
-  v.base = (v.fx * SD + v.fy) * SD + v.fz;
-  v.p = q.w;
-  return v;
+// The gather view of a home record in the 12^3 region at o: region base
+// (11 bits) | mx << 11 | my << 14 | mz << 17 | fast << 20 | ok << 21. The
+// region is staged with wrap, so the window is always one run there.
+__device__ __forceinline__ unsigned region_view(const Geo& g, const PRec& R, const int (&o)[3]) {
+  const int c = R.cnt;
+  const int cx = c & 15, cy = (c >> 4) & 15, cz = (c >> 8) & 15;
+  const bool ok = cx && cy && cz;
+  int f[3];
+#pragma unroll
+  for (int e = 0; e < 3; ++e) {
+    int d = R.st[e] - o[e];
+    if (g.pad == TLGB_PAD_CIRCULAR && d < 0) d += g.N[e];
+    f[e] = d;
+  }
+  const bool fast = ok && cx <= 4 && cy <= 4 && cz <= 4 && f[0] >= 0 && f[0] < 8 && f[1] >= 0 && f[1] < 8 &&
+                    f[2] >= 0 && f[2] < 8;
+  const unsigned base = fast ? (unsigned)((f[0] * 12 + f[1]) * 12 + f[2]) : 0u;
+  return base | (min(cx, 7) << 11) | (min(cy, 7) << 14) | (min(cz, 7) << 17) | ((fast ? 1u : 0u) << 20) |
+         ((ok ? 1u : 0u) << 21);
+}
+
+__device__ __forceinline__ PRec load_prec(const PRec* __restrict__ recs, long long p) {
+  const float4* q = reinterpret_cast<const float4*>(recs + p);
+  PRec R;
+  R.w[0] = __ldg(q);
+  R.w[1] = __ldg(q + 1);
+  R.w[2] = __ldg(q + 2);
+  const int4 t = __ldg(reinterpret_cast<const int4*>(q + 3));
+  R.st[0] = t.x;
+  R.st[1] = t.y;
+  R.st[2] = t.z;
+  R.cnt = t.w;
+  return R;
 }
 
 __device__ __forceinline__ float pick4(const float4& v, int i) {
@@ -1118,6 +1121,7 @@ constexpr int kAB = 128;
 
 __global__ void __launch_bounds__(256, 4) adj_f3_kernel(Geo g, const int4* __restrict__ items,
                                                         const int32_t* __restrict__ entries,
+                                                        const PRec* __restrict__ precs,
                                                         const float* __restrict__ locs, const float* __restrict__ vals,
                                                         const float4* __restrict__ tv, float* __restrict__ gridv,
                                                         float* __restrict__ partial) {
@@ -1146,25 +1150,27 @@ __global__ void __launch_bounds__(256, 4) adj_f3_kernel(Geo g, const int4* __res
   for (int b = it.y; b < it.z; b += kAB) {
     const int nb = min(kAB, it.z - b);
     __syncthreads();  // the previous batch has been applied
-    // tasks: (entry j, dim d) for j < kAB, d < 3; warps 0..3 take dimension 0
-    for (int task = tid; task < 3 * kAB; task += 256) {
-      const int j = task % kAB, d = task / kAB;
-      int info = 0;
-      if (j < nb) {
-        rec3_task<false>(g, locs, entries, b, j, d, o, rec);
-        info = rec[j].info[d];
+    if (tid < kAB) {
+      // warps 0..3: entry tid's record and view, then per plane a ballot of
+      // the entries whose x taps reach it (all planes for the generic path)
+      unsigned view = 0;
+      if (tid < nb) {
+        const long long p = entries[b + tid];
+        const PRec R = load_prec(precs, p);
+        view = grid_view(g, R, o);
+        R3& S = rec[tid];
+        S.w[0] = R.w[0];
+        S.w[1] = R.w[1];
+        S.w[2] = R.w[2];
+        S.view = view;
+        S.p = (int)p;
       }
-      if (d == 0) {
-        // planes touched by the entry's x taps; all planes when the x window
-        // is not a plain run (the generic path checks each tap)
-        const bool okx = (info >> 8) & 1;
-        const bool fx = ((info >> 9) & 1) && g.wrap_safe;
-        const int f = info & 15, n = (info >> 4) & 15;
+      const bool okx = (view >> 28) & 1, fastx = (view >> 27) & 1;
+      const int f = view & 7, n = (view >> 3) & 7;
 #pragma unroll
-        for (int w = 0; w < NW; ++w) {
-          const unsigned bal = __ballot_sync(0xffffffffu, okx && (!fx || (w >= f && w < f + n)));
-          if (lane == 0) pmask[w * MW + (task >> 5)] = bal;
-        }
+      for (int w = 0; w < NW; ++w) {
+        const unsigned bal = __ballot_sync(0xffffffffu, okx && (!fastx || (w >= f && w < f + n)));
+        if (lane == 0) pmask[w * MW + (tid >> 5)] = bal;
       }
     }
     for (int j = tid >> 1; j < nb; j += 128) {
@@ -1198,36 +1204,40 @@ __global__ void __launch_bounds__(256, 4) adj_f3_kernel(Geo g, const int4* __res
         bits &= bits - 1;
         __syncwarp();  // consecutive entries may share cells of this plane
         const R3& R = rec[j];
-        const R3v V = rec3_view<8>(R);
-        if (!V.ok) continue;
-        if (V.fast && g.wrap_safe) {
-          const int t = warp - V.fx;  // in [0, mx) by the mask
-          if (ky < V.my) {
-            const float wxy = (&R.w[0].x)[t] * (&R.w[1].x)[ky];
+        const unsigned view = R.view;
+        if ((view >> 27) & 1) {
+          // plain runs: x taps k0x + t, y taps k0y + ky, z taps k0z + kz
+          const int t = warp - (int)(view & 7);  // in [0, mx) by the mask
+          const unsigned vy = (view >> 9) & 511, vz = (view >> 18) & 511;
+          const int fy = vy & 7, my = (vy >> 3) & 7, k0y = vy >> 6;
+          const int fz = vz & 7, mz = (vz >> 3) & 7, k0z = vz >> 6;
+          if (ky < my) {
+            const float wxy = (&R.w[0].x)[((view >> 6) & 7) + t] * (&R.w[1].x)[k0y + ky];
             const float4 v = *reinterpret_cast<const float4*>(pv + j * VS + cu * 4);
-            float* a = acc + ((V.base + t * 64 + ky * 8 + kzl) * VS) + cu * 4;
-            const bool z0 = kzl < V.mz, z1 = kzl + 2 < V.mz;
+            float* a = acc + (((warp * 8 + fy + ky) * 8 + fz + kzl) * VS) + cu * 4;
+            const bool z0 = kzl < mz, z1 = kzl + 2 < mz;
             float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = r0;
             if (z0) r0 = *reinterpret_cast<const float4*>(a);
             if (z1) r1 = *reinterpret_cast<const float4*>(a + 2 * VS);
             if (z0) {
-              const float w = wxy * (&R.w[2].x)[kzl];
+              const float w = wxy * (&R.w[2].x)[k0z + kzl];
               r0.x = fmaf(w, v.x, r0.x); r0.y = fmaf(w, v.y, r0.y); r0.z = fmaf(w, v.z, r0.z); r0.w = fmaf(w, v.w, r0.w);
               *reinterpret_cast<float4*>(a) = r0;
             }
             if (z1) {
-              const float w = wxy * (&R.w[2].x)[kzl + 2];
+              const float w = wxy * (&R.w[2].x)[k0z + kzl + 2];
               r1.x = fmaf(w, v.x, r1.x); r1.y = fmaf(w, v.y, r1.y); r1.z = fmaf(w, v.z, r1.z); r1.w = fmaf(w, v.w, r1.w);
               *reinterpret_cast<float4*>(a + 2 * VS) = r1;
             }
           }
           continue;
         }
+        if (!((view >> 28) & 1)) continue;  // no valid tap
         // exact-integer coordinates (5 taps) or a window wrapping inside the
         // tile: generic record, this plane's taps in order by 4 lanes
         if (lane == 0) {
           float x3[3];
-          for (int e = 0; e < 3; ++e) x3[e] = load_coord(g, locs, V.p, e);
+          for (int e = 0; e < 3; ++e) x3[e] = load_coord(g, locs, R.p, e);
           lane_rec<5>(g, x3, o, false, slow[warp]);
         }
         __syncwarp();
@@ -1287,6 +1297,7 @@ constexpr int kGB = 64;
 __global__ void __launch_bounds__(256, 2) fwd_f3_kernel(const __grid_constant__ CUtensorMap tmap, int use_tma, Geo g,
                                                         const int4* __restrict__ items,
                                                         const int32_t* __restrict__ entries,
+                                                        const PRec* __restrict__ precs,
                                                         const float* __restrict__ locs,
                                                         const float* __restrict__ gridv, float* __restrict__ out) {
   constexpr int CG = 8, S = 12, PLANE = S * S, VOL = S * S * S, NW = 8;
@@ -1345,9 +1356,17 @@ __global__ void __launch_bounds__(256, 2) fwd_f3_kernel(const __grid_constant__ 
   }
   const int kz = lane & 3, ky = (lane >> 2) & 3, ch = lane >> 4;
   auto build_records = [&](int b) {
-    // tasks (entry j, dim d): warps 2d, 2d + 1 take dimension d
-    const int j = tid & (kGB - 1), d = tid / kGB;
-    if (d < 3 && j < min(kGB, it.z - b)) rec3_task<true>(g, locs, entries, b, j, d, o, rec);
+    // warps 0, 1: entry tid's record and region view
+    if (tid < min(kGB, it.z - b)) {
+      const long long p = entries[b + tid];
+      const PRec R = load_prec(precs, p);
+      R3& S = rec[tid];
+      S.w[0] = R.w[0];
+      S.w[1] = R.w[1];
+      S.w[2] = R.w[2];
+      S.view = region_view(g, R, o);
+      S.p = (int)p;
+    }
   };
   build_records(it.y);  // while the region copy is in flight
   {
@@ -1368,18 +1387,19 @@ __global__ void __launch_bounds__(256, 2) fwd_f3_kernel(const __grid_constant__ 
     }
     for (int j = warp; j < nb; j += NW) {
       const R3& R = rec[j];
-      const R3v V = rec3_view<S>(R);
-      if (!V.ok) continue;  // warp-uniform
+      const unsigned view = R.view;
+      if (!((view >> 21) & 1)) continue;  // no valid tap (warp-uniform)
       float acc[8];
 #pragma unroll
       for (int i = 0; i < 8; ++i) acc[i] = 0.f;
-      if (V.fast) {
-        const float wyz = (ky < V.my && kz < V.mz) ? (&R.w[1].x)[ky] * (&R.w[2].x)[kz] : 0.f;
-        const float2* a = reg + ch * 4 * VOL + V.base + ky * S + kz;
+      if ((view >> 20) & 1) {
+        const int mx = (view >> 11) & 7, my = (view >> 14) & 7, mz = (view >> 17) & 7;
+        const float wyz = (ky < my && kz < mz) ? (&R.w[1].x)[ky] * (&R.w[2].x)[kz] : 0.f;
+        const float2* a = reg + ch * 4 * VOL + (view & 2047) + ky * S + kz;
         const float4 wx = R.w[0];
 #pragma unroll
         for (int kx = 0; kx < 4; ++kx) {
-          if (kx < V.mx) {
+          if (kx < mx) {
             const float w = (kx == 0 ? wx.x : kx == 1 ? wx.y : kx == 2 ? wx.z : wx.w) * wyz;
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
@@ -1393,7 +1413,7 @@ __global__ void __launch_bounds__(256, 2) fwd_f3_kernel(const __grid_constant__ 
         // exact-integer coordinates: generic record
         if (lane == 0) {
           float x3[3];
-          for (int e = 0; e < 3; ++e) x3[e] = load_coord(g, locs, V.p, e);
+          for (int e = 0; e < 3; ++e) x3[e] = load_coord(g, locs, R.p, e);
           lane_rec<5>(g, x3, o, true, slow[warp]);
         }
         __syncwarp();
@@ -1437,7 +1457,7 @@ __global__ void __launch_bounds__(256, 2) fwd_f3_kernel(const __grid_constant__ 
       const float im = __shfl_down_sync(0xffffffffu, s1, 2);
       const int c = c0 + ch * 4 + ((lane >> 2) & 3);
       if ((lane & 3) == 0 && c < g.nbatch)
-        *reinterpret_cast<float2*>(out + ((long long)c * g.npts + V.p) * 2) = make_float2(s1, im);
+        *reinterpret_cast<float2*>(out + ((long long)c * g.npts + R.p) * 2) = make_float2(s1, im);
     }
   }
 }
@@ -1609,7 +1629,7 @@ __global__ void __launch_bounds__(NTHR) interp_grad_kernel(Geo g, const int4* __
 
 struct PlanLayout {
   int64_t e_max, max_fwd, max_adj, ntiles;
-  int64_t off_entries, off_fwd, off_adj, off_split, bytes;
+  int64_t off_entries, off_fwd, off_adj, off_split, off_recs, bytes;
   // tmp
   int64_t t_cnt, t_keys, t_keys2, t_vals2, t_counts, t_hist, t_total, t_bytes;
 };
@@ -1686,6 +1706,19 @@ int64_t max_tiles_per_dim(const Geo& g, int e) {
   return 2;
 }
 
+// Geometries whose plan carries per-point tap records (the 3D 8-entry kernels)
+bool records_ok(const Geo& g) {
+  return g.ndim == 3 && g.norm == 1 && g.T[0] == 8 && g.T[1] == 8 && g.T[2] == 8 && g.NT[0] == 5 && g.NT[1] == 5 &&
+         g.NT[2] == 5;
+}
+
+// The kernel, norm and beta a plan's records hold weights for
+int64_t kernel_key(const Geo& g) {
+  uint32_t bits;
+  memcpy(&bits, &g.beta, 4);
+  return (int64_t)bits | ((int64_t)g.kernel << 32) | ((int64_t)g.norm << 40) | ((int64_t)1 << 48);
+}
+
 PlanLayout layout(const Geo& g) {
   PlanLayout L;
   L.e_max = g.npts * max_tiles_per_dim(g, 0) * max_tiles_per_dim(g, 1) * max_tiles_per_dim(g, 2);
@@ -1701,6 +1734,11 @@ PlanLayout layout(const Geo& g) {
   o = align_up(o + (size_t)L.max_adj * 16, 256);
   L.off_split = o;
   o = align_up(o + (size_t)(L.ntiles + 1) * 16, 256);
+  L.off_recs = 0;
+  if (records_ok(g) && g.npts > 0) {
+    L.off_recs = o;
+    o = align_up(o + (size_t)g.npts * 64, 256);
+  }
   L.bytes = o;
   size_t t = 0;
   L.t_cnt = t;
@@ -1778,6 +1816,8 @@ int check_plan(const Geo& g, const tlgb_interp_plan_info* info, const void* plan
   for (int e = 0; e < 3; ++e)
     if (info->tile[e] != g.T[e] || info->n_tile[e] != g.nt[e])
       TLGB_FAIL(TLGB_ERR_INVALID, "plan was built for another grid");
+  if (info->off_records > 0 && records_ok(g) && info->kernel_key != kernel_key(g))
+    TLGB_FAIL(TLGB_ERR_INVALID, "plan was built for another kernel, norm or beta (its tap weights are stored)");
   return TLGB_OK;
 }
 
@@ -1831,6 +1871,8 @@ extern "C" int tlgb_interp_plan_build(const tlgb_interp_desc* d, const float* lo
     TLGB_CHECK_LAUNCH();
     TLGB_TRY(exclusive_scan_u32(cnt, cnt, g.npts, total, s));
     plan_emit_kernel<<<nb, 256, 0, s>>>(g, locs, cnt, keys, entries);
+    TLGB_CHECK_LAUNCH();
+    if (L.off_recs > 0) point_records_kernel<<<nb, 256, 0, s>>>(g, locs, (PRec*)(P + L.off_recs));
     TLGB_CHECK_LAUNCH();
     TLGB_CUDA(cudaMemcpyAsync(&E, total, 4, cudaMemcpyDeviceToHost, s));
     TLGB_CUDA(cudaStreamSynchronize(s));
@@ -1899,7 +1941,9 @@ extern "C" int tlgb_interp_plan_build(const tlgb_interp_desc* d, const float* lo
   info->off_adj_items = L.off_adj;
   info->off_split = L.off_split;
   info->plan_bytes = L.bytes;
-  info->reserved[0] = n_home;
+  info->off_records = L.off_recs;
+  info->kernel_key = L.off_recs > 0 ? kernel_key(g) : 0;
+  info->n_home = n_home;
   return TLGB_OK;
 }
 
@@ -1913,7 +1957,7 @@ void adj_scratch_parts(const Geo& g, const tlgb_interp_plan_info* info, size_t& 
   const int cg = adj_cg(g);
   const int64_t ncg = cdiv(std::max<long long>(g.nbatch, 1), cg);
   partial_bytes = align_up((size_t)info->n_partials * ncg * tile_floats(g, cg) * sizeof(float), 256);
-  tv_bytes = fast3(g, cg) ? (size_t)ncg * g.npts * 8 * 8 : 0;
+  tv_bytes = (fast3(g, cg) && info->off_records > 0) ? (size_t)ncg * g.npts * 8 * 8 : 0;
 }
 }  // namespace
 }  // namespace tlgb
@@ -2009,7 +2053,8 @@ int launch_fwd_f3(const Geo& g, const tlgb_interp_plan_info* info, const char* P
   TLGB_TRY(set_smem(fwd_f3_kernel, sm));
   dim3 grd((unsigned)info->n_fwd_items, (unsigned)ncg);
   fwd_f3_kernel<<<grd, 256, sm, s>>>(tmap, use_tma, g, (const int4*)(P + info->off_fwd_items),
-                                     (const int32_t*)(P + info->off_entries), locs, (const float*)grid, (float*)out);
+                                     (const int32_t*)(P + info->off_entries), (const PRec*)(P + info->off_records), locs,
+                                     (const float*)grid, (float*)out);
   TLGB_CHECK_LAUNCH();
   return TLGB_OK;
 }
@@ -2030,7 +2075,8 @@ int launch_adj_f3(const Geo& g, const tlgb_interp_plan_info* info, const char* P
   }
   dim3 grd((unsigned)info->n_adj_items, (unsigned)ncg);
   adj_f3_kernel<<<grd, 256, sm, s>>>(g, (const int4*)(P + info->off_adj_items), (const int32_t*)(P + info->off_entries),
-                                    locs, (const float*)vals, tv, (float*)grid, (float*)scratch);
+                                    (const PRec*)(P + info->off_records), locs, (const float*)vals, tv, (float*)grid,
+                                    (float*)scratch);
   TLGB_CHECK_LAUNCH();
   if (info->n_split_tiles > 0) {
     dim3 g2((unsigned)info->n_split_tiles, (unsigned)ncg);
@@ -2045,7 +2091,7 @@ template <int N, int NDIM, int NTB>
 int launch_fwd_t(const Geo& g, int cg, const tlgb_interp_plan_info* info, const char* P, const float* locs,
                  const void* grid, void* out, cudaStream_t s) {
   if constexpr (N == 4 && NDIM == 3 && NTB == 5)
-    if (fast3(g, cg)) return launch_fwd_f3(g, info, P, locs, grid, out, s);
+    if (fast3(g, cg) && info->off_records > 0) return launch_fwd_f3(g, info, P, locs, grid, out, s);
   return launch_fwd_t2<N, NDIM, NTB, false>(g, cg, info, P, locs, grid, out, s);
 }
 
@@ -2053,7 +2099,7 @@ template <int N, int NDIM, int NTB>
 int launch_adj_t(const Geo& g, int cg, const tlgb_interp_plan_info* info, const char* P, const float* locs,
                  const void* vals, void* grid, void* scratch, cudaStream_t s) {
   if constexpr (N == 4 && NDIM == 3 && NTB == 5)
-    if (fast3(g, cg)) return launch_adj_f3(g, info, P, locs, vals, grid, scratch, s);
+    if (fast3(g, cg) && info->off_records > 0) return launch_adj_f3(g, info, P, locs, vals, grid, scratch, s);
   return launch_adj_t2<N, NDIM, NTB, false>(g, cg, info, P, locs, vals, grid, scratch, s);
 }
 
@@ -2123,7 +2169,7 @@ extern "C" int tlgb_interp_forward(const tlgb_interp_desc* d, const tlgb_interp_
   if (g.npts == 0 || g.nbatch == 0) return TLGB_OK;
   if (!locs || !grid || !out) TLGB_FAIL(TLGB_ERR_INVALID, "null pointer");
   cudaStream_t s = (cudaStream_t)stream;
-  if (info->reserved[0] < g.npts)  // points without a valid tap read as zero
+  if (info->n_home < g.npts)  // points without a valid tap read as zero
     TLGB_CUDA(cudaMemsetAsync(out, 0, (size_t)g.nbatch * g.npts * value_size(g), s));
   if (info->n_fwd_items == 0) return TLGB_OK;
   const char* P = (const char*)plan;
@@ -2156,7 +2202,7 @@ extern "C" int tlgb_interp_grad_locs(const tlgb_interp_desc* d, const tlgb_inter
   if (g.npts == 0) return TLGB_OK;
   if (!locs || !grid || !a || !grad_locs) TLGB_FAIL(TLGB_ERR_INVALID, "null pointer");
   cudaStream_t s = (cudaStream_t)stream;
-  if (info->reserved[0] < g.npts || g.nbatch == 0)
+  if (info->n_home < g.npts || g.nbatch == 0)
     TLGB_CUDA(cudaMemsetAsync(grad_locs, 0, (size_t)g.npts * g.ndim * sizeof(float), s));
   if (g.nbatch == 0 || info->n_fwd_items == 0) return TLGB_OK;
   const char* P = (const char*)plan;

@@ -60,7 +60,10 @@ class PlanInfo(ctypes.Structure):
         ("off_adj_items", ctypes.c_int64),
         ("off_split", ctypes.c_int64),
         ("plan_bytes", ctypes.c_int64),
-        ("reserved", ctypes.c_int64 * 4),
+        ("n_home", ctypes.c_int64),
+        ("off_records", ctypes.c_int64),
+        ("kernel_key", ctypes.c_int64),
+        ("reserved", ctypes.c_int64),
     ]
 
 

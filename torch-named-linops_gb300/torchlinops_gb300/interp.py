@@ -101,7 +101,7 @@ def _desc(ndim, grid_size, width, kernel, norm, pad_mode, beta, is_complex, nbat
 class InterpolatePlan:
     """Device-resident binning of one trajectory for one grid / kernel."""
 
-    def __init__(self, locs: Tensor, grid_size, width, kernel: str, pad_mode: str):
+    def __init__(self, locs: Tensor, grid_size, width, kernel: str, pad_mode: str, beta: float = 1.0, norm: int = 1):
         dev = _ext.check_cuda(locs)
         self.device = dev
         ndim = locs.shape[-1]
@@ -112,7 +112,9 @@ class InterpolatePlan:
         self.pad_mode = pad_mode
         self.npts = prod(locs.shape[:-1])
         locs_c = locs.detach().reshape(-1, ndim).to(torch.float32).contiguous()
-        d = _desc(ndim, self.grid_size, self.width, kernel, 1, pad_mode, 1.0, False, 1, self.npts)
+        self.beta, self.norm = float(beta), int(norm)
+        # 3D plans also hold each point's tap weights, so they are built for one (kernel, norm, beta)
+        d = _desc(ndim, self.grid_size, self.width, kernel, self.norm, pad_mode, self.beta, False, 1, self.npts)
         L = _ext.lib()
         pb, tb = ctypes.c_size_t(0), ctypes.c_size_t(0)
         _ext.check(L.tlgb_interp_plan_size(ctypes.byref(d), ctypes.byref(pb), ctypes.byref(tb)), "plan size")
@@ -143,7 +145,8 @@ def clear_plan_cache() -> None:
     _PLAN_CACHE.clear()
 
 
-def get_plan(locs: Tensor, grid_size, width, kernel: str, pad_mode: str) -> InterpolatePlan:
+def get_plan(locs: Tensor, grid_size, width, kernel: str, pad_mode: str, beta: float = 1.0,
+             norm: int = 1) -> InterpolatePlan:
     """Cached plan for ``locs``: rebuilt when ``locs`` changes in place."""
     ndim = locs.shape[-1]
     key = (
@@ -155,6 +158,8 @@ def get_plan(locs: Tensor, grid_size, width, kernel: str, pad_mode: str) -> Inte
         _width_tuple(width, ndim),
         kernel,
         pad_mode,
+        float(beta),
+        int(norm),
     )
     hit = _PLAN_CACHE.get(key)
     if hit is not None:
@@ -163,7 +168,7 @@ def get_plan(locs: Tensor, grid_size, width, kernel: str, pad_mode: str) -> Inte
             _PLAN_CACHE.move_to_end(key)
             return plan
         del _PLAN_CACHE[key]
-    plan = InterpolatePlan(locs, grid_size, width, kernel, pad_mode)
+    plan = InterpolatePlan(locs, grid_size, width, kernel, pad_mode, beta, norm)
     _PLAN_CACHE[key] = (weakref.ref(locs), locs._version, plan)
     while len(_PLAN_CACHE) > _PLAN_CACHE_SIZE:
         _PLAN_CACHE.popitem(last=False)
@@ -210,10 +215,10 @@ def ungrid(
     npts = prod(locs_batch_shape)
     width = _width_tuple(width, ndim)
     is_complex = _check_values(vals)
-    plan = get_plan(locs, grid_size, width, kernel, pad_mode)
+    beta = kernel_params["beta"] if kernel == "kaiser_bessel" else 1.0
+    plan = get_plan(locs, grid_size, width, kernel, pad_mode, beta, norm)
     out = torch.empty(nbatch, npts, dtype=vals.dtype, device=dev)
-    d = _desc(ndim, grid_size, width, kernel, norm, pad_mode, kernel_params["beta"] if kernel == "kaiser_bessel" else 1.0,
-              is_complex, nbatch, npts)
+    d = _desc(ndim, grid_size, width, kernel, norm, pad_mode, beta, is_complex, nbatch, npts)
     v = _as_f32_view(vals, is_complex)
     lc = _locs_f32(locs)
     with torch.cuda.device(dev):
@@ -261,9 +266,9 @@ def grid(
     nbatch = prod(batch_shape)
     width = _width_tuple(width, ndim)
     is_complex = _check_values(vals)
-    plan = get_plan(locs, grid_size, width, kernel, pad_mode)
-    d = _desc(ndim, grid_size, width, kernel, norm, pad_mode, kernel_params["beta"] if kernel == "kaiser_bessel" else 1.0,
-              is_complex, nbatch, npts)
+    beta = kernel_params["beta"] if kernel == "kaiser_bessel" else 1.0
+    plan = get_plan(locs, grid_size, width, kernel, pad_mode, beta, norm)
+    d = _desc(ndim, grid_size, width, kernel, norm, pad_mode, beta, is_complex, nbatch, npts)
     L = _ext.lib()
     sb = ctypes.c_size_t(0)
     _ext.check(L.tlgb_interp_adjoint_scratch_size(ctypes.byref(d), ctypes.byref(plan.info), ctypes.byref(sb)), "grid")
@@ -294,9 +299,9 @@ def _grad_locs(gridvals: Tensor, a: Tensor, locs: Tensor, width, kernel, norm, p
     is_complex = gridvals.is_complex()
     if a.is_complex() != is_complex:
         a = a.to(gridvals.dtype)
-    plan = get_plan(locs, grid_size, width, kernel, pad_mode)
-    d = _desc(ndim, grid_size, width, kernel, norm, pad_mode, kernel_params["beta"] if kernel == "kaiser_bessel" else 1.0,
-              is_complex, nbatch, npts)
+    beta = kernel_params["beta"] if kernel == "kaiser_bessel" else 1.0
+    plan = get_plan(locs, grid_size, width, kernel, pad_mode, beta, norm)
+    d = _desc(ndim, grid_size, width, kernel, norm, pad_mode, beta, is_complex, nbatch, npts)
     g = _as_f32_view(gridvals, is_complex)
     av = _as_f32_view(a.reshape(nbatch, npts), is_complex)
     out = torch.empty(npts, ndim, dtype=torch.float32, device=dev)
