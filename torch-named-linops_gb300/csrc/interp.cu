@@ -1889,8 +1889,10 @@ extern "C" int tlgb_interp_plan_build(const tlgb_interp_desc* d, const float* lo
   TLGB_CUDA(cudaMemcpyAsync(h.data(), hist, h.size() * 4, cudaMemcpyDeviceToHost, s));
   TLGB_CUDA(cudaStreamSynchronize(s));
 
-  // work items (host): heaviest first for load balance; results do not
-  // depend on the order because every item writes its own tile or slot
+  // work items (host). Results do not depend on the order, because every
+  // item writes its own tile, slot or points. Gather items stay in tile
+  // order, so neighbouring regions are read while their shared halos are in
+  // L2. Gridding items go heaviest first, for load balance.
   std::vector<int4> fwd, adj, split;
   int64_t pos = 0, n_home = 0, n_partials = 0;
   for (int64_t t = 0; t < L.ntiles; ++t) {
@@ -1913,7 +1915,6 @@ extern "C" int tlgb_interp_plan_build(const tlgb_interp_desc* d, const float* lo
     pos = end;
   }
   auto heavier = [](const int4& a, const int4& b) { return (a.z - a.y) > (b.z - b.y); };
-  std::stable_sort(fwd.begin(), fwd.end(), heavier);
   std::stable_sort(adj.begin(), adj.end(), heavier);
   if ((int64_t)fwd.size() > L.max_fwd || (int64_t)adj.size() > L.max_adj)
     TLGB_FAIL(TLGB_ERR_DEVICE, "work list larger than its bound");
