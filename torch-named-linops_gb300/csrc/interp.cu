@@ -1110,6 +1110,77 @@ __global__ void __launch_bounds__(256) transpose_vals_kernel(const float2* __res
   }
 }
 
+// Write one x-plane (warp) of an 8^3 x 8-entry tile [x][y][z][entry] (16
+// floats per cell) to the grid: per (x, y) row, lane = (entry, z pair), one
+// 16-byte store per lane, 64 contiguous bytes per entry.
+__device__ __forceinline__ void write_tile_rows(const Geo& g, const float* acc, const int (&o)[3], int x, int lane,
+                                                int c0, int ncoil, float* __restrict__ gridv) {
+  constexpr int VS = 16;
+  const long long gvol = (long long)g.N[0] * g.N[1] * g.N[2];
+  const int gx = o[0] + x;
+  if (gx >= g.N[0]) return;
+  const int c = lane >> 2, zp = lane & 3;
+  // 16-byte stores need an even Z extent (row starts at even elements) and an aligned base
+  const bool vec = o[2] + 8 <= g.N[2] && (g.N[2] & 1) == 0 && (reinterpret_cast<uintptr_t>(gridv) & 15) == 0;
+  for (int y = 0; y < 8; ++y) {
+    const int gy = o[1] + y;
+    if (gy >= g.N[1]) break;
+    const float* srow = acc + (x * 8 + y) * 8 * VS;
+    float* drow = gridv + (((long long)gx * g.N[1] + gy) * g.N[2] + o[2]) * 2 + (long long)(c0 + c) * gvol * 2;
+    const float2 a0 = *reinterpret_cast<const float2*>(srow + (2 * zp) * VS + c * 2);
+    const float2 a1 = *reinterpret_cast<const float2*>(srow + (2 * zp + 1) * VS + c * 2);
+    if (c >= ncoil) continue;
+    if (vec) {
+      *reinterpret_cast<float4*>(drow + 4 * zp) = make_float4(a0.x, a0.y, a1.x, a1.y);
+    } else {
+      if (o[2] + 2 * zp < g.N[2]) *reinterpret_cast<float2*>(drow + 4 * zp) = a0;
+      if (o[2] + 2 * zp + 1 < g.N[2]) *reinterpret_cast<float2*>(drow + 4 * zp + 2) = a1;
+    }
+  }
+}
+
+// Sum the partial tiles of one split tile (8^3 x 8 entries) in slot order:
+// coalesced float4 reads, the sum staged in shared memory, then the same
+// row-wise write-out as an unsplit tile.
+__global__ void __launch_bounds__(256) adj_reduce_f3_kernel(Geo g, const int4* __restrict__ split,
+                                                            const float* __restrict__ partial,
+                                                            float* __restrict__ gridv) {
+  constexpr int TFL = 512 * 16;
+  __shared__ __align__(16) float acc[TFL];
+  const int4 sp = split[blockIdx.x];
+  const int cg = blockIdx.y, ncg = gridDim.y;
+  const int c0 = cg * 8;
+  const int ncoil = (int)min(8ll, g.nbatch - c0);
+  int o[3];
+  {
+    int t = sp.x;
+    o[2] = (t % g.nt[2]) * 8;
+    t /= g.nt[2];
+    o[1] = (t % g.nt[1]) * 8;
+    o[0] = (t / g.nt[1]) * 8;
+  }
+  const int tid = threadIdx.x;
+  float4 sum[TFL / 4 / 256];
+  const float4* src = reinterpret_cast<const float4*>(partial + ((long long)sp.y * ncg + cg) * TFL) + tid;
+#pragma unroll
+  for (int i = 0; i < TFL / 4 / 256; ++i) sum[i] = __ldg(src + i * 256);
+  for (int k = 1; k < sp.z; ++k) {
+    const float4* q = reinterpret_cast<const float4*>(partial + ((long long)(sp.y + k) * ncg + cg) * TFL) + tid;
+#pragma unroll
+    for (int i = 0; i < TFL / 4 / 256; ++i) {
+      const float4 v = __ldg(q + i * 256);
+      sum[i].x += v.x;
+      sum[i].y += v.y;
+      sum[i].z += v.z;
+      sum[i].w += v.w;
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < TFL / 4 / 256; ++i) reinterpret_cast<float4*>(acc)[tid + i * 256] = sum[i];
+  __syncthreads();
+  write_tile_rows(g, acc, o, tid >> 5, tid & 31, c0, ncoil, gridv);
+}
+
 // Gridding: CTA = 8 warps owning one 8^3 x 8-entry output tile
 // ([x][y][z][entry], 16 floats per cell); warp w owns the cells of x-plane w,
 // so no two warps write the same cell. Entries are staged in batches of kAB
@@ -1267,24 +1338,7 @@ __global__ void __launch_bounds__(256, 4) adj_f3_kernel(Geo g, const int4* __res
       *reinterpret_cast<float4*>(dst + i) = *reinterpret_cast<const float4*>(acc + i);
     return;
   }
-  // write-out: warp = x plane, per (x, y) row 8 z x 8 entries; lanes (entry fastest, z)
-  const long long gvol = (long long)g.N[0] * g.N[1] * g.N[2];
-  const int gx = o[0] + warp;
-  if (gx >= g.N[0]) return;
-  for (int y = 0; y < 8; ++y) {
-    const int gy = o[1] + y;
-    if (gy >= g.N[1]) break;
-    const float* srow = acc + (warp * 8 + y) * 8 * VS;
-    float* drow = gridv + (((long long)gx * g.N[1] + gy) * g.N[2] + o[2]) * 2;
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int idx = lane + 32 * h;
-      const int c = idx & 7, z = idx >> 3;
-      if (c < ncoil && o[2] + z < g.N[2])
-        *reinterpret_cast<float2*>(drow + ((long long)(c0 + c) * gvol + z) * 2) =
-            *reinterpret_cast<const float2*>(srow + z * VS + c * 2);
-    }
-  }
+  write_tile_rows(g, acc, o, warp, lane, c0, ncoil, gridv);
 }
 
 // Gather: CTA = 8 warps sharing one 12^3 x 8-entry region ([entry][x][y][z],
@@ -2081,8 +2135,8 @@ int launch_adj_f3(const Geo& g, const tlgb_interp_plan_info* info, const char* P
   TLGB_CHECK_LAUNCH();
   if (info->n_split_tiles > 0) {
     dim3 g2((unsigned)info->n_split_tiles, (unsigned)ncg);
-    adj_reduce_kernel<<<g2, NTHR, 0, s>>>(g, (const int4*)(P + info->off_split), (const float*)scratch, (float*)grid,
-                                          8, (int)ncg);
+    adj_reduce_f3_kernel<<<g2, 256, 0, s>>>(g, (const int4*)(P + info->off_split), (const float*)scratch,
+                                             (float*)grid);
     TLGB_CHECK_LAUNCH();
   }
   return TLGB_OK;
