@@ -45,10 +45,11 @@ const char* tlgb_last_error(void);
 int tlgb_version(void);
 
 /* Reads (and, if `clear`, resets) the device status word of the current
- * device. Kernels whose internal waits are bounded (the TMA-staged gather)
- * set it to a non-zero code instead of hanging when a wait gives up; their
- * outputs are then incomplete. Synchronises the device. *status = 0 means no
- * kernel has reported an error since the last clear. */
+ * device. Kernels whose internal waits are bounded set a bit instead of
+ * hanging when a wait gives up, and their outputs are then incomplete:
+ * 1 = the TMA-staged gather, 2 = the tensor-core convolution. Synchronises
+ * the device. *status = 0 means no kernel has reported an error since the
+ * last clear. */
 int tlgb_device_status(int32_t* status, int32_t clear);
 
 /* ------------------------------------------------------------------------ */

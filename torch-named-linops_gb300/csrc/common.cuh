@@ -59,4 +59,8 @@ int64_t radix_counts_len(int64_t n);
 int radix_sort_pairs(uint32_t* keys, int32_t* vals, uint32_t* keys_tmp, int32_t* vals_tmp,
                      uint32_t* counts_tmp, int64_t n, int bits, cudaStream_t s);
 
+// Device status word of the convolution kernels (read and optionally cleared;
+// synchronous). tlgb_device_status combines it with the interpolation one.
+int conv_device_status(int* v, int clear);
+
 }  // namespace tlgb

@@ -10,7 +10,10 @@
 
 #include <cuda_bf16.h>
 
+#include <cstring>
+
 #include "common.cuh"
+#include "sm100.cuh"
 
 namespace tlgb {
 namespace {
@@ -126,6 +129,126 @@ __global__ void __launch_bounds__(128) conv3d_fwd_kernel(int D, int H, int W, co
       }
     }
   }
+}
+
+// ---- the tcgen05 path of the forward / data gradient
+//
+// CTA = 128 output voxels of one (d, h) row (MMA M = 128) x 16 output
+// channels (N = 16), 4 warps. The 9 (kd, kh) input rows of 130 voxels are
+// staged by 18 TMA copies (8 channels each, zero fill outside the volume) in
+// the canonical no-swizzle K-major layout: 16-byte rows, the two 8-channel
+// halves of a row 2176 bytes apart. Tap (kd, kh, kw) is then the A operand
+// starting kw rows into row kd*3 + kh, so the 27 taps are 27 MMAs of K = 16
+// accumulating in one 128 x 16 FP32 TMEM tile. Weights sit in shared memory
+// in the same layout ([tap][k half][n group][8][16 B]). One thread issues the
+// copies and the MMAs; every wait is bounded and a timeout sets the status
+// word; the epilogue reads TMEM with tcgen05.ld (thread = voxel).
+constexpr int kTcM = 128;
+constexpr int kTcHalo = kTcM + 2;
+constexpr int kTcHalfBytes = 2176;                       // >= 130 * 16, a multiple of 128
+constexpr uint32_t kTcABytes = 9 * 2 * kTcHalfBytes;     // 39168
+constexpr uint32_t kTcBBytes = kTaps * 512;               // 13824
+constexpr uint32_t kTcTxBytes = 9 * 2 * kTcHalo * 16;    // bytes the 18 copies deliver
+constexpr uint32_t kTcSmem = kTcABytes + kTcBBytes + 32;  // 4 CTAs per SM
+constexpr uint32_t kTcCols = 32;                           // TMEM columns (the tile uses 16; 32 is the minimum)
+constexpr uint32_t kTcWait = 1u << 22;
+
+__device__ int g_conv_status;
+
+template <int MODE, bool OUTF32>
+__global__ void __launch_bounds__(128) conv3d_tc_kernel(const __grid_constant__ CUtensorMap xmap, int D, int H, int W,
+                                                        const uint4* __restrict__ wts,
+                                                        const __nv_bfloat16* __restrict__ aux,
+                                                        void* __restrict__ y) {
+  using namespace sm100;
+  extern __shared__ __align__(1024) unsigned char smem[];
+  unsigned char* sa = smem;
+  unsigned char* sb = smem + kTcABytes;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sb + kTcBBytes);  // [0] copies, [1] MMAs
+  uint32_t* slot = reinterpret_cast<uint32_t*>(bars + 2);        // [0] TMEM address, [1] copy status
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int w0 = blockIdx.x * kTcM, h = blockIdx.y, d = blockIdx.z;
+  if (warp == 0) {
+    tmem_alloc(slot, kTcCols);
+    tmem_relinquish();
+  }
+  if (tid == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    fence_mbar_init();
+  }
+  // weights: chunk (t, co, k half) of 8 input channels
+  for (int i = tid; i < kTaps * 16 * 2; i += 128) {
+    const int kh2 = i & 1, co = (i >> 1) & 15, t = i >> 5;
+    *reinterpret_cast<uint4*>(sb + t * 512 + kh2 * 256 + (co >> 3) * 128 + (co & 7) * 16) = __ldg(wts + i);
+  }
+  fence_proxy_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = slot[0];
+  if (tid == 0) {
+    mbar_arrive_expect_tx(&bars[0], kTcTxBytes);
+    for (int r = 0; r < 9; ++r)
+      for (int hf = 0; hf < 2; ++hf)
+        tma_load_4d(sa + (r * 2 + hf) * kTcHalfBytes, &xmap, &bars[0], hf * 8, w0 - 1, h + r % 3 - 1, d + r / 3 - 1);
+    const bool landed = mbar_wait_bounded(&bars[0], 0, kTcWait);
+    if (landed) {
+      tc_fence_after();
+      const uint32_t a0 = smem_u32(sa), b0 = smem_u32(sb);
+      constexpr uint32_t idesc = idesc_bf16_f32(kTcM, 16);
+      for (int t = 0; t < kTaps; ++t) {
+        const int r = t / 3, kw = t % 3;
+        const uint64_t ad = smem_desc(a0 + r * 2 * kTcHalfBytes + kw * 16, kTcHalfBytes, 128);
+        const uint64_t bd = smem_desc(b0 + t * 512, 256, 128);
+        umma_bf16(tmem, ad, bd, idesc, t > 0 ? 1u : 0u);
+      }
+      umma_commit(&bars[1]);
+    }
+    slot[1] = landed ? 1u : 0u;
+  }
+  __syncthreads();
+  const bool issued = slot[1] != 0;
+  const bool done = issued && mbar_wait_bounded(&bars[1], 0, kTcWait);
+  if (__syncthreads_and(done)) {
+    tc_fence_after();
+    float v[16];
+    tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16), v);
+    const int w = w0 + warp * 32 + lane;
+    if (w < W) {
+      const long long vox = ((long long)d * H + h) * W + w;
+      if (MODE == 1) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) v[i] = fmaxf(v[i], 0.f);
+      } else if (MODE == 2) {
+        const uint4* m4 = reinterpret_cast<const uint4*>(aux + vox * 16);
+        uint4 mm[2] = {__ldg(m4), __ldg(m4 + 1)};
+        const __nv_bfloat16* mb = reinterpret_cast<const __nv_bfloat16*>(mm);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) v[i] = __bfloat162float(mb[i]) > 0.f ? v[i] : 0.f;
+      }
+      if (OUTF32) {
+        float4* o = reinterpret_cast<float4*>(reinterpret_cast<float*>(y) + vox * 16);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) o[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+      } else {
+        uint4 pk[2];
+        __nv_bfloat162* pb = reinterpret_cast<__nv_bfloat162*>(pk);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) pb[i] = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
+        uint4* o = reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(y) + vox * 16);
+        o[0] = pk[0];
+        o[1] = pk[1];
+      }
+    }
+  } else {
+    if (tid == 0) atomicExch(&g_conv_status, 2);
+    // give in-flight MMAs a last bounded chance before the TMEM is freed
+    if (tid == 0 && issued) mbar_wait_bounded(&bars[1], 0, kTcWait);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(tmem, kTcCols);
 }
 
 // Weight gradient: dW[t][co][ci] = sum over output voxels v of gy[v][co] *
@@ -258,6 +381,31 @@ int check_conv(const tlgb_conv3d_desc* d) {
   return TLGB_OK;
 }
 
+// 4D tensor map over an activation [D][H][W][16] bf16 for 8-channel x 130-voxel boxes
+bool conv_tensor_map(const tlgb_conv3d_desc* d, const void* x, CUtensorMap* map) {
+  auto enc = sm100::tensor_map_encoder();
+  if (!enc || ((uintptr_t)x & 15)) return false;
+  memset(map, 0, sizeof(*map));
+  const cuuint64_t dims[4] = {16, (cuuint64_t)d->W, (cuuint64_t)d->H, (cuuint64_t)d->D};
+  const cuuint64_t strides[3] = {32, (cuuint64_t)d->W * 32, (cuuint64_t)d->W * d->H * 32};
+  const cuuint32_t box[4] = {8, (cuuint32_t)kTcHalo, 1, 1};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(x), dims, strides, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int MODE, bool OUTF32>
+int launch_conv_tc(const tlgb_conv3d_desc* d, const CUtensorMap& map, const void* w, const void* aux, void* y,
+                   cudaStream_t s) {
+  auto* k = conv3d_tc_kernel<MODE, OUTF32>;
+  TLGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem));
+  dim3 grid((unsigned)((d->W + kTcM - 1) / kTcM), (unsigned)d->H, (unsigned)d->D);
+  k<<<grid, 128, kTcSmem, s>>>(map, d->D, d->H, d->W, (const uint4*)w, (const __nv_bfloat16*)aux, y);
+  TLGB_CHECK_LAUNCH();
+  return TLGB_OK;
+}
+
 int wgrad_parts(const tlgb_conv3d_desc* d) {
   const long long rows = (long long)d->D * d->H * ((d->W + kTileW - 1) / kTileW);
   return (int)std::min<long long>(rows, 4 * 152);
@@ -275,6 +423,18 @@ extern "C" int tlgb_conv3d_fwd(const tlgb_conv3d_desc* d, const void* x, const v
   if (((uintptr_t)x | (uintptr_t)w | (uintptr_t)y | (uintptr_t)aux) & 15)
     TLGB_FAIL(TLGB_ERR_INVALID, "conv3d: buffers must be 16-byte aligned");
   cudaStream_t s = (cudaStream_t)stream;
+  CUtensorMap map;
+  if (conv_tensor_map(d, x, &map)) {
+    if (d->out_f32) {
+      if (d->mode == 0) return launch_conv_tc<0, true>(d, map, w, aux, y, s);
+      if (d->mode == 1) return launch_conv_tc<1, true>(d, map, w, aux, y, s);
+      return launch_conv_tc<2, true>(d, map, w, aux, y, s);
+    }
+    if (d->mode == 0) return launch_conv_tc<0, false>(d, map, w, aux, y, s);
+    if (d->mode == 1) return launch_conv_tc<1, false>(d, map, w, aux, y, s);
+    return launch_conv_tc<2, false>(d, map, w, aux, y, s);
+  }
+  // no tensor-map encoder from the driver: the mma.sync kernel
   dim3 grid((unsigned)((d->W + kTileW - 1) / kTileW), (unsigned)d->H, (unsigned)d->D);
   const uint4* xp = (const uint4*)x;
   const uint4* wp = (const uint4*)w;
@@ -339,3 +499,16 @@ extern "C" int tlgb_conv3d_unpack(const float* y, const void* z, int64_t nvox, c
   TLGB_CHECK_LAUNCH();
   return TLGB_OK;
 }
+
+namespace tlgb {
+int conv_device_status(int* v, int clear) {
+  int x = 0;
+  TLGB_CUDA(cudaMemcpyFromSymbol(&x, g_conv_status, sizeof(int)));
+  if (clear) {
+    const int z = 0;
+    TLGB_CUDA(cudaMemcpyToSymbol(g_conv_status, &z, sizeof(int)));
+  }
+  *v = x;
+  return TLGB_OK;
+}
+}  // namespace tlgb

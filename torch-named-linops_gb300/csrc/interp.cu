@@ -38,10 +38,8 @@
 #include <string>
 #include <vector>
 
-#include <cuda.h>
-#include <cudaTypedefs.h>
-
 #include "common.cuh"
+#include "sm100.cuh"
 
 namespace tlgb {
 namespace {
@@ -1050,40 +1048,12 @@ __device__ __forceinline__ float pick4(const float4& v, int i) {
   return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
 }
 
-// ---- TMA and mbarrier helpers (inline PTX)
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t phase) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(phase)
-      : "memory");
-  return ok != 0;
-}
-// bounded wait: false after `limit` polls (the caller then records an error)
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t phase, uint32_t limit) {
-  for (uint32_t i = 0; i < limit; ++i)
-    if (mbar_try_wait(bar, phase)) return true;
-  return false;
-}
-__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, uint64_t* bar, int x0, int x1, int x2,
-                                            int x3) {
-  asm volatile(
-      "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
-      "[%6];" ::"r"(smem_u32(dst)),
-      "l"(map), "r"(x0), "r"(x1), "r"(x2), "r"(x3), "r"(smem_u32(bar))
-      : "memory");
-}
+using sm100::fence_mbar_init;
+using sm100::mbar_arrive_expect_tx;
+using sm100::mbar_init;
+using sm100::mbar_wait_bounded;
+using sm100::smem_u32;
+using sm100::tma_load_4d;
 
 // device status word: set when a bounded wait gave up (see tlgb_interp_forward)
 __device__ int g_tlgb_status;
@@ -2071,19 +2041,7 @@ int launch_adj_t2(const Geo& g, int cg, const tlgb_interp_plan_info* info, const
   return TLGB_OK;
 }
 
-// cuTensorMapEncodeTiled from the driver, looked up once (no -lcuda)
-PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  static std::once_flag once;
-  std::call_once(once, [] {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-  });
-  return fn;
-}
+using sm100::tensor_map_encoder;
 
 int launch_fwd_f3(const Geo& g, const tlgb_interp_plan_info* info, const char* P, const float* locs,
                   const void* grid, void* out, cudaStream_t s) {
@@ -2346,6 +2304,8 @@ extern "C" int tlgb_device_status(int32_t* status, int32_t clear) {
     const int z = 0;
     TLGB_CUDA(cudaMemcpyToSymbol(tlgb::g_tlgb_status, &z, sizeof(int)));
   }
-  *status = v;
+  int vc = 0;
+  TLGB_TRY(tlgb::conv_device_status(&vc, clear));
+  *status = v | vc;
   return TLGB_OK;
 }
