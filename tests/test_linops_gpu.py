@@ -118,3 +118,21 @@ def test_cg_on_nufft_normal_equations():
     # flexible PCG with a fixed diagonal preconditioner converges too
     x2, info2 = alg.cg_solve(N, b, rtol=1e-4, max_iters=300, M=lambda r: r * 0.5)
     assert info2.converged and info2.true_rel_residual < 2e-4
+
+
+def test_cg_matches_float64_oracle():
+    """alg.cg_solve (float32 vectors, float64 scalars) against textbook CG in
+    float64 on the CPU (oracle/cg.py): the same solution to 1e-4."""
+    from oracle import cg as OCG
+
+    gen = torch.Generator().manual_seed(8)
+    n = 200
+    Q, _ = torch.linalg.qr(torch.randn(n, n, dtype=torch.complex128, generator=gen))
+    M = (Q * torch.logspace(0, 2, n, dtype=torch.float64)) @ Q.conj().T
+    xt = torch.randn(n, dtype=torch.complex128, generator=gen)
+    b = M @ xt
+    ref, it = OCG.cg(lambda v: M @ v, b, rtol=1e-10)
+    Mc = M.to(torch.complex64).to(DEV)
+    x, info = alg.cg_solve(lambda v: Mc @ v, b.to(torch.complex64).to(DEV), rtol=1e-6, max_iters=2000)
+    assert info.converged
+    assert rel_l2(x.cpu(), ref) < 1e-4

@@ -47,9 +47,12 @@ inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
-// Exclusive prefix sum of n uint32 values (in may alias out) with one CTA;
-// used only while building plans (one-time work), deterministic.
-int exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* total_dev,
+// Exclusive prefix sum of n uint32 values (in may alias out), deterministic;
+// *total_dev (if given) receives the sum. Long inputs are scanned by many CTAs
+// with scratch_len(n) uint32 of device scratch (not overlapping in/out);
+// without scratch one CTA does it. Used while building plans.
+int64_t scan_scratch_len(int64_t n);
+int exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* total_dev, uint32_t* scratch,
                        cudaStream_t s);
 
 // Stable LSD radix sort of (key, val) pairs by the low `bits` bits of key.

@@ -1893,7 +1893,7 @@ extern "C" int tlgb_interp_plan_build(const tlgb_interp_desc* d, const float* lo
     const unsigned nb = (unsigned)cdiv(g.npts, 256);
     plan_count_kernel<<<nb, 256, 0, s>>>(g, locs, cnt);
     TLGB_CHECK_LAUNCH();
-    TLGB_TRY(exclusive_scan_u32(cnt, cnt, g.npts, total, s));
+    TLGB_TRY(exclusive_scan_u32(cnt, cnt, g.npts, total, counts, s));  // counts is free until the sort
     plan_emit_kernel<<<nb, 256, 0, s>>>(g, locs, cnt, keys, entries);
     TLGB_CHECK_LAUNCH();
     if (L.off_recs > 0) point_records_kernel<<<nb, 256, 0, s>>>(g, locs, (PRec*)(P + L.off_recs));
