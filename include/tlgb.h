@@ -235,6 +235,33 @@ int tlgb_cg_step(float* x, float* r, float* p, const float* ap, int64_t n, int i
                  void* scratch, size_t scratch_bytes, tlgb_stream_t stream);
 
 /* ------------------------------------------------------------------------ */
+/* Centred-FFT shifts folded into the NUFFT's pad and crop (complex64).      */
+/* The reference's cfftn = fftshift . fftn . ifftshift (utils/_fft.py:7-60)  */
+/* costs two extra grid passes per transform; here the image-side shift is   */
+/* part of one pad / crop gather, and the k-side shift is a shift of the     */
+/* trajectory by -floor(Np/2) (grid units) where it is prepared.             */
+/* ------------------------------------------------------------------------ */
+
+/* Zero pad with the ifftshift folded in: for the padded-grid index j,
+ * i = ((j + shift) mod np) - off per dim; out[b*C + c][j] =
+ * maps[c][i] * apod[i] * x[b][i] where i lies in the image, else 0.
+ * Dims: the last `ndim` (1-3) of x [nbatch][n] and out [nbatch*C][np];
+ * shift = floor(np / 2) gives the reference's ifftshift(pad(x)); off is the
+ * left padding. apod (float, [n]) and maps (complex64, [C][n], C = nmaps)
+ * may be NULL (then C = 1). */
+int tlgb_pad_shift_c64(const void* x, int64_t nbatch, int32_t ndim, const int64_t* n, const int64_t* np,
+                       const int64_t* off, const int64_t* shift, const float* apod, const void* maps, int32_t nmaps,
+                       void* out, tlgb_stream_t stream);
+
+/* Crop with the fftshift folded in, the adjoint of tlgb_pad_shift plus an
+ * axpy: out[b][i] = alpha * apod[i] * sum_c conj(maps[c][i]) *
+ * z[b*C + c][j(i)] + beta * add[b][i], with j = (i + off - shift) mod np per
+ * dim. add may be NULL (then beta is ignored). */
+int tlgb_crop_shift_c64(const void* z, int64_t nbatch, int32_t ndim, const int64_t* n, const int64_t* np,
+                        const int64_t* off, const int64_t* shift, const float* apod, const void* maps, int32_t nmaps,
+                        float alpha, const void* add, float beta, void* out, tlgb_stream_t stream);
+
+/* ------------------------------------------------------------------------ */
 /* 3^3 convolution on the tensor cores (BF16 operands, FP32 accumulation):    */
 /* the layers of the learned CG preconditioner. No counterpart in the         */
 /* reference (torchlinops has no learned preconditioner).                     */

@@ -136,3 +136,47 @@ def test_cg_matches_float64_oracle():
     x, info = alg.cg_solve(lambda v: Mc @ v, b.to(torch.complex64).to(DEV), rtol=1e-6, max_iters=2000)
     assert info.converged
     assert rel_l2(x.cpu(), ref) < 1e-4
+
+
+@pytest.mark.parametrize("im,padded", [((24, 20, 18), (30, 25, 23)), ((16, 15), (20, 19)), ((33,), (41,))])
+def test_pad_shift_and_crop_shift_match_torch(im, padded):
+    """pad_shift = ifftshift(pad(maps * apod * x)), crop_shift its adjoint
+    with fftshift, against torch on odd and even sizes."""
+    gen = torch.Generator().manual_seed(len(im) + padded[0])
+    nd = len(im)
+    dims = tuple(range(-nd, 0))
+    x = torch.randn(*im, dtype=torch.complex64, generator=gen)
+    maps = torch.randn(3, *im, dtype=torch.complex64, generator=gen)
+    apod = torch.rand(*im, generator=gen) + 0.5
+    pad = linops.pad_to_size(im, padded)
+    ref = torch.fft.ifftshift(torch.nn.functional.pad(maps * apod * x, pad), dim=dims)
+    got = linops.pad_shift(x.to(DEV), im, padded, maps=maps.to(DEV), apod=apod.to(DEV)).cpu()
+    torch.testing.assert_close(got, ref, rtol=1e-6, atol=1e-6)  # same values, products rounded in another order
+    assert torch.equal(got == 0, ref == 0)  # the same zero padding
+    z = torch.randn(3, *padded, dtype=torch.complex64, generator=gen)
+    sl = tuple(linops.crop_slice_from_pad(pad))
+    back = (maps.conj() * apod * torch.fft.fftshift(z, dim=dims)[(slice(None),) + sl]).sum(0)
+    add = torch.randn(*im, dtype=torch.complex64, generator=gen)
+    gotb = linops.crop_shift(z.to(DEV), im, padded, maps=maps.to(DEV), apod=apod.to(DEV), alpha=0.5,
+                             add=add.to(DEV), beta=2.0).cpu()
+    torch.testing.assert_close(gotb, 0.5 * back + 2.0 * add, rtol=1e-5, atol=1e-5)
+    # adjoint pair without maps
+    y = torch.randn(*padded, dtype=torch.complex64, generator=gen)
+    lhs = torch.vdot(linops.pad_shift(x.to(DEV), im, padded, apod=apod.to(DEV)).cpu().flatten(), y.flatten())
+    rhs = torch.vdot(x.flatten(), linops.crop_shift(y.to(DEV), im, padded, apod=apod.to(DEV)).cpu().flatten())
+    assert abs(complex(lhs) - complex(rhs)) / abs(complex(lhs)) < 1e-5
+
+
+def test_sense_normal_matches_unfused_operator():
+    """The fused SENSE normal operator equals sum_c conj(S_c) F^H F (S_c x)
+    built from the NUFFT linop and torch elementwise ops."""
+    from torchlinops_gb300 import mri
+
+    n = 20
+    locs = mri.radial_trajectory_3d(100, 40, n, DEV)
+    maps = mri.gaussian_coil_maps_3d(3, n, device=DEV)
+    A = mri.SenseNormal(locs, maps, lam=1e-2, normalise=False)
+    gen = torch.Generator().manual_seed(3)
+    x = torch.randn(n, n, n, dtype=torch.complex64, generator=gen).to(DEV)
+    ref = (maps.conj() * A.F.N(maps * x)).sum(0) + 1e-2 * x
+    assert rel_l2(A(x).cpu(), ref.cpu()) < 1e-5

@@ -14,13 +14,18 @@ re-pointing its functional calls (see the integration notes of this repo).
 * ``Interpolate``    <- linops/interp.py:16-137
 * ``ArrayToBlocks``  <- linops/array_to_blocks.py:16-110
 * ``BlocksToArray``  <- linops/array_to_blocks.py:113-205
-* ``NUFFT``          <- linops/nufft.py:34-392 (interpolate mode)
+* ``NUFFT``          <- linops/nufft.py:34-392 (interpolate mode); its centred
+  FFT's two shifts are folded into ``PadShift`` and the trajectory
+* ``PadShift``, ``pad_shift``, ``crop_shift`` <- pad_last.py + utils/_fft.py
+  (pad, ifftshift / fftshift, crop, apodization and coil maps in one pass)
 * ``Diagonal``, ``Scalar``, ``Pad``, ``FFT`` <- linops/{diagonal,scalar,pad_last,fft}.py
 * ``nufft`` / ``nufft_adjoint`` <- functional/_nufft.py:16-112
 """
 
 from __future__ import annotations
 
+import ctypes
+import math
 from copy import copy
 from math import prod
 from typing import Optional
@@ -30,6 +35,7 @@ import torch.nn as nn
 import torch.nn.functional as F
 from torch import Tensor
 
+from . import _ext
 from . import blocks as B
 from . import interp as I
 
@@ -261,6 +267,94 @@ class Pad(NamedLinop):
         return y[tuple([slice(None)] * (y.ndim - p.D) + p.crop_slice)]
 
 
+def _i64(vals):
+    arr = (ctypes.c_int64 * 3)()
+    for i, v in enumerate(vals):
+        arr[i] = int(v)
+    return arr
+
+
+def pad_shift(x: Tensor, im_size, padded_size, maps: Optional[Tensor] = None, apod: Optional[Tensor] = None) -> Tensor:
+    """ifftshift(pad(apod * x)) (or per coil map: ifftshift(pad(maps_c * apod * x)))
+    over the last ``len(im_size)`` dims in one pass; complex64, CUDA."""
+    nd = len(im_size)
+    _ext.check_cuda(x, maps, apod)
+    if x.dtype != torch.complex64:
+        raise TypeError(f"pad_shift takes complex64, got {x.dtype}")
+    if tuple(x.shape[-nd:]) != tuple(im_size):
+        raise ValueError(f"Mismatched shapes: expected {tuple(im_size)} but got {tuple(x.shape[-nd:])}")
+    pad = pad_to_size(im_size, padded_size)
+    off = [pad[2 * (nd - 1 - i)] for i in range(nd)]
+    shift = [p // 2 for p in padded_size]
+    batch = x.shape[:-nd]
+    xb = x.resolve_conj().resolve_neg().contiguous()
+    nb = math.prod(batch)
+    C = 1
+    if maps is not None:
+        maps = maps.resolve_conj().resolve_neg().to(torch.complex64).contiguous()
+        C = maps.numel() // math.prod(im_size)
+    out_batch = tuple(batch) + ((C,) if maps is not None else ())
+    out = torch.empty(*out_batch, *padded_size, dtype=torch.complex64, device=x.device)
+    ap = None if apod is None else apod.to(torch.float32).contiguous()
+    _ext.check(_ext.lib().tlgb_pad_shift_c64(_ext.ptr(xb), nb, nd, _i64(im_size), _i64(padded_size), _i64(off),
+                                             _i64(shift), _ext.ptr(ap), _ext.ptr(maps), C, _ext.ptr(out),
+                                             _ext.stream_ptr(x.device)), "pad_shift")
+    return out
+
+
+def crop_shift(z: Tensor, im_size, padded_size, maps: Optional[Tensor] = None, apod: Optional[Tensor] = None,
+               alpha: float = 1.0, add: Optional[Tensor] = None, beta: float = 0.0) -> Tensor:
+    """alpha * apod * crop(fftshift(z)) (with maps: summed over the coil dim of
+    z after multiplying by conj(maps)) + beta * add, in one pass."""
+    nd = len(im_size)
+    _ext.check_cuda(z, maps, apod, add)
+    if z.dtype != torch.complex64:
+        raise TypeError(f"crop_shift takes complex64, got {z.dtype}")
+    if tuple(z.shape[-nd:]) != tuple(padded_size):
+        raise ValueError(f"Mismatched shapes: expected {tuple(padded_size)} but got {tuple(z.shape[-nd:])}")
+    pad = pad_to_size(im_size, padded_size)
+    off = [pad[2 * (nd - 1 - i)] for i in range(nd)]
+    shift = [p // 2 for p in padded_size]
+    zb = z.resolve_conj().resolve_neg().contiguous()
+    C = 1
+    batch = z.shape[:-nd]
+    if maps is not None:
+        maps = maps.resolve_conj().resolve_neg().to(torch.complex64).contiguous()
+        C = maps.numel() // math.prod(im_size)
+        batch = batch[:-1]
+    nb = math.prod(batch)
+    out = torch.empty(*batch, *im_size, dtype=torch.complex64, device=z.device)
+    ap = None if apod is None else apod.to(torch.float32).contiguous()
+    ad = None if add is None else add.resolve_conj().resolve_neg().to(torch.complex64).contiguous()
+    _ext.check(_ext.lib().tlgb_crop_shift_c64(_ext.ptr(zb), nb, nd, _i64(im_size), _i64(padded_size), _i64(off),
+                                              _i64(shift), _ext.ptr(ap), _ext.ptr(maps), C, ctypes.c_float(alpha),
+                                              _ext.ptr(ad), ctypes.c_float(beta), _ext.ptr(out),
+                                              _ext.stream_ptr(z.device)), "crop_shift")
+    return out
+
+
+class PadShift(NamedLinop):
+    """apod * x, centred zero pad and ifftshift in one pass; the adjoint is
+    fftshift, crop and apod in one pass. With an uncentred FFT after it and
+    the trajectory shifted by -floor(Np/2), this is the reference's
+    Apodize -> Pad -> cfftn (nufft.py:170-184) without the two shift passes
+    per transform."""
+
+    def __init__(self, padded_size, im_size, apod: Optional[Tensor] = None):
+        super().__init__()
+        self.im_size = tuple(im_size)
+        self.pad_im_size = tuple(padded_size)
+        self.apod = apod
+
+    @staticmethod
+    def fn(p, x, /):
+        return pad_shift(x, p.im_size, p.pad_im_size, apod=p.apod)
+
+    @staticmethod
+    def adj_fn(p, y, /):
+        return crop_shift(y, p.im_size, p.pad_im_size, apod=p.apod)
+
+
 class FFT(NamedLinop):
     """Centred orthonormal FFT over the last ndim dims (fft.py)."""
 
@@ -405,6 +499,16 @@ def prep_locs(locs: Tensor, grid_size, padded_size, pad_mode="circular") -> Tens
     return out
 
 
+def prep_locs_shifted(locs: Tensor, grid_size, padded_size) -> Tensor:
+    """prep_locs (circular) minus floor(Np/2): the trajectory on which an
+    uncentred FFT's output is read where the reference reads fftshift(FFT)."""
+    out = locs.clone()
+    for i in range(-len(grid_size), 0):
+        out[..., i] *= padded_size[i] / grid_size[i]
+        out[..., i] = torch.remainder(out[..., i], torch.tensor(padded_size[i], device=locs.device))
+    return out
+
+
 def apodize_weights(grid_size, padded_size, oversamp, width: float, beta: float) -> Tensor:
     """Separable KB apodization (nufft.py:349-365)."""
     gs = torch.tensor(grid_size)
@@ -438,9 +542,6 @@ class NUFFT(Chain):
         device = locs.device
         ndim = len(grid_size)
         padded_size = tuple(int(i * oversamp) for i in grid_size)
-        pad = Pad(padded_size, grid_size)
-        fft = FFT(ndim=locs.shape[-1], centered=True, norm="ortho")
-        locs_prepared = prep_locs(locs, grid_size, padded_size) if do_prep_locs else locs
         beta = nufft_beta(width, oversamp)
         if apodize_weights is None:
             weight = globals()["apodize_weights"](grid_size, padded_size, oversamp, width, beta).to(device)
@@ -448,18 +549,28 @@ class NUFFT(Chain):
             weight = apodize_weights
         if weight.isnan().any() or weight.isinf().any():
             raise ValueError(f"Nan/Inf values detected in apodization weight (width={width}, oversamp={oversamp}).")
-        apodize = Diagonal(weight)
+        # Apodize -> Pad -> cfftn, with both centring shifts folded into the
+        # pad and the trajectory (no full-grid shift passes); same operator
+        padshift = PadShift(padded_size, grid_size, weight)
+        fft = FFT(ndim=locs.shape[-1], centered=False, norm="ortho")
+        locs_prepared = (prep_locs_shifted(locs, grid_size, padded_size) if do_prep_locs
+                         else torch.remainder(locs - torch.tensor([p // 2 for p in padded_size], device=device,
+                                                                  dtype=locs.dtype), torch.tensor(padded_size, device=device, dtype=locs.dtype)))
         interp = Interpolate(
             locs_prepared, padded_size, width=width, kernel="kaiser_bessel", kernel_params=dict(beta=beta)
         )
         scale_factor = width**ndim * (prod(grid_size) / prod(padded_size)) ** 0.5
         scale = Scalar(torch.tensor(1.0 / scale_factor, device=device))
-        super().__init__(apodize, pad, fft, interp, scale, name="NUFFT")
+        super().__init__(padshift, fft, interp, scale, name="NUFFT")
+        self.apodize_weight = weight
+        self.scale_factor = scale_factor
+        self.padded_size = padded_size
+        self.locs_shifted = locs_prepared
         self.locs = locs
         self.grid_size = tuple(grid_size)
         self.oversamp = oversamp
         self.width = width
-        self.pad = pad
+        self.pad = padshift
         self.fft = fft
         self.interp = interp
 
@@ -470,10 +581,10 @@ def nufft(x: Tensor, locs: Tensor, oversamp: float = 1.25, width: float = 4.0) -
     ndim = locs.shape[-1]
     padded = tuple(int(s * oversamp) for s in grid_size)
     beta = nufft_beta(width, oversamp)
-    x = x * apodize_weights(grid_size, padded, oversamp, width, beta).to(x.device)
-    x = Pad.fn(Pad(padded, grid_size), x)
-    x = cfftn(x, dim=tuple(range(-ndim, 0)), norm="ortho")
-    x = I.interpolate(x, prep_locs(locs, grid_size, padded), width, kernel="kaiser_bessel", kernel_params=dict(beta=beta))
+    x = pad_shift(x, grid_size, padded, apod=apodize_weights(grid_size, padded, oversamp, width, beta).to(x.device))
+    x = torch.fft.fftn(x, dim=tuple(range(-ndim, 0)), norm="ortho")
+    x = I.interpolate(x, prep_locs_shifted(locs, grid_size, padded), width, kernel="kaiser_bessel",
+                      kernel_params=dict(beta=beta))
     return x / (width**ndim * (prod(grid_size) / prod(padded)) ** 0.5)
 
 
@@ -484,8 +595,7 @@ def nufft_adjoint(x: Tensor, locs: Tensor, grid_size, oversamp: float = 1.25, wi
     padded = tuple(int(s * oversamp) for s in grid_size)
     beta = nufft_beta(width, oversamp)
     x = x / (width**ndim * (prod(grid_size) / prod(padded)) ** 0.5)
-    x = I.interpolate_adjoint(x, prep_locs(locs, grid_size, padded), padded, width, kernel="kaiser_bessel",
+    x = I.interpolate_adjoint(x, prep_locs_shifted(locs, grid_size, padded), padded, width, kernel="kaiser_bessel",
                               kernel_params=dict(beta=beta))
-    x = cifftn(x, dim=tuple(range(-ndim, 0)), norm="ortho")
-    x = Pad.adj_fn(Pad(padded, grid_size), x)
-    return x * apodize_weights(grid_size, padded, oversamp, width, beta).to(x.device)
+    x = torch.fft.ifftn(x, dim=tuple(range(-ndim, 0)), norm="ortho")
+    return crop_shift(x, grid_size, padded, apod=apodize_weights(grid_size, padded, oversamp, width, beta).to(x.device))

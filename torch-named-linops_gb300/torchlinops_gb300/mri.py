@@ -142,11 +142,17 @@ def power_method(A, v: Tensor, iters: int = 30) -> float:
 
 
 class SenseNormal:
-    """x -> s * sum_c conj(S_c) F^H F (S_c x) + lam * x for an n^3 image."""
+    """x -> s * sum_c conj(S_c) F^H F (S_c x) + lam * x for an n^3 image.
+
+    F is this package's NUFFT. The coil maps, apodization, pad and centring
+    shift go in one pass (``linops.pad_shift``) and the way back (shift, crop,
+    apodization, conj maps, coil sum, scale and the lam x term) in another
+    (``linops.crop_shift``); between them one FFT, one gather, one gridding
+    and one inverse FFT for all coils at once."""
 
     def __init__(self, locs: Tensor, maps: Tensor, lam: float = 1e-3, oversamp: float = 1.25, width: float = 4.0,
                  normalise: bool = True, seed: int = 0):
-        self.maps = maps
+        self.maps = maps.contiguous()
         self.n = tuple(maps.shape[1:])
         self.F = linops.NUFFT(locs, self.n, oversamp=oversamp, width=width)
         self.lam = lam
@@ -156,9 +162,19 @@ class SenseNormal:
             v0 = torch.complex(torch.randn(*self.n, generator=g), torch.randn(*self.n, generator=g)).to(maps.device)
             self.scale = 1.0 / power_method(self.data_normal, v0)
 
+    def _normal(self, x: Tensor, lam: float) -> Tensor:
+        F = self.F
+        z = linops.pad_shift(x, self.n, F.padded_size, maps=self.maps, apod=F.apodize_weight)
+        z = torch.fft.fftn(z, dim=(-3, -2, -1), norm="ortho")
+        y = F.interp(z)
+        g = F.interp.H(y)
+        g = torch.fft.ifftn(g, dim=(-3, -2, -1), norm="ortho")
+        alpha = self.scale / F.scale_factor**2
+        return linops.crop_shift(g, self.n, F.padded_size, maps=self.maps, apod=F.apodize_weight, alpha=alpha,
+                                 add=x if lam != 0.0 else None, beta=lam)
+
     def data_normal(self, x: Tensor) -> Tensor:
-        y = self.F.N(self.maps * x)
-        return self.scale * (self.maps.conj() * y).sum(0)
+        return self._normal(x, 0.0)
 
     def forward_op(self, x: Tensor) -> Tensor:
         """A x = sqrt(s) F(S x): [ncoil, npts] k-space data."""
@@ -168,4 +184,4 @@ class SenseNormal:
         return math.sqrt(self.scale) * (self.maps.conj() * self.F.H(y)).sum(0)
 
     def __call__(self, x: Tensor) -> Tensor:
-        return self.data_normal(x) + self.lam * x
+        return self._normal(x, self.lam)
