@@ -133,24 +133,30 @@ __global__ void __launch_bounds__(128) conv3d_fwd_kernel(int D, int H, int W, co
 
 // ---- the tcgen05 path of the forward / data gradient
 //
-// CTA = 128 output voxels of one (d, h) row (MMA M = 128) x 16 output
-// channels (N = 16), 4 warps. The 9 (kd, kh) input rows of 130 voxels are
-// staged by 18 TMA copies (8 channels each, zero fill outside the volume) in
-// the canonical no-swizzle K-major layout: 16-byte rows, the two 8-channel
-// halves of a row 2176 bytes apart. Tap (kd, kh, kw) is then the A operand
-// starting kw rows into row kd*3 + kh, so the 27 taps are 27 MMAs of K = 16
-// accumulating in one 128 x 16 FP32 TMEM tile. Weights sit in shared memory
-// in the same layout ([tap][k half][n group][8][16 B]). One thread issues the
-// copies and the MMAs; every wait is bounded and a timeout sets the status
-// word; the epilogue reads TMEM with tcgen05.ld (thread = voxel).
+// Persistent CTAs of 4 warps. A work unit is a column segment of up to kTcRows
+// output rows (fixed d, consecutive h) of 128 voxels along W (MMA M = 128)
+// x 16 output channels (N = 16). Input rows (d + kd - 1, h') sit in a ring of
+// 4 slots per kd; output row h reads rows h - 1, h, h + 1 of each kd, so
+// after the first row each output row needs 3 new rows (6 TMA copies of 8
+// channels x 130 voxels, zero fill outside the volume) instead of 9. Layout:
+// the canonical no-swizzle K-major one, 16-byte rows, the two 8-channel
+// halves of a row 2176 bytes apart; tap (kd, kh, kw) is the A operand kw rows
+// into slot (h + kh - 1) mod 4 of kd, and the 27 taps are 27 MMAs of K = 16
+// into one 128 x 16 FP32 TMEM accumulator. Two accumulators alternate, so
+// the MMAs of row r overlap the epilogue of row r - 1. Weights stay in
+// shared memory ([tap][k half][n group][8][16 B]) for the CTA's lifetime.
+// Thread 0 issues copies and MMAs; every wait is bounded, and a timeout sets
+// the status word and ends the CTA's work after freeing its TMEM.
 constexpr int kTcM = 128;
 constexpr int kTcHalo = kTcM + 2;
+constexpr int kTcRows = 16;                               // output rows per work unit
 constexpr int kTcHalfBytes = 2176;                       // >= 130 * 16, a multiple of 128
-constexpr uint32_t kTcABytes = 9 * 2 * kTcHalfBytes;     // 39168
-constexpr uint32_t kTcBBytes = kTaps * 512;               // 13824
-constexpr uint32_t kTcTxBytes = 9 * 2 * kTcHalo * 16;    // bytes the 18 copies deliver
-constexpr uint32_t kTcSmem = kTcABytes + kTcBBytes + 32;  // 4 CTAs per SM
-constexpr uint32_t kTcCols = 32;                           // TMEM columns (the tile uses 16; 32 is the minimum)
+constexpr int kTcSlotBytes = 2 * kTcHalfBytes;
+constexpr uint32_t kTcABytes = 3 * 4 * kTcSlotBytes;     // 3 kd x 4 ring slots
+constexpr uint32_t kTcBBytes = kTaps * 512;              // 13824
+constexpr uint32_t kTcCopyBytes = kTcHalo * 16;          // one 8-channel row copy
+constexpr uint32_t kTcSmem = kTcABytes + kTcBBytes + 64;
+constexpr uint32_t kTcCols = 32;                         // two 16-column accumulators
 constexpr uint32_t kTcWait = 1u << 22;
 
 __device__ int g_conv_status;
@@ -164,20 +170,20 @@ __global__ void __launch_bounds__(128) conv3d_tc_kernel(const __grid_constant__ 
   extern __shared__ __align__(1024) unsigned char smem[];
   unsigned char* sa = smem;
   unsigned char* sb = smem + kTcABytes;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(sb + kTcBBytes);  // [0] copies, [1] MMAs
-  uint32_t* slot = reinterpret_cast<uint32_t*>(bars + 2);        // [0] TMEM address, [1] copy status
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sb + kTcBBytes);  // [0,1] copies, [2,3] MMAs
+  uint32_t* slot = reinterpret_cast<uint32_t*>(bars + 4);        // [0] TMEM address, [1] failure flag
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int w0 = blockIdx.x * kTcM, h = blockIdx.y, d = blockIdx.z;
+  const int ntw = (W + kTcM - 1) / kTcM, nseg = (H + kTcRows - 1) / kTcRows;
+  const long long nunits = (long long)D * ntw * nseg;
   if (warp == 0) {
     tmem_alloc(slot, kTcCols);
     tmem_relinquish();
   }
   if (tid == 0) {
-    mbar_init(&bars[0], 1);
-    mbar_init(&bars[1], 1);
+    for (int i = 0; i < 4; ++i) mbar_init(&bars[i], 1);
     fence_mbar_init();
+    slot[1] = 0;
   }
-  // weights: chunk (t, co, k half) of 8 input channels
   for (int i = tid; i < kTaps * 16 * 2; i += 128) {
     const int kh2 = i & 1, co = (i >> 1) & 15, t = i >> 5;
     *reinterpret_cast<uint4*>(sb + t * 512 + kh2 * 256 + (co >> 3) * 128 + (co & 7) * 16) = __ldg(wts + i);
@@ -187,66 +193,104 @@ __global__ void __launch_bounds__(128) conv3d_tc_kernel(const __grid_constant__ 
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = slot[0];
-  if (tid == 0) {
-    mbar_arrive_expect_tx(&bars[0], kTcTxBytes);
-    for (int r = 0; r < 9; ++r)
+  const uint32_t a0 = smem_u32(sa), b0 = smem_u32(sb);
+  constexpr uint32_t idesc = idesc_bf16_f32(kTcM, 16);
+  uint32_t lg = 0;     // copy groups issued (thread 0): group k arms bars[k & 1]
+  uint32_t lw = 0;     // copy groups waited on (thread 0)
+  uint32_t og = 0;     // output rows issued in this CTA: row k uses accumulator k & 1 and bars[2 + (k & 1)]
+  bool fail = false;
+
+  auto load_row = [&](int d, int hr, int w0) {  // the 3 kd rows (d + kd - 1, hr) into slot hr mod 4
+    for (int kd = 0; kd < 3; ++kd)
       for (int hf = 0; hf < 2; ++hf)
-        tma_load_4d(sa + (r * 2 + hf) * kTcHalfBytes, &xmap, &bars[0], hf * 8, w0 - 1, h + r % 3 - 1, d + r / 3 - 1);
-    const bool landed = mbar_wait_bounded(&bars[0], 0, kTcWait);
-    if (landed) {
-      tc_fence_after();
-      const uint32_t a0 = smem_u32(sa), b0 = smem_u32(sb);
-      constexpr uint32_t idesc = idesc_bf16_f32(kTcM, 16);
-      for (int t = 0; t < kTaps; ++t) {
-        const int r = t / 3, kw = t % 3;
-        const uint64_t ad = smem_desc(a0 + r * 2 * kTcHalfBytes + kw * 16, kTcHalfBytes, 128);
-        const uint64_t bd = smem_desc(b0 + t * 512, 256, 128);
-        umma_bf16(tmem, ad, bd, idesc, t > 0 ? 1u : 0u);
-      }
-      umma_commit(&bars[1]);
+        tma_load_4d(sa + (kd * 4 + (hr & 3)) * kTcSlotBytes + hf * kTcHalfBytes, &xmap, &bars[lg & 1], hf * 8, w0 - 1,
+                    hr, d + kd - 1);
+  };
+
+  for (long long u = blockIdx.x; u < nunits && !fail; u += gridDim.x) {
+    const int hs = (int)(u % nseg);
+    const long long dw = u / nseg;
+    const int wt = (int)(dw % ntw), d = (int)(dw / ntw);
+    const int w0 = wt * kTcM, h0 = hs * kTcRows;
+    const int R = min(kTcRows, H - h0);
+    if (tid == 0) {
+      mbar_arrive_expect_tx(&bars[lg & 1], 9 * 2 * kTcCopyBytes);
+      for (int hr = h0 - 1; hr <= h0 + 1; ++hr) load_row(d, hr, w0);
+      ++lg;
     }
-    slot[1] = landed ? 1u : 0u;
-  }
-  __syncthreads();
-  const bool issued = slot[1] != 0;
-  const bool done = issued && mbar_wait_bounded(&bars[1], 0, kTcWait);
-  if (__syncthreads_and(done)) {
-    tc_fence_after();
-    float v[16];
-    tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16), v);
-    const int w = w0 + warp * 32 + lane;
-    if (w < W) {
-      const long long vox = ((long long)d * H + h) * W + w;
-      if (MODE == 1) {
-#pragma unroll
-        for (int i = 0; i < 16; ++i) v[i] = fmaxf(v[i], 0.f);
-      } else if (MODE == 2) {
-        const uint4* m4 = reinterpret_cast<const uint4*>(aux + vox * 16);
-        uint4 mm[2] = {__ldg(m4), __ldg(m4 + 1)};
-        const __nv_bfloat16* mb = reinterpret_cast<const __nv_bfloat16*>(mm);
-#pragma unroll
-        for (int i = 0; i < 16; ++i) v[i] = __bfloat162float(mb[i]) > 0.f ? v[i] : 0.f;
+    for (int r = 0; r <= R; ++r) {
+      const int h = h0 + r;
+      if (tid == 0 && r < R && !fail) {
+        if (r + 1 < R) {
+          // row h + 2 (for output h + 1) replaces row h - 2, last read by output h - 1
+          if (r >= 1 && !mbar_wait_bounded(&bars[2 + ((og - 1) & 1)], ((og - 1) >> 1) & 1, kTcWait)) fail = true;
+          mbar_arrive_expect_tx(&bars[lg & 1], 3 * 2 * kTcCopyBytes);
+          load_row(d, h + 2, w0);
+          ++lg;
+        }
+        if (!mbar_wait_bounded(&bars[lw & 1], (lw >> 1) & 1, kTcWait)) fail = true;
+        ++lw;
+        if (!fail) {
+          tc_fence_after();
+          const uint32_t acc = tmem + (og & 1) * 16;
+          for (int t = 0; t < kTaps; ++t) {
+            const int kd = t / 9, kh = (t / 3) % 3, kw = t % 3;
+            const uint32_t aa = a0 + (kd * 4 + ((h + kh - 1) & 3)) * kTcSlotBytes + kw * 16;
+            umma_bf16(acc, smem_desc(aa, kTcHalfBytes, 128), smem_desc(b0 + t * 512, 256, 128), idesc,
+                      t > 0 ? 1u : 0u);
+          }
+          umma_commit(&bars[2 + (og & 1)]);
+        }
+        if (fail) slot[1] = 1;
       }
-      if (OUTF32) {
-        float4* o = reinterpret_cast<float4*>(reinterpret_cast<float*>(y) + vox * 16);
+      if (r < R) ++og;
+      if (r >= 1) {
+        // epilogue of output h - 1 (accumulator (og - 2) & 1 after this row's increment)
+        const uint32_t k = r < R ? og - 2 : og - 1;
+        const bool done = mbar_wait_bounded(&bars[2 + (k & 1)], (k >> 1) & 1, kTcWait);
+        if (!done) slot[1] = 1;
+        if (__syncthreads_and(done)) {
+          tc_fence_after();
+          float v[16];
+          tmem_ld16(tmem + (k & 1) * 16 + ((uint32_t)(warp * 32) << 16), v);
+          const int w = w0 + warp * 32 + lane;
+          if (w < W) {
+            const long long vox = ((long long)d * H + (h - 1)) * W + w;
+            if (MODE == 1) {
 #pragma unroll
-        for (int q = 0; q < 4; ++q) o[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
-      } else {
-        uint4 pk[2];
-        __nv_bfloat162* pb = reinterpret_cast<__nv_bfloat162*>(pk);
+              for (int i = 0; i < 16; ++i) v[i] = fmaxf(v[i], 0.f);
+            } else if (MODE == 2) {
+              const uint4* m4 = reinterpret_cast<const uint4*>(aux + vox * 16);
+              uint4 mm[2] = {__ldg(m4), __ldg(m4 + 1)};
+              const __nv_bfloat16* mb = reinterpret_cast<const __nv_bfloat16*>(mm);
 #pragma unroll
-        for (int i = 0; i < 8; ++i) pb[i] = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
-        uint4* o = reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(y) + vox * 16);
-        o[0] = pk[0];
-        o[1] = pk[1];
+              for (int i = 0; i < 16; ++i) v[i] = __bfloat162float(mb[i]) > 0.f ? v[i] : 0.f;
+            }
+            if (OUTF32) {
+              float4* o = reinterpret_cast<float4*>(reinterpret_cast<float*>(y) + vox * 16);
+#pragma unroll
+              for (int q = 0; q < 4; ++q) o[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+            } else {
+              uint4 pk[2];
+              __nv_bfloat162* pb = reinterpret_cast<__nv_bfloat162*>(pk);
+#pragma unroll
+              for (int i = 0; i < 8; ++i) pb[i] = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
+              uint4* o = reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(y) + vox * 16);
+              o[0] = pk[0];
+              o[1] = pk[1];
+            }
+          }
+        }
+      }
+      tc_fence_before();
+      __syncthreads();
+      if (slot[1]) {
+        fail = true;
+        break;
       }
     }
-  } else {
-    if (tid == 0) atomicExch(&g_conv_status, 2);
-    // give in-flight MMAs a last bounded chance before the TMEM is freed
-    if (tid == 0 && issued) mbar_wait_bounded(&bars[1], 0, kTcWait);
   }
-  tc_fence_before();
+  if (fail && tid == 0) atomicExch(&g_conv_status, 2);
   __syncthreads();
   if (warp == 0) tmem_dealloc(tmem, kTcCols);
 }
@@ -395,12 +439,23 @@ bool conv_tensor_map(const tlgb_conv3d_desc* d, const void* x, CUtensorMap* map)
              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+int sm_count() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      n = 152;
+  }
+  return n;
+}
+
 template <int MODE, bool OUTF32>
 int launch_conv_tc(const tlgb_conv3d_desc* d, const CUtensorMap& map, const void* w, const void* aux, void* y,
                    cudaStream_t s) {
   auto* k = conv3d_tc_kernel<MODE, OUTF32>;
   TLGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem));
-  dim3 grid((unsigned)((d->W + kTcM - 1) / kTcM), (unsigned)d->H, (unsigned)d->D);
+  const long long units = (long long)d->D * ((d->W + kTcM - 1) / kTcM) * ((d->H + kTcRows - 1) / kTcRows);
+  const unsigned grid = (unsigned)std::min<long long>(units, 3ll * sm_count());  // 3 CTAs of 66 KB per SM
   k<<<grid, 128, kTcSmem, s>>>(map, d->D, d->H, d->W, (const uint4*)w, (const __nv_bfloat16*)aux, y);
   TLGB_CHECK_LAUNCH();
   return TLGB_OK;
