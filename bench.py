@@ -513,7 +513,7 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-blocks", action="store_true")
     ap.add_argument("--skip-cg", action="store_true", help="skip the learned vs plain CG comparison")
-    ap.add_argument("--cg-steps", type=int, default=300, help="preconditioner training steps (4 samples each)")
+    ap.add_argument("--cg-steps", type=int, default=500, help="preconditioner training steps (4 samples each)")
     ap.add_argument("--grid", type=int, default=N_GRID, help="grid edge (smaller cases for profiling)")
     ap.add_argument("--points", type=int, default=N_PTS, help="number of points (smaller cases for profiling)")
     args = ap.parse_args()

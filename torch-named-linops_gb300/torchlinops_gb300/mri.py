@@ -86,13 +86,22 @@ def ellipsoid_phantom_3d(n: int, n_ellipsoids: int = 10, gen: Optional[torch.Gen
     return img
 
 
+def _noise(n: int, gen: torch.Generator, device) -> Tensor:
+    """Complex white noise [n, n, n], drawn on the device by a generator that
+    the CPU generator ``gen`` seeds (reproducible, and no host-side volume)."""
+    seed = int(torch.randint(0, 2**62, (1,), generator=gen))
+    dev = torch.device(device)
+    g = torch.Generator(device=dev).manual_seed(seed)
+    return torch.randn(n, n, n, dtype=torch.complex64, generator=g, device=dev)
+
+
 def random_error_field(n: int, gen: torch.Generator, device="cpu", a_max: float = 2.0, band: float = 0.5) -> Tensor:
     """A CG-error-like field: a random phantom plus a Gaussian random field
     with a random power-law spectrum |k|^-a, a in [0, a_max], restricted to
     |k| <= band * n (the ball a radial trajectory samples)."""
     ph = ellipsoid_phantom_3d(n, 10, gen, device)
     a = a_max * float(torch.rand(1, generator=gen))
-    noise = torch.complex(torch.randn(n, n, n, generator=gen), torch.randn(n, n, n, generator=gen)).to(device)
+    noise = _noise(n, gen, device)
     k = torch.fft.fftfreq(n, device=device) * n
     KX, KY, KZ = torch.meshgrid(k, k, k, indexing="ij")
     kr = torch.sqrt(KX**2 + KY**2 + KZ**2)
@@ -106,7 +115,7 @@ def random_error_field(n: int, gen: torch.Generator, device="cpu", a_max: float 
 def shell_field(n: int, gen: torch.Generator, k_lo: float, k_hi: float, device="cpu") -> Tensor:
     """Complex white noise restricted to the k-space shell k_lo <= |k| < k_hi
     (grid units), unit norm."""
-    noise = torch.complex(torch.randn(n, n, n, generator=gen), torch.randn(n, n, n, generator=gen)).to(device)
+    noise = _noise(n, gen, device)
     k = torch.fft.fftfreq(n, device=device) * n
     KX, KY, KZ = torch.meshgrid(k, k, k, indexing="ij")
     kr = torch.sqrt(KX**2 + KY**2 + KZ**2)
