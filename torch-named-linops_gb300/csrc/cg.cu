@@ -17,7 +17,7 @@ namespace tlgb {
 namespace {
 
 constexpr int kDotThreads = 256;
-constexpr int kDotBlocks = 512;  // fixed partial count -> fixed summation order
+constexpr int kDotBlocks = 2048;  // fixed partial count -> fixed summation order (enough CTAs to hide FP64 latency)
 
 __device__ __forceinline__ double2 warp_sum2(double2 v) {
   for (int m = 16; m > 0; m >>= 1) {
@@ -53,11 +53,23 @@ __global__ void __launch_bounds__(kDotThreads) dot_partial_kernel(const float* _
   if (cplx) {
     const float2* x2 = reinterpret_cast<const float2*>(x);
     const float2* y2 = reinterpret_cast<const float2*>(y);
-    for (int64_t i = b + threadIdx.x; i < e; i += kDotThreads) {
+    // two independent accumulators (the FP64 add latency, not bandwidth, bounds this loop)
+    double2 acc2 = make_double2(0.0, 0.0);
+    int64_t i = b + threadIdx.x;
+    for (; i + kDotThreads < e; i += 2 * kDotThreads) {
+      const float2 a = x2[i], c = y2[i], a2 = x2[i + kDotThreads], c2 = y2[i + kDotThreads];
+      acc.x += (double)a.x * c.x + (double)a.y * c.y;
+      acc.y += (double)a.x * c.y - (double)a.y * c.x;
+      acc2.x += (double)a2.x * c2.x + (double)a2.y * c2.y;
+      acc2.y += (double)a2.x * c2.y - (double)a2.y * c2.x;
+    }
+    if (i < e) {
       const float2 a = x2[i], c = y2[i];
       acc.x += (double)a.x * c.x + (double)a.y * c.y;
       acc.y += (double)a.x * c.y - (double)a.y * c.x;
     }
+    acc.x += acc2.x;
+    acc.y += acc2.y;
   } else {
     for (int64_t i = b + threadIdx.x; i < e; i += kDotThreads) acc.x += (double)x[i] * y[i];
   }
