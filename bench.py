@@ -223,7 +223,7 @@ def run_reference(args, world, rank):
         "metric": "3D multicoil gridding+ungridding throughput (256^3 x 8 coils, 2^21 points, KB W=4)",
         "value": value,
         "unit": "point-coil samples/s",
-        "n_gpus": 0,
+        "n_gpus": world,  # the job's GPU count; this arm computes on the host cores only
         "steps": args.steps,
         "warmup": args.warmup,
         "ms_per_step": t * 1e3,
@@ -234,7 +234,8 @@ def run_reference(args, world, rank):
         "data": "synthetic (1/r^2 ball trajectory, N(0,1) complex values), seeded",
         "config": {"workload": f"interp3d_{N_GRID}cube_{N_COIL}coil_{N_PTS}pts", "grid": [N_GRID] * 3, "coils": N_COIL,
                    "points": N_PTS, "width": WIDTH, "oversamp": OVERSAMP, "sample_points": args.ref_sample,
-                   "step": "ungrid + grid of the sample points on the CPU (reference torch path, restated)"},
+                   "step": "ungrid + grid of the sample points on the CPU (reference torch path, restated)",
+                   "device": "host CPU"},
         "cpu_baseline": {k: desc[k] for k in ("cores", "kind", "sample")} | {"value": value, "unit": "point-coil samples/s"},
         "e2e": {"value": value, "unit": "point-coil samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
