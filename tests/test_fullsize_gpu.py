@@ -1,0 +1,110 @@
+"""Parity at the benchmark sizes through size-independent properties.
+
+* 3D interpolation at the headline workload (256^3 x 8 coils complex64,
+  2^21 points in a 1/r^2 ball, KB W=4): the adjoint identity in float64,
+  linearity of gridding, bit-identical repeats, and the oracle on a sample
+  of points (ungrid) and on a sample of output voxels (grid).
+* ArrayToBlocks / BlocksToArray at 16 x 160^3 complex64, block 8^3, stride
+  4: unfold against direct indexing on sampled blocks, and fold(unfold(x))
+  against x added to itself once per covering block, in the same order
+  (bit-exact).
+"""
+
+import math
+
+import pytest
+import torch
+
+from conftest import rel_l2
+from oracle import interp as OI
+
+import torchlinops_gb300 as T
+
+pytestmark = pytest.mark.gpu
+DEV = "cuda"
+N, C, P = 256, 8, 1 << 21
+
+
+@pytest.fixture(scope="module")
+def interp_case():
+    g = torch.Generator().manual_seed(0)
+    r = torch.rand(P, generator=g) * (N / 2)
+    u = torch.randn(P, 3, generator=g)
+    locs = (N / 2 + r[:, None] * u / u.norm(dim=-1, keepdim=True)).to(torch.float32)
+    gd = torch.Generator(device=DEV).manual_seed(1)
+    img = torch.randn(C, N, N, N, dtype=torch.complex64, device=DEV, generator=gd)
+    vals = torch.randn(C, P, dtype=torch.complex64, device=DEV, generator=gd)
+    beta = OI.nufft_beta(4.0, 1.25)
+    return locs, locs.to(DEV), img, vals, beta
+
+
+def test_fullsize_adjoint_identity_and_determinism(interp_case):
+    locs_h, locs, img, vals, beta = interp_case
+    kp = dict(beta=beta)
+    y = T.ungrid(img, locs, 4.0, kernel_params=kp)
+    g1 = T.grid(vals, locs, (N, N, N), 4.0, kernel_params=kp)
+    lhs = torch.vdot(y.flatten().to(torch.complex128), vals.flatten().to(torch.complex128))
+    rhs = torch.vdot(img.flatten().to(torch.complex128), g1.flatten().to(torch.complex128))
+    assert abs(complex(lhs - rhs)) / abs(complex(lhs)) < 1e-5
+    g2 = T.grid(vals, locs, (N, N, N), 4.0, kernel_params=kp)
+    assert torch.equal(g1, g2)  # fixed summation order, no atomics
+    del g2
+    # linearity: grid(2 v1 + v2) = 2 grid(v1) + grid(v2)
+    v2 = torch.roll(vals, 1, dims=0)
+    g3 = T.grid(2 * vals + v2, locs, (N, N, N), 4.0, kernel_params=kp)
+    ref = 2 * g1 + T.grid(v2, locs, (N, N, N), 4.0, kernel_params=kp)
+    num = torch.linalg.vector_norm((g3 - ref).flatten().to(torch.complex128))
+    assert float(num / torch.linalg.vector_norm(ref.flatten().to(torch.complex128))) < 1e-6
+
+
+def test_fullsize_ungrid_matches_oracle_on_a_sample(interp_case):
+    locs_h, locs, img, vals, beta = interp_case
+    y = T.ungrid(img, locs, 4.0, kernel_params=dict(beta=beta))
+    idx = torch.randperm(P, generator=torch.Generator().manual_seed(2))[:3000]
+    ref = OI.ungrid(img.cpu(), locs_h[idx], 4.0, beta=beta)
+    assert rel_l2(y[:, idx].cpu(), ref) < 1e-5
+
+
+def test_fullsize_grid_matches_oracle_on_sampled_voxels(interp_case):
+    """Voxels near the dense centre and in the sparse shell: the oracle grids
+    only the points whose windows reach them."""
+    locs_h, locs, img, vals, beta = interp_case
+    g = T.grid(vals, locs, (N, N, N), 4.0, kernel_params=dict(beta=beta))
+    for centre in ((128, 128, 128), (128, 128, 20), (60, 200, 128)):
+        c = torch.tensor(centre, dtype=torch.float32)
+        near = (locs_h - c).abs().max(dim=-1).values < 6  # windows reaching the 4^3 block below
+        pts = torch.nonzero(near).flatten()
+        sub = OI.grid(vals[:, pts].cpu(), locs_h[pts], (N, N, N), 4.0, beta=beta)
+        sl = tuple(slice(int(v) - 2, int(v) + 2) for v in centre)
+        assert rel_l2(g[(slice(None),) + sl].cpu(), sub[(slice(None),) + sl]) < 1e-5
+
+
+def test_fullsize_unfold_fold():
+    B, S, shape = (8, 8, 8), (4, 4, 4), (16, 160, 160, 160)
+    gd = torch.Generator(device=DEV).manual_seed(3)
+    x = torch.randn(shape, dtype=torch.complex64, device=DEV, generator=gd)
+    y = T.unfold(x, B, S)
+    nb = tuple((s - b) // st + 1 for s, b, st in zip(shape[1:], B, S))
+    assert tuple(y.shape) == (16, *nb, *B)
+    gen = torch.Generator().manual_seed(4)
+    for _ in range(20):
+        n = int(torch.randint(0, 16, (1,), generator=gen))
+        b = [int(torch.randint(0, k, (1,), generator=gen)) for k in nb]
+        blk = x[n, b[0] * 4:b[0] * 4 + 8, b[1] * 4:b[1] * 4 + 8, b[2] * 4:b[2] * 4 + 8]
+        assert torch.equal(y[n, b[0], b[1], b[2]], blk)
+    z = T.fold(y, shape[1:], B, S)
+    del y
+    # every element is added once per covering block, starting from zero, in
+    # ascending block order: the same float additions as acc += x, cnt times
+    cnt = torch.ones(shape[1:], device=DEV)
+    for d in range(3):
+        i = torch.arange(shape[1 + d], device=DEV)
+        lo = torch.clamp(torch.div(i - 8, 4, rounding_mode="floor") + 1, min=0)
+        hi = torch.clamp(torch.div(i, 4, rounding_mode="floor"), max=nb[d] - 1)
+        c = (hi - lo + 1).to(torch.float32)
+        cnt = cnt * c.reshape([-1 if k == d else 1 for k in range(3)])
+    acc = torch.zeros_like(x)
+    for k in range(int(cnt.max())):
+        acc = torch.where(cnt > k, acc + x, acc)
+    assert torch.equal(z, acc)
+    assert torch.equal(T.fold(T.unfold(x, B, S), shape[1:], B, S), z)  # deterministic
