@@ -101,7 +101,8 @@ typedef struct tlgb_interp_plan_info {
 } tlgb_interp_plan_info;
 
 /* Bytes of device memory needed by a plan for this description (worst case)
- * and of temporary device memory needed only while it is built. */
+ * and of temporary device memory needed only while it is built. Plan and
+ * scratch buffers are 16-byte aligned (cudaMalloc gives 256). */
 int tlgb_interp_plan_size(const tlgb_interp_desc* d, size_t* plan_bytes, size_t* tmp_bytes);
 
 /* Bin the points: sort (point, tile) pairs by output tile (stable, so points
@@ -124,7 +125,10 @@ int tlgb_interp_forward(const tlgb_interp_desc* d, const tlgb_interp_plan_info* 
 /* grid[b, v] = sum over points p with v in their window of w(p, v) * vals[b, p]
  * (gridding). Every element of `grid` is written (no accumulation into the
  * caller's contents); the summation order is fixed, so results are
- * bit-identical run to run; no global atomics. */
+ * bit-identical run to run; no global atomics. Output tiles with more pairs
+ * than one work item holds are summed in parts of at most `chunk` pairs, and
+ * the parts are added in a fixed order with compensated (Kahan-Neumaier)
+ * summation. */
 int tlgb_interp_adjoint(const tlgb_interp_desc* d, const tlgb_interp_plan_info* info, const void* plan,
                         const float* locs, const void* vals, void* grid, void* scratch, size_t scratch_bytes,
                         tlgb_stream_t stream);

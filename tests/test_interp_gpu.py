@@ -134,6 +134,40 @@ def test_eight_entry_3d_paths_against_oracle(shape, nb, pad):
     assert rel_l2(adj, o32a) < TOL and rel_l2(adj, o64a) < TOL
 
 
+@pytest.mark.parametrize("kernel", ["kaiser_bessel", "spline"])
+def test_grid_nonfinite_values_stay_in_their_windows(kernel):
+    """A NaN or Inf point value turns exactly the cells of its window
+    non-finite (its valid taps, zero-weight ones included) and no other cell:
+    the 3D 8-entry path, whose rows of tap weights hold zeros outside a
+    window, sends such points through the per-tap path. The reference's own
+    torch path multiplies every tap of the ceil(W+1)^3 patch by the value,
+    masked taps included (grid.py:624, weights * mask * val), so there a NaN
+    reaches the whole patch: a superset of the window."""
+    gen = torch.Generator().manual_seed(9)
+    shape = (32, 32, 32)
+    locs = _ball_locs(20000, 12.0, torch.tensor([16.0, 16.0, 16.0]), gen)
+    pts = torch.complex(torch.randn(8, 20000, generator=gen), torch.randn(8, 20000, generator=gen))
+    bad = [(3, 17, complex(float("nan"), 0.0)), (5, 900, complex(float("inf"), 1.0)),
+           (0, 4000, complex(0.0, float("-inf")))]
+    for c, p, v in bad:
+        pts[c, p] = v
+    beta = OI.nufft_beta(4.0, 1.25)
+    out = T.grid(pts.to(DEV), locs.to(DEV), shape, 4.0, kernel=kernel, kernel_params=dict(beta=beta)).cpu()
+    ref = OI.grid(pts, locs, shape, 4.0, kernel=kernel, beta=beta)
+    window = torch.zeros(8, *shape, dtype=torch.bool)
+    for c, p, _ in bad:
+        taps = []
+        for e in range(3):
+            g, _d, ok = OI.axis_taps(locs[p : p + 1, e], 4.0, kernel, torch.float32)
+            taps.append(g[0][ok[0]] % shape[e])
+        for x, y, z in torch.cartesian_prod(*taps).tolist():
+            window[c, x, y, z] = True
+    assert torch.equal(~torch.isfinite(out), window)
+    assert bool((~torch.isfinite(ref))[window].all())
+    fin = torch.isfinite(ref)
+    assert rel_l2(out[fin], ref[fin]) < TOL
+
+
 def test_gridding_is_deterministic():
     gen = torch.Generator().manual_seed(5)
     locs = _ball_locs(200000, 33, 32, gen).to(DEV)

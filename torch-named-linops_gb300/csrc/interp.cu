@@ -1044,6 +1044,15 @@ __device__ __forceinline__ PRec load_prec(const PRec* __restrict__ recs, long lo
   return R;
 }
 
+// Compensated summation (Neumaier's variant of Kahan's method): s + c
+// carries the running sum; c collects the low-order bits each addition
+// loses, whichever operand is larger.
+__device__ __forceinline__ void comp_add(float& s, float& c, float x) {
+  const float t = s + x;
+  c += fabsf(s) >= fabsf(x) ? (s - t) + x : (x - t) + s;
+  s = t;
+}
+
 __device__ __forceinline__ float pick4(const float4& v, int i) {
   return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
 }
@@ -1109,8 +1118,9 @@ __device__ __forceinline__ void write_tile_rows(const Geo& g, const float* acc, 
   }
 }
 
-// Sum the partial tiles of one split tile (8^3 x 8 entries) in slot order:
-// coalesced float4 reads, the sum staged in shared memory, then the same
+// Sum the partial tiles of one split tile (8^3 x 8 entries) in slot order,
+// compensated (the dense k-space centre piles thousands of points onto a
+// cell; each partial holds at most one chunk of them): coalesced float4 reads, the sum staged in shared memory, then the same
 // row-wise write-out as an unsplit tile.
 __global__ void __launch_bounds__(256) adj_reduce_f3_kernel(Geo g, const int4* __restrict__ split,
                                                             const float* __restrict__ partial,
@@ -1130,37 +1140,74 @@ __global__ void __launch_bounds__(256) adj_reduce_f3_kernel(Geo g, const int4* _
     o[0] = (t / g.nt[1]) * 8;
   }
   const int tid = threadIdx.x;
-  float4 sum[TFL / 4 / 256];
+  float4 sum[TFL / 4 / 256], comp[TFL / 4 / 256];
   const float4* src = reinterpret_cast<const float4*>(partial + ((long long)sp.y * ncg + cg) * TFL) + tid;
 #pragma unroll
-  for (int i = 0; i < TFL / 4 / 256; ++i) sum[i] = __ldg(src + i * 256);
+  for (int i = 0; i < TFL / 4 / 256; ++i) {
+    sum[i] = __ldg(src + i * 256);
+    comp[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
   for (int k = 1; k < sp.z; ++k) {
     const float4* q = reinterpret_cast<const float4*>(partial + ((long long)(sp.y + k) * ncg + cg) * TFL) + tid;
 #pragma unroll
     for (int i = 0; i < TFL / 4 / 256; ++i) {
       const float4 v = __ldg(q + i * 256);
-      sum[i].x += v.x;
-      sum[i].y += v.y;
-      sum[i].z += v.z;
-      sum[i].w += v.w;
+      comp_add(sum[i].x, comp[i].x, v.x);
+      comp_add(sum[i].y, comp[i].y, v.y);
+      comp_add(sum[i].z, comp[i].z, v.z);
+      comp_add(sum[i].w, comp[i].w, v.w);
     }
   }
 #pragma unroll
-  for (int i = 0; i < TFL / 4 / 256; ++i) reinterpret_cast<float4*>(acc)[tid + i * 256] = sum[i];
+  for (int i = 0; i < TFL / 4 / 256; ++i)
+    reinterpret_cast<float4*>(acc)[tid + i * 256] =
+        make_float4(sum[i].x + comp[i].x, sum[i].y + comp[i].y, sum[i].z + comp[i].z, sum[i].w + comp[i].w);
   __syncthreads();
   write_tile_rows(g, acc, o, tid >> 5, tid & 31, c0, ncoil, gridv);
 }
 
-// Gridding: CTA = 8 warps owning one 8^3 x 8-entry output tile
-// ([x][y][z][entry], 16 floats per cell); warp w owns the cells of x-plane w,
-// so no two warps write the same cell. Entries are staged in batches of kAB
-// (records built one dimension per thread, point values, and per plane a
-// bitmask of the entries with taps in it); each warp applies its plane's
-// entries in plan order, so every cell is updated in the same order on every
-// run. Lanes = (entry pair, z-tap parity, y-tap).
-constexpr int kAB = 128;
+// Packed single-precision arithmetic of sm_100+ (two independent IEEE fp32
+// operations, round to nearest: the same results as two scalar ones).
+__device__ __forceinline__ unsigned long long f2_bits(float2 v) { return *reinterpret_cast<unsigned long long*>(&v); }
+__device__ __forceinline__ float2 bits_f2(unsigned long long b) { return *reinterpret_cast<float2*>(&b); }
+// acc += (w, w) * v
+__device__ __forceinline__ void fma2_bcast(float2& acc, float w, float2 v) {
+  unsigned long long a = f2_bits(acc);
+  asm("fma.rn.f32x2 %0, %1, %2, %0;" : "+l"(a) : "l"(f2_bits(make_float2(w, w))), "l"(f2_bits(v)));
+  acc = bits_f2(a);
+}
+// (s, s) * v
+__device__ __forceinline__ float2 mul2_bcast(float s, float2 v) {
+  unsigned long long r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_bits(make_float2(s, s))), "l"(f2_bits(v)));
+  return bits_f2(r);
+}
 
-__global__ void __launch_bounds__(256, 4) adj_f3_kernel(Geo g, const int4* __restrict__ items,
+// Gridding: CTA = 8 warps owning one 8^3 x 8-entry output tile, held in
+// registers: warp w owns x-plane w, lane (y, entry quad, z pair) the cells
+// (w, y, z) for z in {2 zp, 2 zp + 1, 2 zp + 4, 2 zp + 5} and 4 of the 8
+// entries, so no two threads update the same value. Entries are staged in
+// batches of kAB, one thread per entry: its 8 point values, its view of the
+// tile turned into three rows of tap weights (8 per dimension, zero where
+// the window has no tap), and per plane a bitmask of the entries with taps
+// in it (warp ballots). Each warp then applies its plane's entries in plan
+// order, one packed (re, im) FMA per cell and entry, then the entries that
+// need the generic record, also in order. The finished tile goes through
+// shared memory to coalesced row stores.
+constexpr int kAB = 256;
+
+struct AdjStage {
+  float wrow[kAB][24];  // tap weights at tile-local x (0-7), y (8-15), z (16-23)
+  float pv[kAB][16];    // point values, 8 entries complex
+  int pidx[kAB];
+  unsigned fmask[8][kAB / 32];  // per plane: entries on the row path with taps there
+  unsigned smask[kAB / 32];     // entries on the generic path (all planes)
+};
+static_assert(sizeof(AdjStage) >= 512 * 16 * sizeof(float), "the staging area holds the finished tile");
+
+constexpr size_t adj_f3_smem() { return sizeof(AdjStage) + 8 * sizeof(Rec<5>); }
+
+__global__ void __launch_bounds__(256, 3) adj_f3_kernel(Geo g, const int4* __restrict__ items,
                                                         const int32_t* __restrict__ entries,
                                                         const PRec* __restrict__ precs,
                                                         const float* __restrict__ locs, const float* __restrict__ vals,
@@ -1168,11 +1215,8 @@ __global__ void __launch_bounds__(256, 4) adj_f3_kernel(Geo g, const int4* __res
                                                         float* __restrict__ partial) {
   constexpr int CG = 8, VS = 16, TFL = 512 * 16, NW = 8, MW = kAB / 32;
   extern __shared__ __align__(128) unsigned char smem[];
-  float* acc = reinterpret_cast<float*>(smem);                   // [8][8][8][16]
-  R3* rec = reinterpret_cast<R3*>(smem + TFL * sizeof(float));  // [kAB]
-  float* pv = reinterpret_cast<float*>(rec + kAB);              // [kAB][16]
-  Rec<5>* slow = reinterpret_cast<Rec<5>*>(pv + kAB * VS);      // [NW]
-  unsigned* pmask = reinterpret_cast<unsigned*>(slow + NW);     // [NW][MW]
+  AdjStage& S = *reinterpret_cast<AdjStage*>(smem);
+  Rec<5>* slow = reinterpret_cast<Rec<5>*>(smem + sizeof(AdjStage));  // [NW]
   const int4 it = items[blockIdx.x];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int cg = blockIdx.y;
@@ -1186,129 +1230,159 @@ __global__ void __launch_bounds__(256, 4) adj_f3_kernel(Geo g, const int4* __res
     o[1] = (t % g.nt[1]) * 8;
     o[0] = (t / g.nt[1]) * 8;
   }
-  for (int i = tid * 4; i < TFL; i += 256 * 4) *reinterpret_cast<float4*>(acc + i) = make_float4(0.f, 0.f, 0.f, 0.f);
-  const int cu = lane & 3, kzl = (lane >> 2) & 1, ky = lane >> 3;
+  const int y = lane >> 2, cq = (lane >> 1) & 1, zp = lane & 1;
+  float2 acc[4][4];  // [z slot: 2zp, 2zp+1, 2zp+4, 2zp+5][entry 4cq + k]
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+#pragma unroll
+    for (int k = 0; k < 4; ++k) acc[q][k] = make_float2(0.f, 0.f);
   for (int b = it.y; b < it.z; b += kAB) {
     const int nb = min(kAB, it.z - b);
     __syncthreads();  // the previous batch has been applied
-    if (tid < kAB) {
-      // warps 0..3: entry tid's record and view, then per plane a ballot of
-      // the entries whose x taps reach it (all planes for the generic path)
+    {
+      // entry tid: record and point values -> view -> rows of tap weights;
+      // ballots per plane. Entries with a non-finite value take the generic
+      // path, which touches only the cells of the window, as the row path's
+      // zero weights would not keep a NaN or Inf out of the other cells.
       unsigned view = 0;
+      bool finite = true;
       if (tid < nb) {
-        const long long p = entries[b + tid];
+        const int p = entries[b + tid];
         const PRec R = load_prec(precs, p);
+        float4 v[4];
+        if (tv) {
+          const float4* src = tv + ((long long)cg * g.npts + p) * 4;
+#pragma unroll
+          for (int q = 0; q < 4; ++q) v[q] = __ldg(src + q);
+        } else {
+          const float2* v2 = reinterpret_cast<const float2*>(vals);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const int c = 2 * q;
+            const float2 a = c < ncoil ? __ldg(v2 + (long long)(c0 + c) * g.npts + p) : make_float2(0.f, 0.f);
+            const float2 d = c + 1 < ncoil ? __ldg(v2 + (long long)(c0 + c + 1) * g.npts + p) : make_float2(0.f, 0.f);
+            v[q] = make_float4(a.x, a.y, d.x, d.y);
+          }
+        }
+        float4* pd = reinterpret_cast<float4*>(&S.pv[tid][0]);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          pd[q] = v[q];
+          finite = finite && isfinite(v[q].x) && isfinite(v[q].y) && isfinite(v[q].z) && isfinite(v[q].w);
+        }
         view = grid_view(g, R, o);
-        R3& S = rec[tid];
-        S.w[0] = R.w[0];
-        S.w[1] = R.w[1];
-        S.w[2] = R.w[2];
-        S.view = view;
-        S.p = (int)p;
+        S.pidx[tid] = p;
+        if (((view >> 27) & 1) && finite) {
+#pragma unroll
+          for (int e = 0; e < 3; ++e) {
+            const unsigned u = (view >> (9 * e)) & 511;
+            const int f = u & 7, m = (u >> 3) & 7, k0 = u >> 6;
+            float r[8];
+#pragma unroll
+            for (int l = 0; l < 8; ++l) {
+              const int k = l - f;
+              r[l] = (k >= 0 && k < m) ? pick4(R.w[e], k0 + k) : 0.f;
+            }
+            float4* d = reinterpret_cast<float4*>(&S.wrow[tid][8 * e]);
+            d[0] = make_float4(r[0], r[1], r[2], r[3]);
+            d[1] = make_float4(r[4], r[5], r[6], r[7]);
+          }
+        }
       }
-      const bool okx = (view >> 28) & 1, fastx = (view >> 27) & 1;
+      const bool ok = (view >> 28) & 1, fast = ((view >> 27) & 1) && finite;
       const int f = view & 7, n = (view >> 3) & 7;
 #pragma unroll
       for (int w = 0; w < NW; ++w) {
-        const unsigned bal = __ballot_sync(0xffffffffu, okx && (!fastx || (w >= f && w < f + n)));
-        if (lane == 0) pmask[w * MW + (tid >> 5)] = bal;
+        const unsigned bal = __ballot_sync(0xffffffffu, ok && fast && w >= f && w < f + n);
+        if (lane == 0) S.fmask[w][warp] = bal;
       }
-    }
-    for (int j = tid >> 1; j < nb; j += 128) {
-      // point values of the batch: two threads per entry, 4 entries each
-      const long long p = entries[b + j];
-      const int h = tid & 1;
-      float4* d = reinterpret_cast<float4*>(pv + j * VS) + 2 * h;
-      if (tv) {
-        const float4* src = tv + ((long long)cg * g.npts + p) * 4 + 2 * h;
-        d[0] = __ldg(src);
-        d[1] = __ldg(src + 1);
-        continue;
-      }
-#pragma unroll
-      for (int q = 0; q < 2; ++q) {
-        const int c = 4 * h + 2 * q;
-        const float2 v0 = c < ncoil ? __ldg(reinterpret_cast<const float2*>(vals) + (long long)(c0 + c) * g.npts + p)
-                                    : make_float2(0.f, 0.f);
-        const float2 v1 = c + 1 < ncoil
-                              ? __ldg(reinterpret_cast<const float2*>(vals) + (long long)(c0 + c + 1) * g.npts + p)
-                              : make_float2(0.f, 0.f);
-        d[q] = make_float4(v0.x, v0.y, v1.x, v1.y);
-      }
+      const unsigned bs = __ballot_sync(0xffffffffu, ok && !fast);
+      if (lane == 0) S.smask[warp] = bs;
     }
     __syncthreads();
+    // row path: every lane updates its 4 cells x 4 entries (zero weights
+    // outside the window)
 #pragma unroll 1
     for (int mw = 0; mw < MW; ++mw) {
-      unsigned bits = pmask[warp * MW + mw];
+      unsigned bits = S.fmask[warp][mw];
       while (bits) {
         const int j = mw * 32 + __ffs(bits) - 1;
         bits &= bits - 1;
-        __syncwarp();  // consecutive entries may share cells of this plane
-        const R3& R = rec[j];
-        const unsigned view = R.view;
-        if ((view >> 27) & 1) {
-          // plain runs: x taps k0x + t, y taps k0y + ky, z taps k0z + kz
-          const int t = warp - (int)(view & 7);  // in [0, mx) by the mask
-          const unsigned vy = (view >> 9) & 511, vz = (view >> 18) & 511;
-          const int fy = vy & 7, my = (vy >> 3) & 7, k0y = vy >> 6;
-          const int fz = vz & 7, mz = (vz >> 3) & 7, k0z = vz >> 6;
-          if (ky < my) {
-            const float wxy = (&R.w[0].x)[((view >> 6) & 7) + t] * (&R.w[1].x)[k0y + ky];
-            const float4 v = *reinterpret_cast<const float4*>(pv + j * VS + cu * 4);
-            float* a = acc + (((warp * 8 + fy + ky) * 8 + fz + kzl) * VS) + cu * 4;
-            const bool z0 = kzl < mz, z1 = kzl + 2 < mz;
-            float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = r0;
-            if (z0) r0 = *reinterpret_cast<const float4*>(a);
-            if (z1) r1 = *reinterpret_cast<const float4*>(a + 2 * VS);
-            if (z0) {
-              const float w = wxy * (&R.w[2].x)[k0z + kzl];
-              r0.x = fmaf(w, v.x, r0.x); r0.y = fmaf(w, v.y, r0.y); r0.z = fmaf(w, v.z, r0.z); r0.w = fmaf(w, v.w, r0.w);
-              *reinterpret_cast<float4*>(a) = r0;
-            }
-            if (z1) {
-              const float w = wxy * (&R.w[2].x)[k0z + kzl + 2];
-              r1.x = fmaf(w, v.x, r1.x); r1.y = fmaf(w, v.y, r1.y); r1.z = fmaf(w, v.z, r1.z); r1.w = fmaf(w, v.w, r1.w);
-              *reinterpret_cast<float4*>(a + 2 * VS) = r1;
-            }
-          }
-          continue;
+        const float* wr = S.wrow[j];
+        const float wxy = wr[warp] * wr[8 + y];
+        const float2 za = *reinterpret_cast<const float2*>(wr + 16 + 2 * zp);
+        const float2 zb = *reinterpret_cast<const float2*>(wr + 20 + 2 * zp);
+        const float2 wa = mul2_bcast(wxy, za), wb = mul2_bcast(wxy, zb);
+        const float4 v0 = *reinterpret_cast<const float4*>(&S.pv[j][8 * cq]);
+        const float4 v1 = *reinterpret_cast<const float4*>(&S.pv[j][8 * cq + 4]);
+        const float2 v[4] = {make_float2(v0.x, v0.y), make_float2(v0.z, v0.w), make_float2(v1.x, v1.y),
+                             make_float2(v1.z, v1.w)};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          fma2_bcast(acc[0][k], wa.x, v[k]);
+          fma2_bcast(acc[1][k], wa.y, v[k]);
+          fma2_bcast(acc[2][k], wb.x, v[k]);
+          fma2_bcast(acc[3][k], wb.y, v[k]);
         }
-        if (!((view >> 28) & 1)) continue;  // no valid tap
-        // exact-integer coordinates (5 taps) or a window wrapping inside the
-        // tile: generic record, this plane's taps in order by 4 lanes
+      }
+    }
+    // generic path: exact-integer coordinates (5 taps) or a window wrapping
+    // inside the tile; the record is rebuilt from the coordinates by lane 0
+#pragma unroll 1
+    for (int mw = 0; mw < MW; ++mw) {
+      unsigned bits = S.smask[mw];
+      while (bits) {
+        const int j = mw * 32 + __ffs(bits) - 1;
+        bits &= bits - 1;
+        __syncwarp();  // the previous record has been read
         if (lane == 0) {
           float x3[3];
-          for (int e = 0; e < 3; ++e) x3[e] = load_coord(g, locs, R.p, e);
+          for (int e = 0; e < 3; ++e) x3[e] = load_coord(g, locs, S.pidx[j], e);
           lane_rec<5>(g, x3, o, false, slow[warp]);
         }
         __syncwarp();
-        const Rec<5>& S = slow[warp];
-        if (lane < 4) {
-          const float4 vv = *reinterpret_cast<const float4*>(pv + j * VS + lane * 4);
-          for (int kx = 0; kx < S.m[0]; ++kx) {
-            if (S.lc[0][kx] != warp) continue;
-            for (int kyy = 0; kyy < S.m[1]; ++kyy)
-              for (int kz = 0; kz < S.m[2]; ++kz) {
-                const float w = g.norm == 1 ? S.wv[0][kx] * S.wv[1][kyy] * S.wv[2][kz]
-                                            : radial_w(g, S.wv[0][kx], S.wv[1][kyy], S.wv[2][kz]);
-                float* a = acc + ((warp * 8 + S.lc[1][kyy]) * 8 + S.lc[2][kz]) * VS + lane * 4;
-                float4 r = *reinterpret_cast<float4*>(a);
-                r.x = fmaf(w, vv.x, r.x); r.y = fmaf(w, vv.y, r.y); r.z = fmaf(w, vv.z, r.z); r.w = fmaf(w, vv.w, r.w);
-                *reinterpret_cast<float4*>(a) = r;
+        const Rec<5>& Q = slow[warp];
+        const float4 v0 = *reinterpret_cast<const float4*>(&S.pv[j][8 * cq]);
+        const float4 v1 = *reinterpret_cast<const float4*>(&S.pv[j][8 * cq + 4]);
+        const float2 v[4] = {make_float2(v0.x, v0.y), make_float2(v0.z, v0.w), make_float2(v1.x, v1.y),
+                             make_float2(v1.z, v1.w)};
+        for (int kx = 0; kx < Q.m[0]; ++kx) {
+          if (Q.lc[0][kx] != warp) continue;
+          for (int kyy = 0; kyy < Q.m[1]; ++kyy) {
+            if (Q.lc[1][kyy] != y) continue;
+            for (int kz = 0; kz < Q.m[2]; ++kz) {
+              const int z = Q.lc[2][kz];
+              const float w = g.norm == 1 ? Q.wv[0][kx] * Q.wv[1][kyy] * Q.wv[2][kz]
+                                          : radial_w(g, Q.wv[0][kx], Q.wv[1][kyy], Q.wv[2][kz]);
+#pragma unroll
+              for (int q = 0; q < 4; ++q) {
+                if (z != 2 * zp + (q & 1) + 4 * (q >> 1)) continue;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) fma2_bcast(acc[q][k], w, v[k]);
               }
+            }
           }
         }
       }
     }
+  }
+  __syncthreads();  // the staging area becomes the [x][y][z][entry] tile
+  float* tile = reinterpret_cast<float*>(smem);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int z = 2 * zp + (q & 1) + 4 * (q >> 1);
+    float4* d = reinterpret_cast<float4*>(tile + ((warp * 8 + y) * 8 + z) * VS + 8 * cq);
+    d[0] = make_float4(acc[q][0].x, acc[q][0].y, acc[q][1].x, acc[q][1].y);
+    d[1] = make_float4(acc[q][2].x, acc[q][2].y, acc[q][3].x, acc[q][3].y);
   }
   __syncthreads();
   if (it.w >= 0) {
     float* dst = partial + ((long long)it.w * gridDim.y + cg) * TFL;
     for (int i = tid * 4; i < TFL; i += 256 * 4)
-      *reinterpret_cast<float4*>(dst + i) = *reinterpret_cast<const float4*>(acc + i);
+      *reinterpret_cast<float4*>(dst + i) = *reinterpret_cast<const float4*>(tile + i);
     return;
   }
-  write_tile_rows(g, acc, o, warp, lane, c0, ncoil, gridv);
+  write_tile_rows(g, tile, o, warp, lane, c0, ncoil, gridv);
 }
 
 // Gather: CTA = 8 warps sharing one 12^3 x 8-entry region ([entry][x][y][z],
@@ -1486,7 +1560,8 @@ __global__ void __launch_bounds__(256, 2) fwd_f3_kernel(const __grid_constant__ 
   }
 }
 
-// Sum the partial tiles of one split tile in slot order and write it out.
+// Sum the partial tiles of one split tile in slot order, compensated, and
+// write it out.
 __global__ void __launch_bounds__(NTHR) adj_reduce_kernel(Geo g, const int4* __restrict__ split,
                                                           const float* __restrict__ partial,
                                                           float* __restrict__ gridv, int CG, int ncg) {
@@ -1519,9 +1594,9 @@ __global__ void __launch_bounds__(NTHR) adj_reduce_kernel(Geo g, const int4* __r
     const int gx = tc[0] * g.T[0] + x, gy = tc[1] * g.T[1] + y, gz = tc[2] * g.T[2] + z;
     if (gx >= g.N[0] || gy >= g.N[1] || gz >= g.N[2]) continue;
     const int li = ((x * g.T[1] + y) * g.T[2] + z) * vstride + cc * es + f;
-    float s = partial[((long long)sp.y * ncg + cg) * tfl + li];
-    for (int k = 1; k < sp.z; ++k) s += partial[((long long)(sp.y + k) * ncg + cg) * tfl + li];
-    gridv[((long long)(c0 + cc) * gvol + ((long long)gx * g.N[1] + gy) * g.N[2] + gz) * es + f] = s;
+    float s = partial[((long long)sp.y * ncg + cg) * tfl + li], c = 0.f;
+    for (int k = 1; k < sp.z; ++k) comp_add(s, c, partial[((long long)(sp.y + k) * ncg + cg) * tfl + li]);
+    gridv[((long long)(c0 + cc) * gvol + ((long long)gx * g.N[1] + gy) * g.N[2] + gz) * es + f] = s + c;
   }
 }
 
@@ -2075,9 +2150,11 @@ int launch_fwd_f3(const Geo& g, const tlgb_interp_plan_info* info, const char* P
 int launch_adj_f3(const Geo& g, const tlgb_interp_plan_info* info, const char* P, const float* locs,
                   const void* vals, void* grid, void* scratch, cudaStream_t s) {
   const int64_t ncg = cdiv(g.nbatch, 8);
-  const size_t sm = 512 * 16 * sizeof(float) + kAB * (sizeof(R3) + 16 * sizeof(float)) + 8 * sizeof(Rec<5>) +
-                    8 * (kAB / 32) * sizeof(unsigned);
+  const size_t sm = adj_f3_smem();
   TLGB_TRY(set_smem(adj_f3_kernel, sm));
+  // 16-byte asynchronous copies of the point records and transposed values
+  if (((uintptr_t)(P + info->off_records) & 15) || ((uintptr_t)scratch & 15))
+    TLGB_FAIL(TLGB_ERR_INVALID, "interp adjoint: plan and scratch must be 16-byte aligned");
   const float4* tv = nullptr;
   if (g.tv_off >= 0 && g.npts > 0) {
     float2* t = reinterpret_cast<float2*>(static_cast<char*>(scratch) + g.tv_off);
