@@ -237,6 +237,17 @@ int radix_sort_pairs(uint32_t* keys, int32_t* vals, uint32_t* keys_tmp, int32_t*
   return TLGB_OK;
 }
 
+int sm_count() {
+  static int cache[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+  if (cache[dev] == 0) {
+    int n = 0;
+    cache[dev] = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && n > 0 ? n : 152;
+  }
+  return cache[dev];
+}
+
 }  // namespace tlgb
 
 extern "C" const char* tlgb_last_error(void) { return tlgb::g_last_error.c_str(); }

@@ -66,4 +66,7 @@ int radix_sort_pairs(uint32_t* keys, int32_t* vals, uint32_t* keys_tmp, int32_t*
 // synchronous). tlgb_device_status combines it with the interpolation one.
 int conv_device_status(int* v, int clear);
 
+// Streaming multiprocessors of the current device (cached per device).
+int sm_count();
+
 }  // namespace tlgb

@@ -439,16 +439,6 @@ bool conv_tensor_map(const tlgb_conv3d_desc* d, const void* x, CUtensorMap* map)
              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-int sm_count() {
-  static int n = 0;
-  if (n == 0) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-      n = 152;
-  }
-  return n;
-}
-
 template <int MODE, bool OUTF32>
 int launch_conv_tc(const tlgb_conv3d_desc* d, const CUtensorMap& map, const void* w, const void* aux, void* y,
                    cudaStream_t s) {

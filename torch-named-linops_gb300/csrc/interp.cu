@@ -1192,8 +1192,8 @@ __device__ __forceinline__ float2 mul2_bcast(float s, float2 v) {
 // the window has no tap), and per plane a bitmask of the entries with taps
 // in it (warp ballots). Each warp then applies its plane's entries in plan
 // order, one packed (re, im) FMA per cell and entry, then the entries that
-// need the generic record, also in order. The finished tile goes through
-// shared memory to coalesced row stores.
+// need the generic record, also in order. The finished tile is stored from
+// registers.
 constexpr int kAB = 256;
 
 struct AdjStage {
@@ -1203,7 +1203,6 @@ struct AdjStage {
   unsigned fmask[8][kAB / 32];  // per plane: entries on the row path with taps there
   unsigned smask[kAB / 32];     // entries on the generic path (all planes)
 };
-static_assert(sizeof(AdjStage) >= 512 * 16 * sizeof(float), "the staging area holds the finished tile");
 
 constexpr size_t adj_f3_smem() { return sizeof(AdjStage) + 8 * sizeof(Rec<5>); }
 
@@ -1301,28 +1300,48 @@ __global__ void __launch_bounds__(256, 3) adj_f3_kernel(Geo g, const int4* __res
     }
     __syncthreads();
     // row path: every lane updates its 4 cells x 4 entries (zero weights
-    // outside the window)
+    // outside the window); two entries per step, loads first, updates in
+    // entry order
+    struct Visit {
+      float2 wa, wb;  // weights of the lane's z slots
+      float4 v0, v1;  // the lane's 4 entries, complex
+    };
+    auto fetch = [&](int j) {
+      const float* wr = S.wrow[j];
+      const float wxy = wr[warp] * wr[8 + y];
+      Visit d;
+      d.wa = mul2_bcast(wxy, *reinterpret_cast<const float2*>(wr + 16 + 2 * zp));
+      d.wb = mul2_bcast(wxy, *reinterpret_cast<const float2*>(wr + 20 + 2 * zp));
+      d.v0 = *reinterpret_cast<const float4*>(&S.pv[j][8 * cq]);
+      d.v1 = *reinterpret_cast<const float4*>(&S.pv[j][8 * cq + 4]);
+      return d;
+    };
+    auto apply = [&](const Visit& d) {
+      const float2 v[4] = {make_float2(d.v0.x, d.v0.y), make_float2(d.v0.z, d.v0.w), make_float2(d.v1.x, d.v1.y),
+                           make_float2(d.v1.z, d.v1.w)};
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        fma2_bcast(acc[0][k], d.wa.x, v[k]);
+        fma2_bcast(acc[1][k], d.wa.y, v[k]);
+        fma2_bcast(acc[2][k], d.wb.x, v[k]);
+        fma2_bcast(acc[3][k], d.wb.y, v[k]);
+      }
+    };
 #pragma unroll 1
     for (int mw = 0; mw < MW; ++mw) {
       unsigned bits = S.fmask[warp][mw];
       while (bits) {
-        const int j = mw * 32 + __ffs(bits) - 1;
+        const int j0 = mw * 32 + __ffs(bits) - 1;
         bits &= bits - 1;
-        const float* wr = S.wrow[j];
-        const float wxy = wr[warp] * wr[8 + y];
-        const float2 za = *reinterpret_cast<const float2*>(wr + 16 + 2 * zp);
-        const float2 zb = *reinterpret_cast<const float2*>(wr + 20 + 2 * zp);
-        const float2 wa = mul2_bcast(wxy, za), wb = mul2_bcast(wxy, zb);
-        const float4 v0 = *reinterpret_cast<const float4*>(&S.pv[j][8 * cq]);
-        const float4 v1 = *reinterpret_cast<const float4*>(&S.pv[j][8 * cq + 4]);
-        const float2 v[4] = {make_float2(v0.x, v0.y), make_float2(v0.z, v0.w), make_float2(v1.x, v1.y),
-                             make_float2(v1.z, v1.w)};
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          fma2_bcast(acc[0][k], wa.x, v[k]);
-          fma2_bcast(acc[1][k], wa.y, v[k]);
-          fma2_bcast(acc[2][k], wb.x, v[k]);
-          fma2_bcast(acc[3][k], wb.y, v[k]);
+        const Visit d0 = fetch(j0);
+        if (bits) {
+          const int j1 = mw * 32 + __ffs(bits) - 1;
+          bits &= bits - 1;
+          const Visit d1 = fetch(j1);
+          apply(d0);
+          apply(d1);
+        } else {
+          apply(d0);
         }
       }
     }
@@ -1366,23 +1385,42 @@ __global__ void __launch_bounds__(256, 3) adj_f3_kernel(Geo g, const int4* __res
       }
     }
   }
-  __syncthreads();  // the staging area becomes the [x][y][z][entry] tile
-  float* tile = reinterpret_cast<float*>(smem);
-#pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    const int z = 2 * zp + (q & 1) + 4 * (q >> 1);
-    float4* d = reinterpret_cast<float4*>(tile + ((warp * 8 + y) * 8 + z) * VS + 8 * cq);
-    d[0] = make_float4(acc[q][0].x, acc[q][0].y, acc[q][1].x, acc[q][1].y);
-    d[1] = make_float4(acc[q][2].x, acc[q][2].y, acc[q][3].x, acc[q][3].y);
-  }
-  __syncthreads();
+  // Write-out from registers. A split tile's part goes to its partial slot
+  // in the [x][y][z][entry] layout; a whole tile goes to the grid, where the
+  // lanes of z pairs 0 and 1 write 32 contiguous bytes of an entry's row.
   if (it.w >= 0) {
     float* dst = partial + ((long long)it.w * gridDim.y + cg) * TFL;
-    for (int i = tid * 4; i < TFL; i += 256 * 4)
-      *reinterpret_cast<float4*>(dst + i) = *reinterpret_cast<const float4*>(tile + i);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int z = 2 * zp + (q & 1) + 4 * (q >> 1);
+      float4* d = reinterpret_cast<float4*>(dst + ((warp * 8 + y) * 8 + z) * VS + 8 * cq);
+      d[0] = make_float4(acc[q][0].x, acc[q][0].y, acc[q][1].x, acc[q][1].y);
+      d[1] = make_float4(acc[q][2].x, acc[q][2].y, acc[q][3].x, acc[q][3].y);
+    }
     return;
   }
-  write_tile_rows(g, tile, o, warp, lane, c0, ncoil, gridv);
+  const int gx = o[0] + warp, gy = o[1] + y;
+  if (gx >= g.N[0] || gy >= g.N[1]) return;
+  const long long gvol = (long long)g.N[0] * g.N[1] * g.N[2];
+  // 16-byte stores need an even Z extent (row starts at even elements) and an aligned base
+  const bool vec = o[2] + 8 <= g.N[2] && (g.N[2] & 1) == 0 && (reinterpret_cast<uintptr_t>(gridv) & 15) == 0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int c = 4 * cq + k;
+    if (c >= ncoil) continue;
+    float* row = gridv + ((long long)(c0 + c) * gvol + ((long long)gx * g.N[1] + gy) * g.N[2] + o[2]) * 2;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int z = 2 * zp + 4 * h;  // slots 2h, 2h + 1
+      const float2 a = acc[2 * h][k], b = acc[2 * h + 1][k];
+      if (vec) {
+        *reinterpret_cast<float4*>(row + 2 * z) = make_float4(a.x, a.y, b.x, b.y);
+      } else {
+        if (o[2] + z < g.N[2]) *reinterpret_cast<float2*>(row + 2 * z) = a;
+        if (o[2] + z + 1 < g.N[2]) *reinterpret_cast<float2*>(row + 2 * z + 2) = b;
+      }
+    }
+  }
 }
 
 // Gather: CTA = 8 warps sharing one 12^3 x 8-entry region ([entry][x][y][z],
