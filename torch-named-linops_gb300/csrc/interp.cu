@@ -1089,46 +1089,19 @@ __global__ void __launch_bounds__(256) transpose_vals_kernel(const float2* __res
   }
 }
 
-// Write one x-plane (warp) of an 8^3 x 8-entry tile [x][y][z][entry] (16
-// floats per cell) to the grid: per (x, y) row, lane = (entry, z pair), one
-// 16-byte store per lane, 64 contiguous bytes per entry.
-__device__ __forceinline__ void write_tile_rows(const Geo& g, const float* acc, const int (&o)[3], int x, int lane,
-                                                int c0, int ncoil, float* __restrict__ gridv) {
-  constexpr int VS = 16;
-  const long long gvol = (long long)g.N[0] * g.N[1] * g.N[2];
-  const int gx = o[0] + x;
-  if (gx >= g.N[0]) return;
-  const int c = lane >> 2, zp = lane & 3;
-  // 16-byte stores need an even Z extent (row starts at even elements) and an aligned base
-  const bool vec = o[2] + 8 <= g.N[2] && (g.N[2] & 1) == 0 && (reinterpret_cast<uintptr_t>(gridv) & 15) == 0;
-  for (int y = 0; y < 8; ++y) {
-    const int gy = o[1] + y;
-    if (gy >= g.N[1]) break;
-    const float* srow = acc + (x * 8 + y) * 8 * VS;
-    float* drow = gridv + (((long long)gx * g.N[1] + gy) * g.N[2] + o[2]) * 2 + (long long)(c0 + c) * gvol * 2;
-    const float2 a0 = *reinterpret_cast<const float2*>(srow + (2 * zp) * VS + c * 2);
-    const float2 a1 = *reinterpret_cast<const float2*>(srow + (2 * zp + 1) * VS + c * 2);
-    if (c >= ncoil) continue;
-    if (vec) {
-      *reinterpret_cast<float4*>(drow + 4 * zp) = make_float4(a0.x, a0.y, a1.x, a1.y);
-    } else {
-      if (o[2] + 2 * zp < g.N[2]) *reinterpret_cast<float2*>(drow + 4 * zp) = a0;
-      if (o[2] + 2 * zp + 1 < g.N[2]) *reinterpret_cast<float2*>(drow + 4 * zp + 2) = a1;
-    }
-  }
-}
-
 // Sum the partial tiles of one split tile (8^3 x 8 entries) in slot order,
 // compensated (the dense k-space centre piles thousands of points onto a
-// cell; each partial holds at most one chunk of them): coalesced float4 reads, the sum staged in shared memory, then the same
-// row-wise write-out as an unsplit tile.
+// cell; each partial holds at most one chunk of them). CTA = one x-plane
+// (blockIdx.z) of one split tile: 256 threads x one float4 of the plane per
+// partial, four partials in flight; then warp w writes row y = w of the
+// plane, lane = (entry, z pair), 16 bytes per lane.
 __global__ void __launch_bounds__(256) adj_reduce_f3_kernel(Geo g, const int4* __restrict__ split,
                                                             const float* __restrict__ partial,
                                                             float* __restrict__ gridv) {
-  constexpr int TFL = 512 * 16;
-  __shared__ __align__(16) float acc[TFL];
+  constexpr int TFL = 512 * 16, PFL = 64 * 16, VS = 16;
+  __shared__ __align__(16) float acc[PFL];
   const int4 sp = split[blockIdx.x];
-  const int cg = blockIdx.y, ncg = gridDim.y;
+  const int cg = blockIdx.y, ncg = gridDim.y, x = blockIdx.z;
   const int c0 = cg * 8;
   const int ncoil = (int)min(8ll, g.nbatch - c0);
   int o[3];
@@ -1140,30 +1113,50 @@ __global__ void __launch_bounds__(256) adj_reduce_f3_kernel(Geo g, const int4* _
     o[0] = (t / g.nt[1]) * 8;
   }
   const int tid = threadIdx.x;
-  float4 sum[TFL / 4 / 256], comp[TFL / 4 / 256];
-  const float4* src = reinterpret_cast<const float4*>(partial + ((long long)sp.y * ncg + cg) * TFL) + tid;
+  const long long step = (long long)ncg * TFL / 4;  // float4s between consecutive partials
+  const float4* src = reinterpret_cast<const float4*>(partial + ((long long)sp.y * ncg + cg) * TFL + x * PFL) + tid;
+  float4 sum = __ldg(src), comp = make_float4(0.f, 0.f, 0.f, 0.f);
+  int k = 1;
+  for (; k + 4 <= sp.z; k += 4) {
+    float4 v[4];
 #pragma unroll
-  for (int i = 0; i < TFL / 4 / 256; ++i) {
-    sum[i] = __ldg(src + i * 256);
-    comp[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-  }
-  for (int k = 1; k < sp.z; ++k) {
-    const float4* q = reinterpret_cast<const float4*>(partial + ((long long)(sp.y + k) * ncg + cg) * TFL) + tid;
+    for (int i = 0; i < 4; ++i) v[i] = __ldg(src + (k + i) * step);
 #pragma unroll
-    for (int i = 0; i < TFL / 4 / 256; ++i) {
-      const float4 v = __ldg(q + i * 256);
-      comp_add(sum[i].x, comp[i].x, v.x);
-      comp_add(sum[i].y, comp[i].y, v.y);
-      comp_add(sum[i].z, comp[i].z, v.z);
-      comp_add(sum[i].w, comp[i].w, v.w);
+    for (int i = 0; i < 4; ++i) {
+      comp_add(sum.x, comp.x, v[i].x);
+      comp_add(sum.y, comp.y, v[i].y);
+      comp_add(sum.z, comp.z, v[i].z);
+      comp_add(sum.w, comp.w, v[i].w);
     }
   }
-#pragma unroll
-  for (int i = 0; i < TFL / 4 / 256; ++i)
-    reinterpret_cast<float4*>(acc)[tid + i * 256] =
-        make_float4(sum[i].x + comp[i].x, sum[i].y + comp[i].y, sum[i].z + comp[i].z, sum[i].w + comp[i].w);
+  for (; k < sp.z; ++k) {
+    const float4 v = __ldg(src + k * step);
+    comp_add(sum.x, comp.x, v.x);
+    comp_add(sum.y, comp.y, v.y);
+    comp_add(sum.z, comp.z, v.z);
+    comp_add(sum.w, comp.w, v.w);
+  }
+  reinterpret_cast<float4*>(acc)[tid] =
+      make_float4(sum.x + comp.x, sum.y + comp.y, sum.z + comp.z, sum.w + comp.w);
   __syncthreads();
-  write_tile_rows(g, acc, o, tid >> 5, tid & 31, c0, ncoil, gridv);
+  const int yy = tid >> 5, lane = tid & 31;
+  const int gx = o[0] + x, gy = o[1] + yy;
+  if (gx >= g.N[0] || gy >= g.N[1]) return;
+  const long long gvol = (long long)g.N[0] * g.N[1] * g.N[2];
+  const int c = lane >> 2, zp = lane & 3;
+  if (c >= ncoil) return;
+  const float* srow = acc + yy * 8 * VS;
+  const float2 a0 = *reinterpret_cast<const float2*>(srow + (2 * zp) * VS + c * 2);
+  const float2 a1 = *reinterpret_cast<const float2*>(srow + (2 * zp + 1) * VS + c * 2);
+  float* drow = gridv + ((long long)(c0 + c) * gvol + ((long long)gx * g.N[1] + gy) * g.N[2] + o[2]) * 2;
+  // 16-byte stores need an even Z extent (row starts at even elements) and an aligned base
+  const bool vec = o[2] + 8 <= g.N[2] && (g.N[2] & 1) == 0 && (reinterpret_cast<uintptr_t>(gridv) & 15) == 0;
+  if (vec) {
+    *reinterpret_cast<float4*>(drow + 4 * zp) = make_float4(a0.x, a0.y, a1.x, a1.y);
+  } else {
+    if (o[2] + 2 * zp < g.N[2]) *reinterpret_cast<float2*>(drow + 4 * zp) = a0;
+    if (o[2] + 2 * zp + 1 < g.N[2]) *reinterpret_cast<float2*>(drow + 4 * zp + 2) = a1;
+  }
 }
 
 // Packed single-precision arithmetic of sm_100+ (two independent IEEE fp32
@@ -2207,7 +2200,7 @@ int launch_adj_f3(const Geo& g, const tlgb_interp_plan_info* info, const char* P
                                     (float*)scratch);
   TLGB_CHECK_LAUNCH();
   if (info->n_split_tiles > 0) {
-    dim3 g2((unsigned)info->n_split_tiles, (unsigned)ncg);
+    dim3 g2((unsigned)info->n_split_tiles, (unsigned)ncg, 8);
     adj_reduce_f3_kernel<<<g2, 256, 0, s>>>(g, (const int4*)(P + info->off_split), (const float*)scratch,
                                              (float*)grid);
     TLGB_CHECK_LAUNCH();
