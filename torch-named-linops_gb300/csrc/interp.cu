@@ -1418,9 +1418,10 @@ __global__ void __launch_bounds__(256, 3) adj_f3_kernel(Geo g, const int4* __res
 
 // Gather: CTA = 8 warps sharing one 12^3 x 8-entry region ([entry][x][y][z],
 // loaded by one TMA bulk tensor copy when the region needs no wrap), two CTAs
-// per SM. Records of kGB entries are built per batch, one per thread; each
-// warp then takes every 8th point. Lanes = (z-tap, y-tap, entry half): a lane
-// sums 4 x-taps x 4 entries, then 8 values are reduced over 16 lanes.
+// per SM. Each warp takes every 8th point of the item, building the records
+// of its next 8 points itself (kGB = 8 warps x 8 slots). Lanes = (entry,
+// z-tap): a lane sums its entry's 4 y-taps x 4 x-taps, two points at a time,
+// then the 4 z-tap lanes of each entry add up.
 constexpr int kGB = 64;
 
 __global__ void __launch_bounds__(256, 2) fwd_f3_kernel(const __grid_constant__ CUtensorMap tmap, int use_tma, Geo g,
@@ -1483,110 +1484,141 @@ __global__ void __launch_bounds__(256, 2) fwd_f3_kernel(const __grid_constant__ 
                     : make_float2(0.f, 0.f);
     }
   }
-  const int kz = lane & 3, ky = (lane >> 2) & 3, ch = lane >> 4;
-  auto build_records = [&](int b) {
-    // warps 0, 1: entry tid's record and region view
-    if (tid < min(kGB, it.z - b)) {
-      const long long p = entries[b + tid];
-      const PRec R = load_prec(precs, p);
-      R3& S = rec[tid];
+  // lane = (entry c, z tap kz). Iteration t reads y tap (t + c) & 3: the 8
+  // entries' regions are 13,824 B apart (the same banks), so rotating the y
+  // taps by entry spreads one load instruction over 4 bank windows.
+  const int c = lane >> 2, kz = lane & 3;
+  int kyo[4], rowoff[4];
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    kyo[t] = (t + c) & 3;
+    rowoff[t] = kyo[t] * S;
+  }
+  // Each warp takes the item's points warp, warp + 8, ... in mini-batches of
+  // 8 and keeps its own 8 record slots. Lanes 0-7 run two mini-batches
+  // ahead: the point indices of mini-batch m + 2 and the point records of
+  // m + 1 are in flight in registers while the warp gathers mini-batch m.
+  R3* wrec = rec + warp * 8;
+  const int npt = it.z - it.y;
+  auto point_at = [&](int base) -> int {
+    const int j = base + 8 * lane;
+    return (lane < 8 && j < npt) ? entries[it.y + j] : -1;
+  };
+  auto fetch = [&](int p) {
+    PRec R;
+    if (p >= 0) R = load_prec(precs, p);
+    return R;
+  };
+  auto publish = [&](int p, const PRec& R) {
+    if (p >= 0) {
+      R3& S = wrec[lane];
       S.w[0] = R.w[0];
       S.w[1] = R.w[1];
       S.w[2] = R.w[2];
       S.view = region_view(g, R, o);
-      S.p = (int)p;
+      S.p = p;
     }
+    __syncwarp();
   };
-  build_records(it.y);  // while the region copy is in flight
+  int pc = point_at(warp);           // mini-batch 0: indices
+  int pn = point_at(warp + 8 * NW);  // mini-batch 1: indices
+  PRec Rc = fetch(pc);               // mini-batch 0: records
+  auto build_records = [&](int base) {
+    publish(pc, Rc);  // the mini-batch at base
+    Rc = fetch(pn);   // the next one's records (its indices are in)
+    pc = pn;
+    pn = point_at(base + 16 * NW);  // the one after's indices
+  };
+  build_records(warp);  // while the region copy is in flight
   {
-    // the copy must have landed: bounded wait, then a CTA-wide vote
+    // the copy must have landed: one thread polls (bounded), the others
+    // wait at the barrier without taking issue slots; then a CTA-wide vote
     bool ok = true;
-    if (tma) ok = mbar_wait_bounded(bar, 0, 1u << 22);
+    if (tma && tid == 0) ok = mbar_wait_bounded(bar, 0, 1u << 22);
     if (__syncthreads_or(!ok)) {
       if (tid == 0) atomicExch(&g_tlgb_status, 1);
       return;
     }
   }
-  for (int b = it.y; b < it.z; b += kGB) {
-    const int nb = min(kGB, it.z - b);
-    if (b != it.y) {
-      __syncthreads();  // the previous batch has been read
-      build_records(b);
-      __syncthreads();
-    }
-    for (int j = warp; j < nb; j += NW) {
-      const R3& R = rec[j];
-      const unsigned view = R.view;
-      if (!((view >> 21) & 1)) continue;  // no valid tap (warp-uniform)
-      float acc[8];
+  {
+    // points of the plain-run view, two per step: sum over y taps of
+    // wy wz (sum over x taps of wx v). A record's weights are zero past its
+    // tap count, so taps outside the window contribute 0; every tap of the
+    // 4^3 box lies inside the staged region.
+    auto gather_box = [&](const R3& R) {
+      const float4 wx = R.w[0];
+      const float wz = (&R.w[2].x)[kz];
+      const float* wy = &R.w[1].x;
+      const float2* a = reg + c * VOL + (R.view & 2047) + kz;
+      float2 acc = make_float2(0.f, 0.f);
 #pragma unroll
-      for (int i = 0; i < 8; ++i) acc[i] = 0.f;
-      if ((view >> 20) & 1) {
-        const int mx = (view >> 11) & 7, my = (view >> 14) & 7, mz = (view >> 17) & 7;
-        const float wyz = (ky < my && kz < mz) ? (&R.w[1].x)[ky] * (&R.w[2].x)[kz] : 0.f;
-        const float2* a = reg + ch * 4 * VOL + (view & 2047) + ky * S + kz;
-        const float4 wx = R.w[0];
-#pragma unroll
-        for (int kx = 0; kx < 4; ++kx) {
-          if (kx < mx) {
-            const float w = (kx == 0 ? wx.x : kx == 1 ? wx.y : kx == 2 ? wx.z : wx.w) * wyz;
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-              const float2 v = a[c * VOL + kx * PLANE];
-              acc[2 * c] = fmaf(w, v.x, acc[2 * c]);
-              acc[2 * c + 1] = fmaf(w, v.y, acc[2 * c + 1]);
-            }
+      for (int t = 0; t < 4; ++t) {
+        const float wyz = wy[kyo[t]] * wz;
+        const float2* ar = a + rowoff[t];
+        float2 sx = mul2_bcast(wx.x, ar[0]);
+        fma2_bcast(sx, wx.y, ar[PLANE]);
+        fma2_bcast(sx, wx.z, ar[2 * PLANE]);
+        fma2_bcast(sx, wx.w, ar[3 * PLANE]);
+        acc.x = fmaf(wyz, sx.x, acc.x);
+        acc.y = fmaf(wyz, sx.y, acc.y);
+      }
+      return acc;
+    };
+    // the generic record path (exact-integer coordinates)
+    auto gather_rec = [&](const R3& R) {
+      if (lane == 0) {
+        float x3[3];
+        for (int e = 0; e < 3; ++e) x3[e] = load_coord(g, locs, R.p, e);
+        lane_rec<5>(g, x3, o, true, slow[warp]);
+      }
+      __syncwarp();
+      const Rec<5>& Sr = slow[warp];
+      float2 acc = make_float2(0.f, 0.f);
+      for (int kzz = kz; kzz < Sr.m[2]; kzz += 4)
+        for (int kyy = 0; kyy < Sr.m[1]; ++kyy)
+          for (int kx = 0; kx < Sr.m[0]; ++kx) {
+            const float w = g.norm == 1 ? Sr.wv[0][kx] * Sr.wv[1][kyy] * Sr.wv[2][kzz]
+                                        : radial_w(g, Sr.wv[0][kx], Sr.wv[1][kyy], Sr.wv[2][kzz]);
+            fma2_bcast(acc, w, reg[c * VOL + (Sr.lc[0][kx] * S + Sr.lc[1][kyy]) * S + Sr.lc[2][kzz]]);
           }
+      __syncwarp();
+      return acc;
+    };
+    // sum over the 4 z-tap lanes of each entry, then lane kz = 0 stores
+    auto finish = [&](float2 acc, int p) {
+      acc.x += __shfl_xor_sync(0xffffffffu, acc.x, 1);
+      acc.y += __shfl_xor_sync(0xffffffffu, acc.y, 1);
+      acc.x += __shfl_xor_sync(0xffffffffu, acc.x, 2);
+      acc.y += __shfl_xor_sync(0xffffffffu, acc.y, 2);
+      if (kz == 0 && c0 + c < g.nbatch)
+        *reinterpret_cast<float2*>(out + ((long long)(c0 + c) * g.npts + p) * 2) = acc;
+    };
+    auto one = [&](const R3& R) {
+      const unsigned view = R.view;
+      if (!((view >> 21) & 1)) return;  // no valid tap (warp-uniform)
+      finish((view >> 20) & 1 ? gather_box(R) : gather_rec(R), R.p);
+    };
+    for (int base = warp; base < npt; base += 8 * NW) {
+      if (base != warp) {
+        __syncwarp();  // the previous mini-batch has been read
+        build_records(base);
+      }
+      const int nb = min(8, (npt - base + NW - 1) / NW);
+      int i = 0;
+      for (; i + 1 < nb; i += 2) {
+        const R3& R0 = wrec[i];
+        const R3& R1 = wrec[i + 1];
+        if ((R0.view & R1.view) >> 20 & 1) {
+          // both on the plain-run path (which implies a valid tap): interleaved
+          const float2 a0 = gather_box(R0), a1 = gather_box(R1);
+          finish(a0, R0.p);
+          finish(a1, R1.p);
+        } else {
+          one(R0);
+          one(R1);
         }
-      } else {
-        // exact-integer coordinates: generic record
-        if (lane == 0) {
-          float x3[3];
-          for (int e = 0; e < 3; ++e) x3[e] = load_coord(g, locs, R.p, e);
-          lane_rec<5>(g, x3, o, true, slow[warp]);
-        }
-        __syncwarp();
-        const Rec<5>& Sr = slow[warp];
-        for (int kzz = kz; kzz < Sr.m[2]; kzz += 4)
-          for (int kyy = ky; kyy < Sr.m[1]; kyy += 4)
-            for (int kx = 0; kx < Sr.m[0]; ++kx) {
-              const float w = g.norm == 1 ? Sr.wv[0][kx] * Sr.wv[1][kyy] * Sr.wv[2][kzz]
-                                          : radial_w(g, Sr.wv[0][kx], Sr.wv[1][kyy], Sr.wv[2][kzz]);
-              const float2* a = reg + ch * 4 * VOL + (Sr.lc[0][kx] * S + Sr.lc[1][kyy]) * S + Sr.lc[2][kzz];
-#pragma unroll
-              for (int c = 0; c < 4; ++c) {
-                const float2 v = a[c * VOL];
-                acc[2 * c] = fmaf(w, v.x, acc[2 * c]);
-                acc[2 * c + 1] = fmaf(w, v.y, acc[2 * c + 1]);
-              }
-            }
-        __syncwarp();
       }
-      // reduce-scatter 8 values over the 16 lanes of each entry half: lane L
-      // ends with value (L >> 1) & 7 (entry (L >> 2) & 3 of its half, re if
-      // L & 2 == 0)
-      float s4[4], s2[2];
-      const bool b3 = lane & 8, b2 = lane & 4, b1 = lane & 2;
-#pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        const float send = b3 ? acc[i] : acc[i + 4];
-        s4[i] = (b3 ? acc[i + 4] : acc[i]) + __shfl_xor_sync(0xffffffffu, send, 8);
-      }
-#pragma unroll
-      for (int i = 0; i < 2; ++i) {
-        const float send = b2 ? s4[i] : s4[i + 2];
-        s2[i] = (b2 ? s4[i + 2] : s4[i]) + __shfl_xor_sync(0xffffffffu, send, 4);
-      }
-      float s1;
-      {
-        const float send = b1 ? s2[0] : s2[1];
-        s1 = (b1 ? s2[1] : s2[0]) + __shfl_xor_sync(0xffffffffu, send, 2);
-      }
-      s1 += __shfl_xor_sync(0xffffffffu, s1, 1);
-      const float im = __shfl_down_sync(0xffffffffu, s1, 2);
-      const int c = c0 + ch * 4 + ((lane >> 2) & 3);
-      if ((lane & 3) == 0 && c < g.nbatch)
-        *reinterpret_cast<float2*>(out + ((long long)c * g.npts + R.p) * 2) = make_float2(s1, im);
+      if (i < nb) one(wrec[i]);
     }
   }
 }
