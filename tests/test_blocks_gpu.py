@@ -42,6 +42,11 @@ def test_blocks_match_reference_bit_exact(case):
         ((4, 120, 120, 120), (10, 10, 10), (10, 10, 10), torch.complex64),
         ((2, 1025), (25,), (25,), torch.float64),
         ((5, 64, 80), (16, 8), (4, 8), torch.complex128),
+        # even innermost block, stride and extent: the paired fold, with
+        # uncovered trailing elements (f64) and a stride not dividing the block (f32)
+        ((2, 30, 34, 42), (4, 6, 8), (2, 4, 6), torch.float64),
+        ((3, 50, 64), (6, 10), (2, 4), torch.float32),
+        ((2, 18, 20, 22), (3, 4, 6), (3, 2, 2), torch.complex64),
     ],
 )
 def test_blocks_random_against_oracle(shape, block, stride, dtype):

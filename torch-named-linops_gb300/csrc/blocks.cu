@@ -16,6 +16,8 @@
 
 #include "common.cuh"
 
+#include <type_traits>
+
 namespace tlgb {
 namespace {
 
@@ -185,6 +187,58 @@ __global__ void __launch_bounds__(256) fold_kernel(const T* __restrict__ in, T* 
   }
 }
 
+// Fold of adjacent element pairs along the innermost dimension. When the
+// innermost block size and stride are both even (and the extent is even),
+// elements 2h and 2h + 1 are covered by the same blocks and sit next to each
+// other in every block, so one 2-element load per covering block serves both;
+// offsets inside one batch entry fit in 32 bits (checked by the caller). Each
+// element still sums its covering block entries in ascending block order,
+// starting from 0: the same float additions as fold_kernel.
+template <typename E, typename V>
+__global__ void __launch_bounds__(256) fold_pairs_kernel(const E* __restrict__ in, E* __restrict__ out, BlkGeo g,
+                                                         FastDiv div_half2, FastDiv ds0, FastDiv ds1, FastDiv ds2) {
+  static_assert(sizeof(V) == 2 * sizeof(E), "a pair of elements");
+  const int64_t plane = blockIdx.x;  // (n, x0)
+  const int64_t x0 = plane % g.im[0];
+  const int64_t n = plane / g.im[0];
+  const uint32_t B1 = (uint32_t)g.B[1], B2 = (uint32_t)g.B[2], s0 = (uint32_t)g.s[0], s1 = (uint32_t)g.s[1],
+                 s2 = (uint32_t)g.s[2], nb1 = (uint32_t)g.nb[1], nb2 = (uint32_t)g.nb[2];
+  const uint32_t bvol = (uint32_t)(g.B[0] * g.B[1] * g.B[2]);
+  const E* src = in + n * (g.nb[0] * g.nb[1] * g.nb[2]) * (int64_t)bvol;
+  E* dst = out + plane * (g.im[1] * g.im[2]);
+  const uint32_t half2 = (uint32_t)(g.im[2] / 2), tasks = (uint32_t)g.im[1] * half2;
+  int64_t lo0, hi0;
+  cover(x0, g.B[0], g.s[0], g.nb[0], ds0, lo0, hi0);
+  for (uint32_t t = threadIdx.x; t < tasks; t += blockDim.x) {
+    const uint32_t x1 = fdiv(t, div_half2);
+    const uint32_t x2 = 2 * (t - x1 * half2);
+    int64_t lo1, hi1, lo2, hi2;
+    cover(x1, g.B[1], g.s[1], g.nb[1], ds1, lo1, hi1);
+    cover(x2, g.B[2], g.s[2], g.nb[2], ds2, lo2, hi2);
+    E a0 = Acc<E>::zero(), a1 = Acc<E>::zero();
+    for (uint32_t b0 = (uint32_t)lo0; b0 <= (uint32_t)hi0 && lo0 <= hi0; ++b0) {
+      const uint32_t i0 = (uint32_t)x0 - b0 * s0;
+      for (uint32_t b1 = (uint32_t)lo1; (int64_t)b1 <= hi1; ++b1) {
+        const uint32_t i1 = x1 - b1 * s1;
+        const uint32_t blk01 = (b0 * nb1 + b1) * nb2;
+        const uint32_t k01 = (i0 * B1 + i1) * B2;
+        for (uint32_t b2 = (uint32_t)lo2; (int64_t)b2 <= hi2; ++b2) {
+          const uint32_t off = (blk01 + b2) * bvol + k01 + (x2 - b2 * s2);
+          const V v = __ldg(reinterpret_cast<const V*>(src + off));
+          const E* e = reinterpret_cast<const E*>(&v);
+          Acc<E>::add(a0, e[0]);
+          Acc<E>::add(a1, e[1]);
+        }
+      }
+    }
+    V r;
+    E* re = reinterpret_cast<E*>(&r);
+    re[0] = a0;
+    re[1] = a1;
+    *reinterpret_cast<V*>(dst + (int64_t)x1 * g.im[2] + x2) = r;
+  }
+}
+
 int check_desc(const tlgb_blocks_desc* d, BlkGeo& g, int& esize) {
   if (!d) TLGB_FAIL(TLGB_ERR_INVALID, "null blocks descriptor");
   if (d->ndim < 1 || d->ndim > 3) TLGB_FAIL(TLGB_ERR_INVALID, "ndim must be 1, 2 or 3");
@@ -260,6 +314,21 @@ int launch_fold(const BlkGeo& g, const int32_t* mask_inv, const void* in, void* 
   const FastDiv d2 = make_fastdiv((uint32_t)g.im[2]);
   const FastDiv s0 = make_fastdiv((uint32_t)g.s[0]), s1 = make_fastdiv((uint32_t)g.s[1]),
                 s2 = make_fastdiv((uint32_t)g.s[2]);
+  if constexpr (!std::is_same<T, double2>::value) {
+    // element pairs: even innermost block, stride and extent, 32-bit offsets
+    // inside a batch entry, pair-aligned pointers
+    using V = typename std::conditional<std::is_same<T, float>::value, float2,
+                                        typename std::conditional<std::is_same<T, double>::value, double2,
+                                                                  float4>::type>::type;
+    const int64_t per_entry = g.nb[0] * g.nb[1] * g.nb[2] * g.B[0] * g.B[1] * g.B[2];
+    if (!mask_inv && g.B[2] % 2 == 0 && g.s[2] % 2 == 0 && g.im[2] >= 2 && g.im[2] % 2 == 0 && per_entry < (1ll << 31) &&
+        g.im[1] * g.im[2] < (1ll << 31) && ((uintptr_t)in % sizeof(V)) == 0 && ((uintptr_t)out % sizeof(V)) == 0) {
+      const FastDiv h2 = make_fastdiv((uint32_t)(g.im[2] / 2));
+      fold_pairs_kernel<T, V><<<(unsigned)nplane, 256, 0, s>>>((const T*)in, (T*)out, g, h2, s0, s1, s2);
+      TLGB_CHECK_LAUNCH();
+      return TLGB_OK;
+    }
+  }
   if (mask_inv)
     fold_kernel<T, true><<<(unsigned)nplane, 256, 0, s>>>((const T*)in, (T*)out, g, mask_inv, d2, s0, s1, s2);
   else
