@@ -344,6 +344,8 @@ def run_gpu(args, world, rank, local):
     torch.cuda.empty_cache()
     if not args.skip_blocks:
         kernels.update(bench_blocks(dev, peak, args))
+    if not args.skip_nufft2d:
+        kernels["nufft2d"] = bench_nufft2d(dev, peak)
     line = None
     if rank == 0:
         cpu = None
@@ -439,6 +441,70 @@ def bench_blocks(dev, peak, args):
     }
 
 
+def bench_nufft2d(dev, peak):
+    """The differentiable 2D NUFFT: 32 slices x 8 coils of a 256^2 complex64
+    image (padded 320^2), golden-angle radial 402 spokes x 512 readouts with
+    N(0, 0.1) jitter, through the functional nufft. Times the forward, the
+    forward + backward for the image gradient (trajectory fixed: one plan),
+    and the forward + backward for image and trajectory gradients (the plan
+    is rebuilt every call, as when the trajectory changes each step)."""
+    from torchlinops_gb300 import linops
+
+    S, C, N, SP, RD = 32, 8, 256, 402, 512
+    g = torch.Generator().manual_seed(4)
+    ang = torch.arange(SP, dtype=torch.float64) * math.pi * (math.sqrt(5.0) - 1.0) / 2.0
+    r = (torch.arange(RD, dtype=torch.float64) - RD // 2) * (N / RD)
+    locs = torch.stack([r[None, :] * torch.cos(ang[:, None]), r[None, :] * torch.sin(ang[:, None])], dim=-1)
+    locs = (locs + 0.1 * torch.randn(locs.shape, generator=g, dtype=torch.float64)).to(torch.float32).to(dev)
+    gd = torch.Generator(device=dev).manual_seed(5)
+    x = torch.randn(S, C, N, N, dtype=torch.complex64, device=dev, generator=gd)
+    a = torch.randn(S, C, SP, RD, dtype=torch.complex64, device=dev, generator=gd)
+    s = torch.cuda.current_stream(dev)
+
+    def timed(fn, reps=10):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(reps):
+            fn()
+        e1.record(s)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    def fwd():
+        with torch.no_grad():
+            linops.nufft(x, locs)
+
+    xg = x.clone().requires_grad_(True)
+
+    def fwd_bwd_image():
+        xg.grad = None
+        (a.conj() * linops.nufft(xg, locs)).real.sum().backward()
+
+    lg = locs.clone().requires_grad_(True)
+
+    def fwd_bwd_both():
+        xg.grad = None
+        lg.grad = None
+        (a.conj() * linops.nufft(xg, lg)).real.sum().backward()
+
+    f_ms, fb_ms, fbl_ms = timed(fwd), timed(fwd_bwd_image), timed(fwd_bwd_both)
+    # one ungrid of this workload: grid 256 x 320^2 c64 + locs + 256 x 205,824 c64 values
+    ungrid_bytes = S * C * 320 * 320 * 8 + SP * RD * 2 * 4 + S * C * SP * RD * 8
+    del x, a, xg, lg
+    torch.cuda.empty_cache()
+    return {
+        "workload": "32 slices x 8 coils x 256^2 c64, padded 320^2, golden-angle radial 402 x 512 (+N(0,0.1) jitter)",
+        "fwd_ms": f_ms,
+        "fwd_bwd_image_ms": fb_ms,
+        "fwd_bwd_image_and_locs_ms": fbl_ms,
+        "ungrid_algorithmic_bytes": ungrid_bytes,
+        "samples_per_s_fwd": S * C * SP * RD / (f_ms / 1e3),
+    }
+
+
 def bench_cg(dev, args):
     """Learned-preconditioned vs plain CG to relative residual 1e-4 on 3D
     SENSE: 128^3 image, 8 Gaussian coil maps, 3D radial 2048 spokes x 512
@@ -514,6 +580,7 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-blocks", action="store_true")
     ap.add_argument("--skip-cg", action="store_true", help="skip the learned vs plain CG comparison")
+    ap.add_argument("--skip-nufft2d", action="store_true", help="skip the differentiable 2D NUFFT timing")
     ap.add_argument("--cg-steps", type=int, default=500, help="preconditioner training steps (4 samples each)")
     ap.add_argument("--grid", type=int, default=N_GRID, help="grid edge (smaller cases for profiling)")
     ap.add_argument("--points", type=int, default=N_PTS, help="number of points (smaller cases for profiling)")

@@ -242,28 +242,33 @@ int tlgb_cg_step(float* x, float* r, float* p, const float* ap, int64_t n, int i
 /* Centred-FFT shifts folded into the NUFFT's pad and crop (complex64).      */
 /* The reference's cfftn = fftshift . fftn . ifftshift (utils/_fft.py:7-60)  */
 /* costs two extra grid passes per transform; here the image-side shift is   */
-/* part of one pad / crop gather, and the k-side shift is a shift of the     */
-/* trajectory by -floor(Np/2) (grid units) where it is prepared.             */
+/* part of one pad / crop gather, and the k-side shift is the modulation     */
+/* fftshift(fftn(z)) = fftn(z . m), m[j] = prod_e exp(2 pi i j_e h_e / Np_e), */
+/* h_e = floor(Np_e / 2) (the sign (-1)^j_e for even Np_e), applied in the   */
+/* same gather, so the interpolation reads the reference's own coordinates.  */
 /* ------------------------------------------------------------------------ */
 
 /* Zero pad with the ifftshift folded in: for the padded-grid index j,
  * i = ((j + shift) mod np) - off per dim; out[b*C + c][j] =
- * maps[c][i] * apod[i] * x[b][i] where i lies in the image, else 0.
+ * mod[j] * maps[c][i] * apod[i] * x[b][i] where i lies in the image, else 0,
+ * with mod[j] = m[j] above when `modulate` is nonzero, else 1.
  * Dims: the last `ndim` (1-3) of x [nbatch][n] and out [nbatch*C][np];
  * shift = floor(np / 2) gives the reference's ifftshift(pad(x)); off is the
  * left padding. apod (float, [n]) and maps (complex64, [C][n], C = nmaps)
  * may be NULL (then C = 1). */
 int tlgb_pad_shift_c64(const void* x, int64_t nbatch, int32_t ndim, const int64_t* n, const int64_t* np,
-                       const int64_t* off, const int64_t* shift, const float* apod, const void* maps, int32_t nmaps,
-                       void* out, tlgb_stream_t stream);
+                       const int64_t* off, const int64_t* shift, int32_t modulate, const float* apod,
+                       const void* maps, int32_t nmaps, void* out, tlgb_stream_t stream);
 
 /* Crop with the fftshift folded in, the adjoint of tlgb_pad_shift plus an
  * axpy: out[b][i] = alpha * apod[i] * sum_c conj(maps[c][i]) *
- * z[b*C + c][j(i)] + beta * add[b][i], with j = (i + off - shift) mod np per
- * dim. add may be NULL (then beta is ignored). */
+ * conj(mod[j]) * z[b*C + c][j(i)] + beta * add[b][i], with
+ * j = (i + off - shift) mod np per dim. add may be NULL (then beta is
+ * ignored). */
 int tlgb_crop_shift_c64(const void* z, int64_t nbatch, int32_t ndim, const int64_t* n, const int64_t* np,
-                        const int64_t* off, const int64_t* shift, const float* apod, const void* maps, int32_t nmaps,
-                        float alpha, const void* add, float beta, void* out, tlgb_stream_t stream);
+                        const int64_t* off, const int64_t* shift, int32_t modulate, const float* apod,
+                        const void* maps, int32_t nmaps, float alpha, const void* add, float beta, void* out,
+                        tlgb_stream_t stream);
 
 /* ------------------------------------------------------------------------ */
 /* 3^3 convolution on the tensor cores (BF16 operands, FP32 accumulation):    */

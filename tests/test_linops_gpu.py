@@ -160,11 +160,66 @@ def test_pad_shift_and_crop_shift_match_torch(im, padded):
     gotb = linops.crop_shift(z.to(DEV), im, padded, maps=maps.to(DEV), apod=apod.to(DEV), alpha=0.5,
                              add=add.to(DEV), beta=2.0).cpu()
     torch.testing.assert_close(gotb, 0.5 * back + 2.0 * add, rtol=1e-5, atol=1e-5)
+    # with the k-space modulation, an uncentred fftn of the pad is the centred
+    # cfftn (fftshift . fftn . ifftshift) of the padded image, and the crop
+    # of an uncentred ifftn is the crop of the centred cifftn
+    xm = linops.pad_shift(x.to(DEV), im, padded, maps=maps.to(DEV), apod=apod.to(DEV), modulate=True)
+    k = torch.fft.fftn(xm, dim=dims, norm="ortho").cpu()
+    kref = torch.fft.fftshift(torch.fft.fftn(ref, dim=dims, norm="ortho"), dim=dims)
+    torch.testing.assert_close(k, kref, rtol=1e-5, atol=1e-5)
+    G = torch.randn(3, *padded, dtype=torch.complex64, generator=gen)
+    cif = torch.fft.fftshift(torch.fft.ifftn(torch.fft.ifftshift(G, dim=dims), dim=dims, norm="ortho"), dim=dims)
+    backm = (maps.conj() * apod * cif[(slice(None),) + sl]).sum(0)
+    gotm = linops.crop_shift(torch.fft.ifftn(G.to(DEV), dim=dims, norm="ortho"), im, padded, maps=maps.to(DEV),
+                             apod=apod.to(DEV), modulate=True).cpu()
+    torch.testing.assert_close(gotm, backm, rtol=1e-5, atol=1e-5)
     # adjoint pair without maps
     y = torch.randn(*padded, dtype=torch.complex64, generator=gen)
     lhs = torch.vdot(linops.pad_shift(x.to(DEV), im, padded, apod=apod.to(DEV)).cpu().flatten(), y.flatten())
     rhs = torch.vdot(x.flatten(), linops.crop_shift(y.to(DEV), im, padded, apod=apod.to(DEV)).cpu().flatten())
     assert abs(complex(lhs) - complex(rhs)) / abs(complex(lhs)) < 1e-5
+
+
+@pytest.mark.parametrize("im,padded", [((10, 12), (13, 15)), ((6, 7, 8), (8, 9, 10))])
+def test_pad_shift_and_crop_shift_gradients_match_torch(im, padded):
+    """Autograd through pad_shift (x) and crop_shift (z and add) against torch
+    autograd of the unfused ops, with coil maps and apodization."""
+    gen = torch.Generator().manual_seed(3 + len(im))
+    nd = len(im)
+    dims = tuple(range(-nd, 0))
+    x = torch.randn(2, *im, dtype=torch.complex64, generator=gen)
+    maps = torch.randn(3, *im, dtype=torch.complex64, generator=gen)
+    apod = torch.rand(*im, generator=gen) + 0.5
+    a = torch.randn(2, 3, *padded, dtype=torch.complex64, generator=gen)
+    pad = linops.pad_to_size(im, padded)
+    xr = x.clone().requires_grad_(True)
+    ref = torch.fft.ifftshift(torch.nn.functional.pad(maps[None] * apod * xr[:, None], pad), dim=dims)
+    (a.conj() * ref).real.sum().backward()
+    xg = x.to(DEV).requires_grad_(True)
+    out = linops.pad_shift(xg, im, padded, maps=maps.to(DEV), apod=apod.to(DEV))
+    (a.to(DEV).conj() * out).real.sum().backward()
+    torch.testing.assert_close(xg.grad.cpu(), xr.grad, rtol=1e-5, atol=1e-5)
+    # the modulated pad through an uncentred fftn against torch's cfftn
+    xr2 = x.clone().requires_grad_(True)
+    ref2 = torch.fft.ifftshift(torch.nn.functional.pad(maps[None] * apod * xr2[:, None], pad), dim=dims)
+    k2 = torch.fft.fftshift(torch.fft.fftn(ref2, dim=dims, norm="ortho"), dim=dims)
+    (a.conj() * k2).real.sum().backward()
+    xg2 = x.to(DEV).requires_grad_(True)
+    outm = linops.pad_shift(xg2, im, padded, maps=maps.to(DEV), apod=apod.to(DEV), modulate=True)
+    (a.to(DEV).conj() * torch.fft.fftn(outm, dim=dims, norm="ortho")).real.sum().backward()
+    torch.testing.assert_close(xg2.grad.cpu(), xr2.grad, rtol=1e-5, atol=1e-5)
+    z = torch.randn(2, 3, *padded, dtype=torch.complex64, generator=gen)
+    add = torch.randn(2, *im, dtype=torch.complex64, generator=gen)
+    b = torch.randn(2, *im, dtype=torch.complex64, generator=gen)
+    sl = (slice(None), slice(None)) + tuple(linops.crop_slice_from_pad(pad))
+    zr, ar = z.clone().requires_grad_(True), add.clone().requires_grad_(True)
+    back = 0.5 * (maps.conj() * apod * torch.fft.fftshift(zr, dim=dims)[sl]).sum(1) + 2.0 * ar
+    (b.conj() * back).real.sum().backward()
+    zg, ag = z.to(DEV).requires_grad_(True), add.to(DEV).requires_grad_(True)
+    got = linops.crop_shift(zg, im, padded, maps=maps.to(DEV), apod=apod.to(DEV), alpha=0.5, add=ag, beta=2.0)
+    (b.to(DEV).conj() * got).real.sum().backward()
+    torch.testing.assert_close(zg.grad.cpu(), zr.grad, rtol=1e-5, atol=1e-5)
+    torch.testing.assert_close(ag.grad.cpu(), ar.grad, rtol=1e-6, atol=1e-6)
 
 
 def test_sense_normal_matches_unfused_operator():

@@ -114,3 +114,20 @@ def test_norm_weights_round_trip():
     x = torch.randn(1, 15, 15, generator=torch.Generator().manual_seed(3))
     x2 = (1.0 / w.clamp(min=1e-6)) * OB.fold(OB.unfold(x, (3, 3), (1, 1)), (15, 15), (3, 3), (1, 1))
     torch.testing.assert_close(x, x2)
+
+
+@pytest.mark.parametrize("name", ["2d", "3d"])
+def test_nufft_oracle_matches_reference_golden(name):
+    """The NUFFT oracle (float32 mirror and FP64) against the reference's own
+    functional nufft / nufft_adjoint outputs (tests/golden/make_golden.py)."""
+    from oracle import nufft as ON
+
+    d = np.load(f"{GOLDEN}/nufft.npz")
+    x = to_torch(d[f"{name}_x"], True)
+    y = to_torch(d[f"{name}_y"], True)
+    locs = torch.from_numpy(d[f"{name}_locs"])
+    fwd = to_torch(d[f"{name}_fwd"], True)
+    adj = to_torch(d[f"{name}_adj"], True)
+    for dtype, tol in ((torch.float32, 2e-6), (torch.float64, 1e-5)):
+        assert rel_l2(ON.nufft(x, locs, dtype=dtype), fwd) < tol
+        assert rel_l2(ON.nufft_adjoint(y, locs, tuple(x.shape[-locs.shape[-1]:]), dtype=dtype), adj) < tol

@@ -5,11 +5,17 @@
 // cfftn = fftshift . fftn . ifftshift (linops/nufft.py:170-184,
 // utils/_fft.py:7-60). Each shift is a full-grid pass. Here:
 //   ifftshift(Pad(a x))[j] = a[i] x[i], i = (j + floor(Np/2)) mod Np - off
-// is one gather (tlgb_pad_shift), the k-space fftshift becomes a shift of the
-// trajectory by -floor(Np/2) (done where the locations are prepared), and
-//   Crop(fftshift(Z))[i] = Z[(i + off - floor(Np/2)) mod Np]
-// is one gather on the way back (tlgb_crop_shift), which can also apply the
-// conjugate coil maps, the coil sum and an axpy.
+// is one gather (tlgb_pad_shift), and the k-space fftshift is a modulation
+// of the same gather's output:
+//   fftshift(fftn(z)) = fftn(z . m),  m[j] = prod_e exp(2 pi i j_e h_e / Np_e),
+//   h_e = floor(Np_e / 2),
+// which for even Np_e is the sign (-1)^j_e (exact). So an uncentred fftn of
+// the gather's output is the reference's centred k-space, read at the
+// reference's own interpolation coordinates. On the way back,
+//   Crop(fftshift(ifftn(ifftshift(G))))[i] = conj(m[j]) ifftn(G)[j],
+//   j = (i + off - floor(Np/2)) mod Np,
+// is one gather (tlgb_crop_shift), which can also apply the conjugate coil
+// maps, the coil sum and an axpy.
 
 #include "common.cuh"
 
@@ -19,7 +25,33 @@ namespace {
 struct PadGeo {
   int n[3], np[3], off[3], sh[3];  // internal dims padded to 3 (leading 1s)
   long long nvol, npvol;
+  int modulate;  // multiply by m[j] (pad) / conj(m[j]) (crop)
 };
+
+// m[j] of the uncentred index j: a sign for even extents, a phase otherwise
+__device__ __forceinline__ float2 modulation(const PadGeo& G, int j0, int j1, int j2) {
+  const int j[3] = {j0, j1, j2};
+  int sign = 0;
+  float ph = 0.f;  // in units of pi
+  bool odd = false;
+#pragma unroll
+  for (int e = 0; e < 3; ++e) {
+    if ((G.np[e] & 1) == 0) {
+      sign ^= j[e] & 1;
+    } else {
+      odd = true;
+      // 2 j h / Np with h = floor(Np / 2), reduced mod 2 in integers first
+      ph += (float)((2ll * j[e] * (G.np[e] / 2)) % (2ll * G.np[e])) / (float)G.np[e];
+    }
+  }
+  float c = 1.f, s = 0.f;
+  if (odd) sincospif(ph, &s, &c);
+  return sign ? make_float2(-c, -s) : make_float2(c, s);
+}
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
 
 __device__ __forceinline__ int wrapm(int v, int m) {
   v %= m;
@@ -41,6 +73,7 @@ __global__ void pad_shift_kernel(PadGeo G, const float2* __restrict__ x, long lo
   const long long i = in ? ((long long)i0 * G.n[1] + i1) * G.n[2] + i2 : 0;
   const float a = (in && apod) ? apod[i] : 1.f;
   const int C = maps ? nmaps : 1;
+  const float2 md = G.modulate ? modulation(G, j0, j1, j2) : make_float2(1.f, 0.f);
   for (long long b = 0; b < nbatch; ++b) {
     float2 v = make_float2(0.f, 0.f);
     if (in) {
@@ -54,6 +87,7 @@ __global__ void pad_shift_kernel(PadGeo G, const float2* __restrict__ x, long lo
         const float2 m = maps[(long long)c * G.nvol + i];
         o = make_float2(m.x * v.x - m.y * v.y, m.x * v.y + m.y * v.x);
       }
+      if (G.modulate) o = cmul(o, md);
       out[(b * C + c) * G.npvol + j] = o;
     }
   }
@@ -74,10 +108,16 @@ __global__ void crop_shift_kernel(PadGeo G, const float2* __restrict__ z, long l
   const long long j = ((long long)j0 * G.np[1] + j1) * G.np[2] + j2;
   const float a = (apod ? apod[i] : 1.f) * alpha;
   const int C = maps ? nmaps : 1;
+  float2 md = make_float2(1.f, 0.f);
+  if (G.modulate) {
+    md = modulation(G, j0, j1, j2);
+    md.y = -md.y;  // conj(m[j])
+  }
   for (long long b = 0; b < nbatch; ++b) {
     float sx = 0.f, sy = 0.f;
     for (int c = 0; c < C; ++c) {
-      const float2 v = z[(b * C + c) * G.npvol + j];
+      float2 v = z[(b * C + c) * G.npvol + j];
+      if (G.modulate) v = cmul(v, md);
       if (maps) {
         const float2 m = maps[(long long)c * G.nvol + i];
         sx += m.x * v.x + m.y * v.y;  // conj(m) * v
@@ -98,7 +138,8 @@ __global__ void crop_shift_kernel(PadGeo G, const float2* __restrict__ z, long l
 }
 
 int make_pad_geo(int32_t ndim, const int64_t* n, const int64_t* np, const int64_t* off, const int64_t* shift,
-                 PadGeo& G) {
+                 int32_t modulate, PadGeo& G) {
+  G.modulate = modulate ? 1 : 0;
   if (ndim < 1 || ndim > 3 || !n || !np || !off || !shift) TLGB_FAIL(TLGB_ERR_INVALID, "pad/crop: bad dims");
   G.nvol = G.npvol = 1;
   for (int e = 0; e < 3; ++e) {
@@ -122,10 +163,10 @@ int make_pad_geo(int32_t ndim, const int64_t* n, const int64_t* np, const int64_
 using namespace tlgb;
 
 extern "C" int tlgb_pad_shift_c64(const void* x, int64_t nbatch, int32_t ndim, const int64_t* n, const int64_t* np,
-                                  const int64_t* off, const int64_t* shift, const float* apod, const void* maps,
-                                  int32_t nmaps, void* out, tlgb_stream_t stream) {
+                                  const int64_t* off, const int64_t* shift, int32_t modulate, const float* apod,
+                                  const void* maps, int32_t nmaps, void* out, tlgb_stream_t stream) {
   PadGeo G;
-  TLGB_TRY(make_pad_geo(ndim, n, np, off, shift, G));
+  TLGB_TRY(make_pad_geo(ndim, n, np, off, shift, modulate, G));
   if (nbatch < 0 || (maps && nmaps < 1)) TLGB_FAIL(TLGB_ERR_INVALID, "pad_shift: bad batch or map count");
   if (nbatch == 0) return TLGB_OK;
   if (!x || !out) TLGB_FAIL(TLGB_ERR_INVALID, "null pointer");
@@ -136,11 +177,11 @@ extern "C" int tlgb_pad_shift_c64(const void* x, int64_t nbatch, int32_t ndim, c
 }
 
 extern "C" int tlgb_crop_shift_c64(const void* z, int64_t nbatch, int32_t ndim, const int64_t* n, const int64_t* np,
-                                   const int64_t* off, const int64_t* shift, const float* apod, const void* maps,
-                                   int32_t nmaps, float alpha, const void* add, float beta, void* out,
-                                   tlgb_stream_t stream) {
+                                   const int64_t* off, const int64_t* shift, int32_t modulate, const float* apod,
+                                   const void* maps, int32_t nmaps, float alpha, const void* add, float beta,
+                                   void* out, tlgb_stream_t stream) {
   PadGeo G;
-  TLGB_TRY(make_pad_geo(ndim, n, np, off, shift, G));
+  TLGB_TRY(make_pad_geo(ndim, n, np, off, shift, modulate, G));
   if (nbatch < 0 || (maps && nmaps < 1)) TLGB_FAIL(TLGB_ERR_INVALID, "crop_shift: bad batch or map count");
   if (nbatch == 0) return TLGB_OK;
   if (!z || !out) TLGB_FAIL(TLGB_ERR_INVALID, "null pointer");

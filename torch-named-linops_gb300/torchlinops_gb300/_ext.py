@@ -112,10 +112,10 @@ _SIGNATURES = {
     "tlgb_dot_f64": ([_P, _P, ctypes.c_int64, ctypes.c_int, _P, _P, ctypes.c_size_t, _P], ctypes.c_int),
     "tlgb_cg_set_pap": ([_P, _P, ctypes.c_int64, ctypes.c_int, _P, _P, ctypes.c_size_t, _P], ctypes.c_int),
     "tlgb_cg_step": ([_P, _P, _P, _P, ctypes.c_int64, ctypes.c_int, _P, _P, ctypes.c_size_t, _P], ctypes.c_int),
-    "tlgb_pad_shift_c64": ([_P, ctypes.c_int64, ctypes.c_int32, _P, _P, _P, _P, _P, _P, ctypes.c_int32, _P, _P],
-                           ctypes.c_int),
-    "tlgb_crop_shift_c64": ([_P, ctypes.c_int64, ctypes.c_int32, _P, _P, _P, _P, _P, _P, ctypes.c_int32,
-                             ctypes.c_float, _P, ctypes.c_float, _P, _P], ctypes.c_int),
+    "tlgb_pad_shift_c64": ([_P, ctypes.c_int64, ctypes.c_int32, _P, _P, _P, _P, ctypes.c_int32, _P, _P,
+                            ctypes.c_int32, _P, _P], ctypes.c_int),
+    "tlgb_crop_shift_c64": ([_P, ctypes.c_int64, ctypes.c_int32, _P, _P, _P, _P, ctypes.c_int32, _P, _P,
+                             ctypes.c_int32, ctypes.c_float, _P, ctypes.c_float, _P, _P], ctypes.c_int),
     "tlgb_conv3d_fwd": ([_P, _P, _P, _P, _P, _P], ctypes.c_int),
     "tlgb_conv3d_wgrad_scratch_size": ([_P, ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
     "tlgb_conv3d_wgrad": ([_P, _P, _P, _P, _P, ctypes.c_size_t, _P], ctypes.c_int),

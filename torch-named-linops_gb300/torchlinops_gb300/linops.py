@@ -26,6 +26,8 @@ from __future__ import annotations
 
 import ctypes
 import math
+import weakref
+from collections import OrderedDict
 from copy import copy
 from math import prod
 from typing import Optional
@@ -274,9 +276,8 @@ def _i64(vals):
     return arr
 
 
-def pad_shift(x: Tensor, im_size, padded_size, maps: Optional[Tensor] = None, apod: Optional[Tensor] = None) -> Tensor:
-    """ifftshift(pad(apod * x)) (or per coil map: ifftshift(pad(maps_c * apod * x)))
-    over the last ``len(im_size)`` dims in one pass; complex64, CUDA."""
+def _pad_shift(x: Tensor, im_size, padded_size, maps: Optional[Tensor] = None, apod: Optional[Tensor] = None,
+               modulate: bool = False) -> Tensor:
     nd = len(im_size)
     _ext.check_cuda(x, maps, apod)
     if x.dtype != torch.complex64:
@@ -297,15 +298,13 @@ def pad_shift(x: Tensor, im_size, padded_size, maps: Optional[Tensor] = None, ap
     out = torch.empty(*out_batch, *padded_size, dtype=torch.complex64, device=x.device)
     ap = None if apod is None else apod.to(torch.float32).contiguous()
     _ext.check(_ext.lib().tlgb_pad_shift_c64(_ext.ptr(xb), nb, nd, _i64(im_size), _i64(padded_size), _i64(off),
-                                             _i64(shift), _ext.ptr(ap), _ext.ptr(maps), C, _ext.ptr(out),
-                                             _ext.stream_ptr(x.device)), "pad_shift")
+                                             _i64(shift), int(bool(modulate)), _ext.ptr(ap), _ext.ptr(maps), C,
+                                             _ext.ptr(out), _ext.stream_ptr(x.device)), "pad_shift")
     return out
 
 
-def crop_shift(z: Tensor, im_size, padded_size, maps: Optional[Tensor] = None, apod: Optional[Tensor] = None,
-               alpha: float = 1.0, add: Optional[Tensor] = None, beta: float = 0.0) -> Tensor:
-    """alpha * apod * crop(fftshift(z)) (with maps: summed over the coil dim of
-    z after multiplying by conj(maps)) + beta * add, in one pass."""
+def _crop_shift(z: Tensor, im_size, padded_size, maps: Optional[Tensor] = None, apod: Optional[Tensor] = None,
+                alpha: float = 1.0, add: Optional[Tensor] = None, beta: float = 0.0, modulate: bool = False) -> Tensor:
     nd = len(im_size)
     _ext.check_cuda(z, maps, apod, add)
     if z.dtype != torch.complex64:
@@ -327,18 +326,83 @@ def crop_shift(z: Tensor, im_size, padded_size, maps: Optional[Tensor] = None, a
     ap = None if apod is None else apod.to(torch.float32).contiguous()
     ad = None if add is None else add.resolve_conj().resolve_neg().to(torch.complex64).contiguous()
     _ext.check(_ext.lib().tlgb_crop_shift_c64(_ext.ptr(zb), nb, nd, _i64(im_size), _i64(padded_size), _i64(off),
-                                              _i64(shift), _ext.ptr(ap), _ext.ptr(maps), C, ctypes.c_float(alpha),
-                                              _ext.ptr(ad), ctypes.c_float(beta), _ext.ptr(out),
-                                              _ext.stream_ptr(z.device)), "crop_shift")
+                                              _i64(shift), int(bool(modulate)), _ext.ptr(ap), _ext.ptr(maps), C,
+                                              ctypes.c_float(alpha), _ext.ptr(ad), ctypes.c_float(beta),
+                                              _ext.ptr(out), _ext.stream_ptr(z.device)), "crop_shift")
     return out
 
 
+class _PadShiftFn(torch.autograd.Function):
+    """pad_shift is C-linear in x; its adjoint is crop_shift with the same
+    maps and apodization, so the backward pass is one crop_shift. Maps and
+    apodization are constants (no gradient)."""
+
+    @staticmethod
+    def forward(ctx, x, im_size, padded_size, maps, apod, modulate):
+        ctx.args = (tuple(im_size), tuple(padded_size), maps, apod, modulate)
+        return _pad_shift(x, im_size, padded_size, maps, apod, modulate)
+
+    @staticmethod
+    def backward(ctx, g):
+        im_size, padded_size, maps, apod, modulate = ctx.args
+        gx = None
+        if ctx.needs_input_grad[0]:
+            gx = _crop_shift(g.contiguous(), im_size, padded_size, maps, apod, modulate=modulate)
+        return gx, None, None, None, None, None
+
+
+class _CropShiftFn(torch.autograd.Function):
+    """alpha * crop_shift(z) + beta * add: the backward pass is alpha *
+    pad_shift(g) for z and beta * g for add."""
+
+    @staticmethod
+    def forward(ctx, z, add, im_size, padded_size, maps, apod, alpha, beta, modulate):
+        ctx.args = (tuple(im_size), tuple(padded_size), maps, apod, alpha, beta, modulate)
+        return _crop_shift(z, im_size, padded_size, maps, apod, alpha, add, beta, modulate)
+
+    @staticmethod
+    def backward(ctx, g):
+        im_size, padded_size, maps, apod, alpha, beta, modulate = ctx.args
+        gz = gadd = None
+        if ctx.needs_input_grad[0]:
+            gz = _pad_shift(g.contiguous(), im_size, padded_size, maps, apod, modulate)
+            if alpha != 1.0:
+                gz = gz * alpha
+        if ctx.needs_input_grad[1]:
+            gadd = g * beta
+        return gz, gadd, None, None, None, None, None, None, None
+
+
+def pad_shift(x: Tensor, im_size, padded_size, maps: Optional[Tensor] = None, apod: Optional[Tensor] = None,
+              modulate: bool = False) -> Tensor:
+    """ifftshift(pad(apod * x)) (or per coil map: ifftshift(pad(maps_c * apod * x)))
+    over the last ``len(im_size)`` dims in one pass; complex64, CUDA.
+    ``modulate`` multiplies by m[j] = prod_e exp(2 pi i j_e floor(Np_e/2) / Np_e)
+    (the sign (-1)^j_e for even sizes), so that an uncentred fftn of the
+    result is the centred cfftn of the padded image. Differentiable in ``x``."""
+    if torch.is_grad_enabled() and x.requires_grad:
+        return _PadShiftFn.apply(x, im_size, padded_size, maps, apod, modulate)
+    return _pad_shift(x, im_size, padded_size, maps, apod, modulate)
+
+
+def crop_shift(z: Tensor, im_size, padded_size, maps: Optional[Tensor] = None, apod: Optional[Tensor] = None,
+               alpha: float = 1.0, add: Optional[Tensor] = None, beta: float = 0.0, modulate: bool = False) -> Tensor:
+    """alpha * apod * crop(fftshift(z)) (with maps: summed over the coil dim of
+    z after multiplying by conj(maps)) + beta * add, in one pass; with
+    ``modulate``, z is first multiplied by conj(m[j]) (the adjoint of
+    pad_shift's modulation). Differentiable in ``z`` and ``add``."""
+    if torch.is_grad_enabled() and (z.requires_grad or (add is not None and add.requires_grad)):
+        return _CropShiftFn.apply(z, add, im_size, padded_size, maps, apod, alpha, beta, modulate)
+    return _crop_shift(z, im_size, padded_size, maps, apod, alpha, add, beta, modulate)
+
+
 class PadShift(NamedLinop):
-    """apod * x, centred zero pad and ifftshift in one pass; the adjoint is
-    fftshift, crop and apod in one pass. With an uncentred FFT after it and
-    the trajectory shifted by -floor(Np/2), this is the reference's
-    Apodize -> Pad -> cfftn (nufft.py:170-184) without the two shift passes
-    per transform."""
+    """apod * x, centred zero pad, ifftshift and the k-space centring
+    modulation in one pass; the adjoint is the conjugate modulation,
+    fftshift, crop and apod in one pass. With an uncentred FFT after it, this
+    is the reference's Apodize -> Pad -> cfftn (nufft.py:170-184) without
+    the two shift passes per transform, and the interpolation after it reads
+    the reference's own coordinates."""
 
     def __init__(self, padded_size, im_size, apod: Optional[Tensor] = None):
         super().__init__()
@@ -348,11 +412,11 @@ class PadShift(NamedLinop):
 
     @staticmethod
     def fn(p, x, /):
-        return pad_shift(x, p.im_size, p.pad_im_size, apod=p.apod)
+        return pad_shift(x, p.im_size, p.pad_im_size, apod=p.apod, modulate=True)
 
     @staticmethod
     def adj_fn(p, y, /):
-        return crop_shift(y, p.im_size, p.pad_im_size, apod=p.apod)
+        return crop_shift(y, p.im_size, p.pad_im_size, apod=p.apod, modulate=True)
 
 
 class FFT(NamedLinop):
@@ -499,16 +563,6 @@ def prep_locs(locs: Tensor, grid_size, padded_size, pad_mode="circular") -> Tens
     return out
 
 
-def prep_locs_shifted(locs: Tensor, grid_size, padded_size) -> Tensor:
-    """prep_locs (circular) minus floor(Np/2): the trajectory on which an
-    uncentred FFT's output is read where the reference reads fftshift(FFT)."""
-    out = locs.clone()
-    for i in range(-len(grid_size), 0):
-        out[..., i] *= padded_size[i] / grid_size[i]
-        out[..., i] = torch.remainder(out[..., i], torch.tensor(padded_size[i], device=locs.device))
-    return out
-
-
 def apodize_weights(grid_size, padded_size, oversamp, width: float, beta: float) -> Tensor:
     """Separable KB apodization (nufft.py:349-365)."""
     gs = torch.tensor(grid_size)
@@ -550,12 +604,11 @@ class NUFFT(Chain):
         if weight.isnan().any() or weight.isinf().any():
             raise ValueError(f"Nan/Inf values detected in apodization weight (width={width}, oversamp={oversamp}).")
         # Apodize -> Pad -> cfftn, with both centring shifts folded into the
-        # pad and the trajectory (no full-grid shift passes); same operator
+        # pad gather (no full-grid shift passes); same operator, same
+        # interpolation coordinates as the reference
         padshift = PadShift(padded_size, grid_size, weight)
         fft = FFT(ndim=locs.shape[-1], centered=False, norm="ortho")
-        locs_prepared = (prep_locs_shifted(locs, grid_size, padded_size) if do_prep_locs
-                         else torch.remainder(locs - torch.tensor([p // 2 for p in padded_size], device=device,
-                                                                  dtype=locs.dtype), torch.tensor(padded_size, device=device, dtype=locs.dtype)))
+        locs_prepared = prep_locs(locs, grid_size, padded_size) if do_prep_locs else locs
         interp = Interpolate(
             locs_prepared, padded_size, width=width, kernel="kaiser_bessel", kernel_params=dict(beta=beta)
         )
@@ -565,7 +618,7 @@ class NUFFT(Chain):
         self.apodize_weight = weight
         self.scale_factor = scale_factor
         self.padded_size = padded_size
-        self.locs_shifted = locs_prepared
+        self.locs_prepared = locs_prepared
         self.locs = locs
         self.grid_size = tuple(grid_size)
         self.oversamp = oversamp
@@ -575,27 +628,57 @@ class NUFFT(Chain):
         self.interp = interp
 
 
+_PREPARED_LOCS: "OrderedDict[tuple, tuple]" = OrderedDict()
+
+
+def _prepared_locs(locs: Tensor, grid_size, padded) -> Tensor:
+    """prep_locs for the functional transforms, memoised per locs tensor
+    (object, version, weak reference) so that repeated calls on one
+    trajectory reuse one interpolation plan. Locations that require a
+    gradient are rescaled afresh (a trajectory being optimised changes every
+    step, and the result carries the autograd graph)."""
+    if locs.requires_grad and torch.is_grad_enabled():
+        return prep_locs(locs, grid_size, padded)
+    key = (id(locs), locs.data_ptr(), tuple(locs.shape), locs.dtype, tuple(grid_size), tuple(padded))
+    hit = _PREPARED_LOCS.get(key)
+    if hit is not None:
+        ref, version, out = hit
+        if ref() is locs and version == locs._version:
+            _PREPARED_LOCS.move_to_end(key)
+            return out
+        del _PREPARED_LOCS[key]
+    out = prep_locs(locs.detach(), grid_size, padded)
+    _PREPARED_LOCS[key] = (weakref.ref(locs), locs._version, out)
+    while len(_PREPARED_LOCS) > 16:
+        _PREPARED_LOCS.popitem(last=False)
+    return out
+
+
 def nufft(x: Tensor, locs: Tensor, oversamp: float = 1.25, width: float = 4.0) -> Tensor:
-    """Functional NUFFT (functional/_nufft.py:16-62)."""
+    """Functional NUFFT (functional/_nufft.py:16-62). Differentiable in ``x``
+    and ``locs``."""
     grid_size = tuple(x.shape[-locs.shape[-1]:])
     ndim = locs.shape[-1]
     padded = tuple(int(s * oversamp) for s in grid_size)
     beta = nufft_beta(width, oversamp)
-    x = pad_shift(x, grid_size, padded, apod=apodize_weights(grid_size, padded, oversamp, width, beta).to(x.device))
+    x = pad_shift(x, grid_size, padded, apod=apodize_weights(grid_size, padded, oversamp, width, beta).to(x.device),
+                  modulate=True)
     x = torch.fft.fftn(x, dim=tuple(range(-ndim, 0)), norm="ortho")
-    x = I.interpolate(x, prep_locs_shifted(locs, grid_size, padded), width, kernel="kaiser_bessel",
+    x = I.interpolate(x, _prepared_locs(locs, grid_size, padded), width, kernel="kaiser_bessel",
                       kernel_params=dict(beta=beta))
     return x / (width**ndim * (prod(grid_size) / prod(padded)) ** 0.5)
 
 
 def nufft_adjoint(x: Tensor, locs: Tensor, grid_size, oversamp: float = 1.25, width: float = 4.0) -> Tensor:
-    """Functional adjoint NUFFT (functional/_nufft.py:65-112)."""
+    """Functional adjoint NUFFT (functional/_nufft.py:65-112). Differentiable
+    in ``x`` and ``locs``."""
     grid_size = tuple(grid_size)
     ndim = locs.shape[-1]
     padded = tuple(int(s * oversamp) for s in grid_size)
     beta = nufft_beta(width, oversamp)
     x = x / (width**ndim * (prod(grid_size) / prod(padded)) ** 0.5)
-    x = I.interpolate_adjoint(x, prep_locs_shifted(locs, grid_size, padded), padded, width, kernel="kaiser_bessel",
+    x = I.interpolate_adjoint(x, _prepared_locs(locs, grid_size, padded), padded, width, kernel="kaiser_bessel",
                               kernel_params=dict(beta=beta))
     x = torch.fft.ifftn(x, dim=tuple(range(-ndim, 0)), norm="ortho")
-    return crop_shift(x, grid_size, padded, apod=apodize_weights(grid_size, padded, oversamp, width, beta).to(x.device))
+    return crop_shift(x, grid_size, padded, apod=apodize_weights(grid_size, padded, oversamp, width, beta).to(x.device),
+                      modulate=True)

@@ -153,8 +153,9 @@ def power_method(A, v: Tensor, iters: int = 30) -> float:
 class SenseNormal:
     """x -> s * sum_c conj(S_c) F^H F (S_c x) + lam * x for an n^3 image.
 
-    F is this package's NUFFT. The coil maps, apodization, pad and centring
-    shift go in one pass (``linops.pad_shift``) and the way back (shift, crop,
+    F is this package's NUFFT. The coil maps, apodization, pad and both
+    centring shifts (the k-space one as a modulation) go in one pass
+    (``linops.pad_shift``) and the way back (modulation, shift, crop,
     apodization, conj maps, coil sum, scale and the lam x term) in another
     (``linops.crop_shift``); between them one FFT, one gather, one gridding
     and one inverse FFT for all coils at once."""
@@ -173,14 +174,14 @@ class SenseNormal:
 
     def _normal(self, x: Tensor, lam: float) -> Tensor:
         F = self.F
-        z = linops.pad_shift(x, self.n, F.padded_size, maps=self.maps, apod=F.apodize_weight)
+        z = linops.pad_shift(x, self.n, F.padded_size, maps=self.maps, apod=F.apodize_weight, modulate=True)
         z = torch.fft.fftn(z, dim=(-3, -2, -1), norm="ortho")
         y = F.interp(z)
         g = F.interp.H(y)
         g = torch.fft.ifftn(g, dim=(-3, -2, -1), norm="ortho")
         alpha = self.scale / F.scale_factor**2
         return linops.crop_shift(g, self.n, F.padded_size, maps=self.maps, apod=F.apodize_weight, alpha=alpha,
-                                 add=x if lam != 0.0 else None, beta=lam)
+                                 add=x if lam != 0.0 else None, beta=lam, modulate=True)
 
     def data_normal(self, x: Tensor) -> Tensor:
         return self._normal(x, 0.0)
