@@ -9,7 +9,7 @@ restates, independently of the CUDA code, which pairs exist and their order:
   ``oracle.interp``: ``lower = ceil(x - W/2)``, taps ``lower + k`` with
   ``|d| <= W/2`` and, for Kaiser-Bessel, ``|d| <= 1``; zero padding drops
   taps outside ``[0, N)``, circular padding wraps them);
-* tiles are 8^3 in 3D, 32 x 32 in 2D and 512 in 1D (clipped to the grid),
+* tiles are 8^3 in 3D, 16 x 16 in 2D and 512 in 1D (clipped to the grid),
   numbered ``(t0 * nt1 + t1) * nt2 + t2`` over internal dims padded to 3;
 * a point pairs with every tile that one of its valid taps lands in (the
   product of the distinct tiles per axis, at most 3 per axis); its home pair
@@ -35,7 +35,7 @@ __all__ = ["tile_shape", "plan_pairs"]
 def tile_shape(grid_size):
     nd = len(grid_size)
     N = (1,) * (3 - nd) + tuple(int(n) for n in grid_size)
-    T = {3: (8, 8, 8), 2: (1, 32, 32), 1: (1, 1, 512)}[nd]
+    T = {3: (8, 8, 8), 2: (1, 16, 16), 1: (1, 1, 512)}[nd]
     T = tuple(min(t, n) for t, n in zip(T, N))
     nt = tuple(-(-n // t) for n, t in zip(N, T))
     return N, T, nt

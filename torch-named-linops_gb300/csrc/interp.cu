@@ -1839,7 +1839,7 @@ int make_geo(const tlgb_interp_desc* d, Geo& g) {
     maxnt = std::max(maxnt, nt);
   }
   if (d->ndim == 3 && maxnt > 9) TLGB_FAIL(TLGB_ERR_UNSUPPORTED, "3D kernel width must be below 8 grid units");
-  const int T3[3] = {8, 8, 8}, T2[3] = {1, 32, 32}, T1[3] = {1, 1, 512};
+  const int T3[3] = {8, 8, 8}, T2[3] = {1, 16, 16}, T1[3] = {1, 1, 512};
   const int* T = d->ndim == 3 ? T3 : (d->ndim == 2 ? T2 : T1);
   g.wrap_safe = 1;
   g.tv_off = -1;
