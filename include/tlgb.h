@@ -160,13 +160,20 @@ int tlgb_interp_adjoint(const tlgb_interp_desc* d, const tlgb_interp_plan_info* 
 int tlgb_interp_adjoint_fixed(const tlgb_interp_desc* d, const tlgb_interp_plan_info* info, const void* plan,
                               const float* locs, const void* vals, void* grid, tlgb_stream_t stream);
 
+/* Scratch bytes tlgb_interp_grad_locs can use to split a batch of many
+ * coil groups over several CTAs per tile (0 when it would not split). */
+int tlgb_interp_grad_scratch_size(const tlgb_interp_desc* d, const tlgb_interp_plan_info* info, size_t* bytes);
+
 /* grad_locs[p, e] = sum_b Re( conj(a[b, p]) * sum_taps dw(p, tap)/dx_e * grid[b, tap] )
  * -- the gradient w.r.t. the trajectory of sum Re(conj(a) * ungrid(grid)),
  * and (with grid := the output cotangent, a := the point values) of the
- * gridding operator. Written, not accumulated. */
+ * gridding operator. Written, not accumulated. With scratch of at least
+ * tlgb_interp_grad_scratch_size bytes the coil groups are split over CTAs
+ * and their partial sums added in a fixed order (deterministic); with less
+ * (or NULL) one CTA per tile walks all coil groups. */
 int tlgb_interp_grad_locs(const tlgb_interp_desc* d, const tlgb_interp_plan_info* info, const void* plan,
-                          const float* locs, const void* grid, const void* a, float* grad_locs,
-                          tlgb_stream_t stream);
+                          const float* locs, const void* grid, const void* a, float* grad_locs, void* scratch,
+                          size_t scratch_bytes, tlgb_stream_t stream);
 
 /* ------------------------------------------------------------------------ */
 /* ArrayToBlocks / BlocksToArray (unfold / fold), 1D-3D.                      */

@@ -1670,7 +1670,8 @@ __global__ void __launch_bounds__(NTHR) interp_grad_kernel(Geo g, const int4* __
                                                               const int32_t* __restrict__ entries,
                                                               const float* __restrict__ locs,
                                                               const V* __restrict__ gridv, const V* __restrict__ a,
-                                                              float* __restrict__ grad, int CG, int chunk) {
+                                                              float* __restrict__ grad, int CG, int chunk,
+                                                              float* __restrict__ partial) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int4 it = items[blockIdx.x];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1701,7 +1702,11 @@ __global__ void __launch_bounds__(NTHR) interp_grad_kernel(Geo g, const int4* __
   const int q = lane >> lgc;
   const int QN = 32 >> lgc;
   const int ncg = (int)((g.nbatch + CG - 1) / CG);
-  for (int cg = 0; cg < ncg; ++cg) {
+  // blockIdx.y takes a contiguous share of the coil groups (all of them when
+  // gridDim.y == 1); its sums go to its partial slot
+  const int gps = (ncg + (int)gridDim.y - 1) / (int)gridDim.y;
+  const int cg_end = min(ncg, ((int)blockIdx.y + 1) * gps);
+  for (int cg = (int)blockIdx.y * gps; cg < cg_end; ++cg) {
     const int c0 = cg * CG;
     const int ncoil = (int)min((long long)CG, g.nbatch - c0);
     __syncthreads();
@@ -1781,10 +1786,21 @@ __global__ void __launch_bounds__(NTHR) interp_grad_kernel(Geo g, const int4* __
     }
   }
   __syncthreads();
+  float* dst = gridDim.y == 1 ? grad : partial + (long long)blockIdx.y * g.npts * g.ndim;
   for (int i = threadIdx.x; i < npt; i += NTHR) {
     const long long p = entries[it.y + i];
-    for (int e = 3 - g.ndim; e < 3; ++e) grad[p * g.ndim + (e - (3 - g.ndim))] = gacc[i * 3 + e];
+    for (int e = 3 - g.ndim; e < 3; ++e) dst[p * g.ndim + (e - (3 - g.ndim))] = gacc[i * 3 + e];
   }
+}
+
+// grad[i] = sum over slots s of partial[s][i], in slot order
+__global__ void __launch_bounds__(256) grad_reduce_kernel(const float* __restrict__ partial, int nsplit, long long n,
+                                                          float* __restrict__ grad) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float s = partial[i];
+  for (int k = 1; k < nsplit; ++k) s += partial[(long long)k * n + i];
+  grad[i] = s;
 }
 
 // ------------------------------------------------------------- host helpers
@@ -1971,6 +1987,21 @@ int grad_cg(const Geo& g, size_t taps_bytes) {
 
 size_t grad_smem(const Geo& g, int cg, size_t taps_bytes) {
   return (size_t)region_vol(g) * cg * value_size(g) + NWARP * taps_bytes;
+}
+
+// Parts the coil groups of the trajectory gradient are split into: enough
+// CTAs to fill the device when a plan has few tiles and the batch many
+// groups (each part restages the region and re-evaluates the taps).
+int grad_splits(const Geo& g, const tlgb_interp_plan_info* info) {
+  const int cg = grad_cg(g, sizeof(PTaps<true>));
+  const long long ncg = cdiv(std::max<long long>(g.nbatch, 1), cg);
+  const long long items = std::max<long long>(info->n_fwd_items, 1);
+  const long long want = cdiv(8ll * sm_count(), items);  // ~8 CTAs per SM
+  return (int)std::max(1ll, std::min(ncg, want));
+}
+
+size_t grad_scratch_bytes(const Geo& g, int nsplit) {
+  return nsplit > 1 ? (size_t)nsplit * g.npts * g.ndim * sizeof(float) : 0;
 }
 
 int check_plan(const Geo& g, const tlgb_interp_plan_info* info, const void* plan) {
@@ -2299,15 +2330,26 @@ int launch_adj(const Geo& g, const tlgb_interp_plan_info* info, const char* P, c
 
 template <typename V, int NORM>
 int launch_grad(const Geo& g, const tlgb_interp_plan_info* info, const char* P, const float* locs, const void* grid,
-                const void* a, float* grad, cudaStream_t s) {
+                const void* a, float* grad, void* scratch, size_t scratch_bytes, cudaStream_t s) {
   const int cg = grad_cg(g, sizeof(PTaps<true>));
   const size_t sm = grad_smem(g, cg, sizeof(PTaps<true>)) + kFwdChunk * 3 * sizeof(float);
   auto* k = interp_grad_kernel<V, NORM>;
   TLGB_TRY(set_smem(k, sm));
-  k<<<(unsigned)info->n_fwd_items, NTHR, sm, s>>>(g, (const int4*)(P + info->off_fwd_items),
-                                                  (const int32_t*)(P + info->off_entries), locs, (const V*)grid,
-                                                  (const V*)a, grad, cg, (int)kFwdChunk);
+  int nsplit = grad_splits(g, info);
+  const size_t need = grad_scratch_bytes(g, nsplit);
+  if (!scratch || scratch_bytes < need) nsplit = 1;  // one pass over all coil groups per tile
+  float* partial = static_cast<float*>(scratch);
+  const long long n = (long long)g.npts * g.ndim;
+  if (nsplit > 1 && info->n_home < g.npts)  // points without taps get no partial writes
+    TLGB_CUDA(cudaMemsetAsync(partial, 0, need, s));
+  dim3 grd((unsigned)info->n_fwd_items, (unsigned)nsplit);
+  k<<<grd, NTHR, sm, s>>>(g, (const int4*)(P + info->off_fwd_items), (const int32_t*)(P + info->off_entries), locs,
+                          (const V*)grid, (const V*)a, grad, cg, (int)kFwdChunk, partial);
   TLGB_CHECK_LAUNCH();
+  if (nsplit > 1) {
+    grad_reduce_kernel<<<(unsigned)cdiv(n, 256), 256, 0, s>>>(partial, nsplit, n, grad);
+    TLGB_CHECK_LAUNCH();
+  }
   return TLGB_OK;
 }
 
@@ -2346,9 +2388,18 @@ extern "C" int tlgb_interp_adjoint(const tlgb_interp_desc* d, const tlgb_interp_
   return launch_adj(g, info, P, locs, vals, grid, scratch, s);
 }
 
+extern "C" int tlgb_interp_grad_scratch_size(const tlgb_interp_desc* d, const tlgb_interp_plan_info* info,
+                                             size_t* bytes) {
+  Geo g;
+  TLGB_TRY(make_geo(d, g));
+  if (!info || !bytes) TLGB_FAIL(TLGB_ERR_INVALID, "null pointer");
+  *bytes = grad_scratch_bytes(g, grad_splits(g, info));
+  return TLGB_OK;
+}
+
 extern "C" int tlgb_interp_grad_locs(const tlgb_interp_desc* d, const tlgb_interp_plan_info* info, const void* plan,
                                      const float* locs, const void* grid, const void* a, float* grad_locs,
-                                     tlgb_stream_t stream) {
+                                     void* scratch, size_t scratch_bytes, tlgb_stream_t stream) {
   Geo g;
   TLGB_TRY(make_geo(d, g));
   TLGB_TRY(check_plan(g, info, plan));
@@ -2360,10 +2411,10 @@ extern "C" int tlgb_interp_grad_locs(const tlgb_interp_desc* d, const tlgb_inter
   if (g.nbatch == 0 || info->n_fwd_items == 0) return TLGB_OK;
   const char* P = (const char*)plan;
   if (g.cplx)
-    return g.norm == 1 ? launch_grad<float2, 1>(g, info, P, locs, grid, a, grad_locs, s)
-                       : launch_grad<float2, 2>(g, info, P, locs, grid, a, grad_locs, s);
-  return g.norm == 1 ? launch_grad<float, 1>(g, info, P, locs, grid, a, grad_locs, s)
-                     : launch_grad<float, 2>(g, info, P, locs, grid, a, grad_locs, s);
+    return g.norm == 1 ? launch_grad<float2, 1>(g, info, P, locs, grid, a, grad_locs, scratch, scratch_bytes, s)
+                       : launch_grad<float2, 2>(g, info, P, locs, grid, a, grad_locs, scratch, scratch_bytes, s);
+  return g.norm == 1 ? launch_grad<float, 1>(g, info, P, locs, grid, a, grad_locs, scratch, scratch_bytes, s)
+                     : launch_grad<float, 2>(g, info, P, locs, grid, a, grad_locs, scratch, scratch_bytes, s);
 }
 
 // ------------------------------------------------ gridding without allocation

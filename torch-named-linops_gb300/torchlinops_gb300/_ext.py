@@ -104,7 +104,8 @@ _SIGNATURES = {
     "tlgb_interp_adjoint_scratch_size": ([_P, _P, _P], ctypes.c_int),
     "tlgb_interp_forward": ([_P, _P, _P, _P, _P, _P, _P], ctypes.c_int),
     "tlgb_interp_adjoint": ([_P, _P, _P, _P, _P, _P, _P, ctypes.c_size_t, _P], ctypes.c_int),
-    "tlgb_interp_grad_locs": ([_P, _P, _P, _P, _P, _P, _P, _P], ctypes.c_int),
+    "tlgb_interp_grad_scratch_size": ([_P, _P, ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
+    "tlgb_interp_grad_locs": ([_P, _P, _P, _P, _P, _P, _P, _P, ctypes.c_size_t, _P], ctypes.c_int),
     "tlgb_interp_adjoint_fixed": ([_P, _P, _P, _P, _P, _P, _P], ctypes.c_int),
     "tlgb_unfold": ([_P, _P, _P, _P], ctypes.c_int),
     "tlgb_fold": ([_P, _P, _P, _P], ctypes.c_int),

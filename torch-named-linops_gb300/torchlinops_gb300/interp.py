@@ -306,11 +306,16 @@ def _grad_locs(gridvals: Tensor, a: Tensor, locs: Tensor, width, kernel, norm, p
     av = _as_f32_view(a.reshape(nbatch, npts), is_complex)
     out = torch.empty(npts, ndim, dtype=torch.float32, device=dev)
     lc = _locs_f32(locs)
+    L = _ext.lib()
+    sb = ctypes.c_size_t(0)
+    _ext.check(L.tlgb_interp_grad_scratch_size(ctypes.byref(d), ctypes.byref(plan.info), ctypes.byref(sb)),
+               "trajectory gradient")
+    scratch = torch.empty(max(sb.value, 1), dtype=torch.uint8, device=dev)
     with torch.cuda.device(dev):
         _ext.check(
-            _ext.lib().tlgb_interp_grad_locs(
+            L.tlgb_interp_grad_locs(
                 ctypes.byref(d), ctypes.byref(plan.info), _ext.ptr(plan.buffer), _ext.ptr(lc), _ext.ptr(g),
-                _ext.ptr(av), _ext.ptr(out), _ext.stream_ptr(dev),
+                _ext.ptr(av), _ext.ptr(out), _ext.ptr(scratch), sb.value, _ext.stream_ptr(dev),
             ),
             "trajectory gradient",
         )
