@@ -265,7 +265,9 @@ def run_gpu(args, world, rank, local):
     plan = get_plan(locs, (N_GRID,) * 3, WIDTH, "kaiser_bessel", "circular", beta)
     torch.cuda.synchronize()
     plan_ms = (time.perf_counter() - t0) * 1e3
-    launches_per_step = 2 + (1 if plan.info.n_split_tiles > 0 else 0)
+    # per step: the gather, the point-major value transpose, the gridding and
+    # (when dense tiles are split) the ordered sum of their parts
+    launches_per_step = 3 + (1 if plan.info.n_split_tiles > 0 else 0)
 
     stream = torch.cuda.current_stream(dev)
     for _ in range(args.warmup):
