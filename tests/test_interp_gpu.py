@@ -134,6 +134,36 @@ def test_eight_entry_3d_paths_against_oracle(shape, nb, pad):
     assert rel_l2(adj, o32a) < TOL and rel_l2(adj, o64a) < TOL
 
 
+@pytest.mark.parametrize("shape", [(160, 144), (90, 61)])
+@pytest.mark.parametrize("nb", [8, 11])
+@pytest.mark.parametrize("pad", ["circular", "zero"])
+def test_eight_entry_2d_paths_against_oracle(shape, nb, pad):
+    """2D, 8 complex entries per group: the TMA-staged gather (even Z) and its
+    plain-load fallback (odd Z, wrapping edge regions), a ragged last group,
+    dense tiles, points across every edge and exact-integer points."""
+    from torchlinops_gb300 import _ext
+
+    gen = torch.Generator().manual_seed(nb + len(pad) + shape[1])
+    n = torch.tensor(shape, dtype=torch.float32)
+    ball = _ball_locs(20000, 10.0, n / 2, gen, ndim=2)
+    spread = torch.rand(20000, 2, generator=gen) * (n + 4) - 2  # edges and a little outside
+    ints = torch.randint(0, min(shape), (500, 2), generator=gen).to(torch.float32)
+    locs = torch.cat([ball, spread, ints])
+    npts = locs.shape[0]
+    img = torch.complex(torch.randn(nb, *shape, generator=gen), torch.randn(nb, *shape, generator=gen))
+    pts = torch.complex(torch.randn(nb, npts, generator=gen), torch.randn(nb, npts, generator=gen))
+    beta = OI.nufft_beta(4.0, 1.25)
+    kw = dict(kernel="kaiser_bessel", pad_mode=pad)
+    _ext.device_status(clear=True)
+    fwd = T.ungrid(img.to(DEV), locs.to(DEV), 4.0, kernel_params=dict(beta=beta), **kw).cpu()
+    adj = T.grid(pts.to(DEV), locs.to(DEV), shape, 4.0, kernel_params=dict(beta=beta), **kw).cpu()
+    assert _ext.device_status() == 0
+    assert rel_l2(fwd, OI.ungrid(img, locs, 4.0, beta=beta, **kw)) < TOL
+    assert rel_l2(fwd, OI.ungrid(img, locs, 4.0, beta=beta, dtype=torch.float64, **kw)) < TOL
+    assert rel_l2(adj, OI.grid(pts, locs, shape, 4.0, beta=beta, **kw)) < TOL
+    assert rel_l2(adj, OI.grid(pts, locs, shape, 4.0, beta=beta, dtype=torch.float64, **kw)) < TOL
+
+
 @pytest.mark.parametrize("kernel", ["kaiser_bessel", "spline"])
 def test_grid_nonfinite_values_stay_in_their_windows(kernel):
     """A NaN or Inf point value turns exactly the cells of its window

@@ -942,6 +942,13 @@ __global__ void point_records_kernel(Geo g, const float* __restrict__ locs, PRec
   for (int e = 0; e < 3; ++e) {
     float w0 = 0.f, w1 = 0.f, w2 = 0.f, w3 = 0.f;
     int c = 0, st = 0;
+    if (!g.act[e]) {
+      // a leading dimension of a 2D geometry: one tap of weight 1 at 0
+      R.w[e] = make_float4(1.f, 0.f, 0.f, 0.f);
+      R.st[e] = 0;
+      cnt |= 1 << (4 * e);
+      continue;
+    }
     const float x = load_coord(g, locs, p, e);
     if (coord_ok(x)) {
       const int lower = lower_of(g, e, x);
@@ -1623,6 +1630,209 @@ __global__ void __launch_bounds__(256, 2) fwd_f3_kernel(const __grid_constant__ 
   }
 }
 
+// The gather view of a home record in the 20 x 20 region of a 2D tile at o:
+// region base (y * 20 + z, 9 bits) | my << 11 | mz << 14 | fast << 20 |
+// ok << 21 (the bit positions of region_view).
+__device__ __forceinline__ unsigned region_view2(const Geo& g, const PRec& R, const int (&o)[3]) {
+  const int c = R.cnt;
+  const int cy = (c >> 4) & 15, cz = (c >> 8) & 15;
+  const bool ok = (c & 15) && cy && cz;
+  int f[3];
+#pragma unroll
+  for (int e = 1; e < 3; ++e) {
+    int d = R.st[e] - o[e];
+    if (g.pad == TLGB_PAD_CIRCULAR && d < 0) d += g.N[e];
+    f[e] = d;
+  }
+  const bool fast = ok && cy <= 4 && cz <= 4 && f[1] >= 0 && f[1] < 16 && f[2] >= 0 && f[2] < 16;
+  const unsigned base = fast ? (unsigned)(f[1] * 20 + f[2]) : 0u;
+  return base | (min(cy, 7) << 11) | (min(cz, 7) << 14) | ((fast ? 1u : 0u) << 20) | ((ok ? 1u : 0u) << 21);
+}
+
+// 2D gather: CTA = 8 warps sharing the 20 x 20 x 8-entry region
+// ([entry][y][z]) of one 16 x 16 tile, loaded by one TMA bulk tensor copy
+// when the region needs no wrap. Each warp takes every 8th point of the
+// item, building the records of its next 8 points itself, two mini-batches
+// ahead. Lanes = (entry, z-tap): a lane sums its entry's 4 y-taps, two points
+// at a time, then the 4 z-tap lanes of each entry add up; the y taps of entry
+// c start at row (c & 3), so one load instruction spans 4 bank windows.
+__global__ void __launch_bounds__(256, 3) fwd_f2_kernel(const __grid_constant__ CUtensorMap tmap, int use_tma, Geo g,
+                                                        const int4* __restrict__ items,
+                                                        const int32_t* __restrict__ entries,
+                                                        const PRec* __restrict__ precs,
+                                                        const float* __restrict__ locs,
+                                                        const float* __restrict__ gridv, float* __restrict__ out) {
+  constexpr int CG = 8, S = 20, VOL = S * S, NW = 8;
+  constexpr uint32_t RBYTES = VOL * CG * 8;
+  extern __shared__ __align__(128) unsigned char smem[];
+  float2* reg = reinterpret_cast<float2*>(smem);               // [8][20][20]
+  R3* rec = reinterpret_cast<R3*>(smem + RBYTES);              // [8 warps][8]
+  Rec<5>* slow = reinterpret_cast<Rec<5>*>(rec + 64);          // [NW]
+  static_assert((64 * sizeof(R3) + NW * sizeof(Rec<5>)) % 8 == 0, "mbarrier alignment");
+  uint64_t* bar = reinterpret_cast<uint64_t*>(slow + NW);
+  const int4 it = items[blockIdx.x];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int c0 = blockIdx.y * CG;
+  int o[3];
+  {
+    int t = it.x;
+    o[2] = (t % g.nt[2]) * g.T[2];
+    t /= g.nt[2];
+    o[1] = (t % g.nt[1]) * g.T[1];
+    o[0] = 0;
+  }
+  const bool wraps = g.pad == TLGB_PAD_CIRCULAR && (o[1] + S > g.N[1] || o[2] + S > g.N[2]);
+  const bool tma = use_tma && !wraps;
+  if (tma) {
+    if (tid == 0) {
+      mbar_init(bar, 1);
+      fence_mbar_init();
+    }
+    __syncthreads();
+    if (tid == 0) {
+      mbar_arrive_expect_tx(bar, RBYTES);
+      tma_load_4d(reg, &tmap, bar, o[2], o[1], 0, c0);
+    }
+  } else {
+    // plain loads with wrap / zero fill: rows (entry, y) of 20 z
+    const int ncoil = (int)min((long long)CG, g.nbatch - c0);
+    const long long gvol = (long long)g.N[1] * g.N[2];
+    for (int idx = tid; idx < CG * VOL; idx += NW * 32) {
+      const int z = idx % S;
+      const int r = idx / S;
+      const int y = r % S, c = r / S;
+      int gy = o[1] + y, gz = o[2] + z;
+      bool in = c < ncoil;
+      if (g.pad == TLGB_PAD_CIRCULAR) {
+        gy = wrapi(gy, g.N[1]);
+        gz = wrapi(gz, g.N[2]);
+      } else {
+        in = in && gy < g.N[1] && gz < g.N[2];
+      }
+      reg[idx] = in ? __ldg(reinterpret_cast<const float2*>(gridv) + (long long)(c0 + c) * gvol +
+                           (long long)gy * g.N[2] + gz)
+                    : make_float2(0.f, 0.f);
+    }
+  }
+  const int c = lane >> 2, kz = lane & 3;
+  int kyo[4], rowoff[4];
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    kyo[t] = (t + c) & 3;
+    rowoff[t] = kyo[t] * S;
+  }
+  R3* wrec = rec + warp * 8;
+  const int npt = it.z - it.y;
+  auto point_at = [&](int base) -> int {
+    const int j = base + 8 * lane;
+    return (lane < 8 && j < npt) ? entries[it.y + j] : -1;
+  };
+  auto fetch = [&](int p) {
+    PRec R;
+    if (p >= 0) R = load_prec(precs, p);
+    return R;
+  };
+  auto publish = [&](int p, const PRec& R) {
+    if (p >= 0) {
+      R3& Sr = wrec[lane];
+      Sr.w[0] = R.w[0];
+      Sr.w[1] = R.w[1];
+      Sr.w[2] = R.w[2];
+      Sr.view = region_view2(g, R, o);
+      Sr.p = p;
+    }
+    __syncwarp();
+  };
+  int pc = point_at(warp);
+  int pn = point_at(warp + 8 * NW);
+  PRec Rc = fetch(pc);
+  auto build_records = [&](int base) {
+    publish(pc, Rc);
+    Rc = fetch(pn);
+    pc = pn;
+    pn = point_at(base + 16 * NW);
+  };
+  build_records(warp);  // while the region copy is in flight
+  {
+    bool ok = true;
+    if (tma && tid == 0) ok = mbar_wait_bounded(bar, 0, 1u << 22);
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) atomicExch(&g_tlgb_status, 1);
+      return;
+    }
+  }
+  // sum over y taps of wy wz v; weights are zero past a record's tap count
+  // and every tap of the 4 x 4 box lies inside the region
+  auto gather_box = [&](const R3& R) {
+    const float wz = (&R.w[2].x)[kz];
+    const float* wy = &R.w[1].x;
+    const float2* a = reg + c * VOL + (R.view & 2047) + kz;
+    float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const float w = wy[kyo[t]] * wz;
+      const float2 v = a[rowoff[t]];
+      acc.x = fmaf(w, v.x, acc.x);
+      acc.y = fmaf(w, v.y, acc.y);
+    }
+    return acc;
+  };
+  auto gather_rec = [&](const R3& R) {
+    if (lane == 0) {
+      float x3[3] = {0.f, 0.f, 0.f};
+      for (int e = 1; e < 3; ++e) x3[e] = load_coord(g, locs, R.p, e);
+      lane_rec<5>(g, x3, o, true, slow[warp]);
+    }
+    __syncwarp();
+    const Rec<5>& Sr = slow[warp];
+    float2 acc = make_float2(0.f, 0.f);
+    if (Sr.m[0] > 0)
+      for (int kzz = kz; kzz < Sr.m[2]; kzz += 4)
+        for (int kyy = 0; kyy < Sr.m[1]; ++kyy) {
+          const float w = Sr.wv[1][kyy] * Sr.wv[2][kzz];
+          const float2 v = reg[c * VOL + Sr.lc[1][kyy] * S + Sr.lc[2][kzz]];
+          acc.x = fmaf(w, v.x, acc.x);
+          acc.y = fmaf(w, v.y, acc.y);
+        }
+    __syncwarp();
+    return acc;
+  };
+  auto finish = [&](float2 acc, int p) {
+    acc.x += __shfl_xor_sync(0xffffffffu, acc.x, 1);
+    acc.y += __shfl_xor_sync(0xffffffffu, acc.y, 1);
+    acc.x += __shfl_xor_sync(0xffffffffu, acc.x, 2);
+    acc.y += __shfl_xor_sync(0xffffffffu, acc.y, 2);
+    if (kz == 0 && c0 + c < g.nbatch)
+      *reinterpret_cast<float2*>(out + ((long long)(c0 + c) * g.npts + p) * 2) = acc;
+  };
+  auto one = [&](const R3& R) {
+    const unsigned view = R.view;
+    if (!((view >> 21) & 1)) return;  // no valid tap (warp-uniform)
+    finish((view >> 20) & 1 ? gather_box(R) : gather_rec(R), R.p);
+  };
+  for (int base = warp; base < npt; base += 8 * NW) {
+    if (base != warp) {
+      __syncwarp();  // the previous mini-batch has been read
+      build_records(base);
+    }
+    const int nb = min(8, (npt - base + NW - 1) / NW);
+    int i = 0;
+    for (; i + 1 < nb; i += 2) {
+      const R3& R0 = wrec[i];
+      const R3& R1 = wrec[i + 1];
+      if ((R0.view & R1.view) >> 20 & 1) {
+        const float2 a0 = gather_box(R0), a1 = gather_box(R1);
+        finish(a0, R0.p);
+        finish(a1, R1.p);
+      } else {
+        one(R0);
+        one(R1);
+      }
+    }
+    if (i < nb) one(wrec[i]);
+  }
+}
+
 // Sum the partial tiles of one split tile in slot order, compensated, and
 // write it out.
 __global__ void __launch_bounds__(NTHR) adj_reduce_kernel(Geo g, const int4* __restrict__ split,
@@ -1886,8 +2096,10 @@ int64_t max_tiles_per_dim(const Geo& g, int e) {
 
 // Geometries whose plan carries per-point tap records (the 3D 8-entry kernels)
 bool records_ok(const Geo& g) {
-  return g.ndim == 3 && g.norm == 1 && g.T[0] == 8 && g.T[1] == 8 && g.T[2] == 8 && g.NT[0] == 5 && g.NT[1] == 5 &&
-         g.NT[2] == 5;
+  if (g.norm != 1) return false;
+  if (g.ndim == 3)
+    return g.T[0] == 8 && g.T[1] == 8 && g.T[2] == 8 && g.NT[0] == 5 && g.NT[1] == 5 && g.NT[2] == 5;
+  return g.ndim == 2 && g.T[1] == 16 && g.T[2] == 16 && g.NT[1] == 5 && g.NT[2] == 5;
 }
 
 // The kernel, norm and beta a plan's records hold weights for
@@ -2241,6 +2453,40 @@ int launch_fwd_f3(const Geo& g, const tlgb_interp_plan_info* info, const char* P
   return TLGB_OK;
 }
 
+bool fast2(const Geo& g, int cg) {
+  return g.ndim == 2 && g.cplx && cg == 8 && g.norm == 1 && g.T[1] == 16 && g.T[2] == 16 && g.NT[1] == 5 &&
+         g.NT[2] == 5;
+}
+
+int launch_fwd_f2(const Geo& g, const tlgb_interp_plan_info* info, const char* P, const float* locs,
+                  const void* grid, void* out, cudaStream_t s) {
+  const int64_t ncg = cdiv(g.nbatch, 8);
+  const size_t sm = 20 * 20 * 8 * 8 + 64 * sizeof(R3) + 8 * sizeof(Rec<5>) + 8;
+  // [batch][Y][Z] complex64 as a 4D map {Z, Y, 1, batch}, box 20 x 20 x 1 x 8
+  CUtensorMap tmap;
+  memset(&tmap, 0, sizeof(tmap));
+  int use_tma = 0;
+  auto enc = tensor_map_encoder();
+  const uint64_t zb = (uint64_t)g.N[2] * 8;
+  if (enc && (zb % 16) == 0 && ((uintptr_t)grid % 16) == 0) {
+    const cuuint64_t dims[4] = {(cuuint64_t)g.N[2], (cuuint64_t)g.N[1], 1, (cuuint64_t)g.nbatch};
+    const cuuint64_t strides[3] = {zb, zb * g.N[1], zb * g.N[1]};
+    const cuuint32_t box[4] = {20, 20, 1, 8};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    const CUresult r = enc(&tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4, const_cast<void*>(grid), dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    use_tma = (r == CUDA_SUCCESS) ? 1 : 0;
+  }
+  TLGB_TRY(set_smem(fwd_f2_kernel, sm));
+  dim3 grd((unsigned)info->n_fwd_items, (unsigned)ncg);
+  fwd_f2_kernel<<<grd, 256, sm, s>>>(tmap, use_tma, g, (const int4*)(P + info->off_fwd_items),
+                                     (const int32_t*)(P + info->off_entries), (const PRec*)(P + info->off_records), locs,
+                                     (const float*)grid, (float*)out);
+  TLGB_CHECK_LAUNCH();
+  return TLGB_OK;
+}
+
 int launch_adj_f3(const Geo& g, const tlgb_interp_plan_info* info, const char* P, const float* locs,
                   const void* vals, void* grid, void* scratch, cudaStream_t s) {
   const int64_t ncg = cdiv(g.nbatch, 8);
@@ -2276,6 +2522,8 @@ int launch_fwd_t(const Geo& g, int cg, const tlgb_interp_plan_info* info, const 
                  const void* grid, void* out, cudaStream_t s) {
   if constexpr (N == 4 && NDIM == 3 && NTB == 5)
     if (fast3(g, cg) && info->off_records > 0) return launch_fwd_f3(g, info, P, locs, grid, out, s);
+  if constexpr (NDIM == 2 && NTB == 5)
+    if (fast2(g, cg) && info->off_records > 0) return launch_fwd_f2(g, info, P, locs, grid, out, s);
   return launch_fwd_t2<N, NDIM, NTB, false>(g, cg, info, P, locs, grid, out, s);
 }
 
