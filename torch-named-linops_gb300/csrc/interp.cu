@@ -1423,6 +1423,266 @@ __global__ void __launch_bounds__(256, 3) adj_f3_kernel(Geo g, const int4* __res
   }
 }
 
+// 2D gridding. The view of one dimension of a record from a 16-wide tile at o
+// (grid N): f | m << 4 | k0 << 7, as tile_view (f first local position, m
+// taps inside the tile, k0 the first of them in the record). fast is
+// cleared for 5-tap windows and, in circular mode on a grid below 32, for
+// windows that could meet the tile twice.
+__device__ __forceinline__ int tile_view16(int st, int c, int o, int N, bool circ, bool& fast) {
+  const int te = min(16, N - o);
+  int d = st - o;
+  if (circ && d < 0) d += N;
+  int f, k0, m;
+  if (d >= 0 && d < te) {
+    f = d;
+    k0 = 0;
+    m = min(c, te - d);
+  } else {
+    f = 0;
+    k0 = circ ? N - d : -d;
+    m = (d >= te && !circ) ? 0 : min(c - k0, te);
+  }
+  if (m < 0 || k0 < 0) m = 0, k0 = 0;
+  if (c > 4 || (circ && N < 32)) fast = false;
+  return f | (m << 4) | (min(k0, 7) << 7);
+}
+
+// (y view) | (z view) << 10 | fast << 27 | ok << 28
+__device__ __forceinline__ unsigned grid_view2(const Geo& g, const PRec& R, const int (&o)[3]) {
+  bool fast = true;
+  const bool circ = g.pad == TLGB_PAD_CIRCULAR;
+  const int c = R.cnt;
+  const bool ok = (c & 15) && ((c >> 4) & 15) && ((c >> 8) & 15);
+  const unsigned vy = tile_view16(R.st[1], (c >> 4) & 15, o[1], g.N[1], circ, fast);
+  const unsigned vz = tile_view16(R.st[2], (c >> 8) & 15, o[2], g.N[2], circ, fast);
+  return vy | (vz << 10) | ((fast ? 1u : 0u) << 27) | ((ok ? 1u : 0u) << 28);
+}
+
+// CTA = 8 warps owning one 16 x 16 x 8-entry output tile of a 2D grid, held
+// in registers: warp w owns rows 2w and 2w + 1, lane (row, z pair, entry
+// half) the cells (y, 2 zq) and (y, 2 zq + 1) for 4 of the 8 entries. Pairs
+// are staged in batches of kAB2, one thread per pair: its 8 point values,
+// its rows of tap weights over the tile (16 in y, 16 in z, zero where the
+// window has no tap), and per 2-row slab a bitmask of the pairs with taps
+// there. Each warp applies its slab's pairs in plan order, two per step, then
+// the pairs that need the generic record (5 taps, a window wrapping inside
+// the tile, a non-finite value), also in order.
+constexpr int kAB2 = 256;
+
+struct AdjStage2 {
+  float wrow[kAB2][32];  // tap weights at tile-local y (0-15) and z (16-31)
+  float pv[kAB2][16];    // point values, 8 entries complex
+  int pidx[kAB2];
+  unsigned fmask[8][kAB2 / 32];  // per slab: pairs on the row path with taps there
+  unsigned smask[kAB2 / 32];     // pairs on the generic path (all slabs)
+};
+
+constexpr size_t adj_f2_smem() { return sizeof(AdjStage2) + 8 * sizeof(Rec<5>); }
+
+__global__ void __launch_bounds__(256, 4) adj_f2_kernel(Geo g, const int4* __restrict__ items,
+                                                        const int32_t* __restrict__ entries,
+                                                        const PRec* __restrict__ precs,
+                                                        const float* __restrict__ locs, const float* __restrict__ vals,
+                                                        const float4* __restrict__ tv, float* __restrict__ gridv,
+                                                        float* __restrict__ partial) {
+  constexpr int CG = 8, VS = 16, TFL = 256 * 16, NW = 8, MW = kAB2 / 32;
+  extern __shared__ __align__(128) unsigned char smem[];
+  AdjStage2& S = *reinterpret_cast<AdjStage2*>(smem);
+  Rec<5>* slow = reinterpret_cast<Rec<5>*>(smem + sizeof(AdjStage2));  // [NW]
+  const int4 it = items[blockIdx.x];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int cg = blockIdx.y;
+  const int c0 = cg * CG;
+  const int ncoil = (int)min((long long)CG, g.nbatch - c0);
+  int o[3];
+  {
+    int t = it.x;
+    o[2] = (t % g.nt[2]) * 16;
+    t /= g.nt[2];
+    o[1] = (t % g.nt[1]) * 16;
+    o[0] = 0;
+  }
+  const int r = lane >> 4, zq = (lane >> 1) & 7, eh = lane & 1;
+  const int y = 2 * warp + r;
+  float2 acc[2][4];  // [z = 2 zq + i][entry 4 eh + k]
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int k = 0; k < 4; ++k) acc[i][k] = make_float2(0.f, 0.f);
+  for (int b = it.y; b < it.z; b += kAB2) {
+    const int nb = min(kAB2, it.z - b);
+    __syncthreads();  // the previous batch has been applied
+    {
+      unsigned view = 0;
+      bool finite = true;
+      if (tid < nb) {
+        const int p = entries[b + tid];
+        const PRec R = load_prec(precs, p);
+        float4 v[4];
+        if (tv) {
+          const float4* src = tv + ((long long)cg * g.npts + p) * 4;
+#pragma unroll
+          for (int q = 0; q < 4; ++q) v[q] = __ldg(src + q);
+        } else {
+          const float2* v2 = reinterpret_cast<const float2*>(vals);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const int c = 2 * q;
+            const float2 a = c < ncoil ? __ldg(v2 + (long long)(c0 + c) * g.npts + p) : make_float2(0.f, 0.f);
+            const float2 d = c + 1 < ncoil ? __ldg(v2 + (long long)(c0 + c + 1) * g.npts + p) : make_float2(0.f, 0.f);
+            v[q] = make_float4(a.x, a.y, d.x, d.y);
+          }
+        }
+        float4* pd = reinterpret_cast<float4*>(&S.pv[tid][0]);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          pd[q] = v[q];
+          finite = finite && isfinite(v[q].x) && isfinite(v[q].y) && isfinite(v[q].z) && isfinite(v[q].w);
+        }
+        view = grid_view2(g, R, o);
+        S.pidx[tid] = p;
+        if (((view >> 27) & 1) && finite) {
+#pragma unroll
+          for (int e = 0; e < 2; ++e) {
+            const unsigned u = (view >> (10 * e)) & 1023;
+            const int f = u & 15, m = (u >> 4) & 7, k0 = u >> 7;
+            const float4 w = R.w[1 + e];
+            float4* d = reinterpret_cast<float4*>(&S.wrow[tid][16 * e]);
+#pragma unroll
+            for (int l4 = 0; l4 < 4; ++l4) {
+              float rr[4];
+#pragma unroll
+              for (int i = 0; i < 4; ++i) {
+                const int k = 4 * l4 + i - f;
+                rr[i] = (k >= 0 && k < m) ? pick4(w, k0 + k) : 0.f;
+              }
+              d[l4] = make_float4(rr[0], rr[1], rr[2], rr[3]);
+            }
+          }
+        }
+      }
+      const bool ok = (view >> 28) & 1, fast = ((view >> 27) & 1) && finite;
+      const int fy = view & 15, my = (view >> 4) & 7;
+#pragma unroll
+      for (int w = 0; w < NW; ++w) {
+        const unsigned bal = __ballot_sync(0xffffffffu, ok && fast && fy <= 2 * w + 1 && fy + my > 2 * w);
+        if (lane == 0) S.fmask[w][warp] = bal;
+      }
+      const unsigned bs = __ballot_sync(0xffffffffu, ok && !fast);
+      if (lane == 0) S.smask[warp] = bs;
+    }
+    __syncthreads();
+    struct Visit {
+      float w0, w1;   // weights of the lane's two cells
+      float4 v0, v1;  // the lane's 4 entries, complex
+    };
+    auto fetch = [&](int j) {
+      const float* wr = S.wrow[j];
+      const float wy = wr[y];
+      const float2 wz = *reinterpret_cast<const float2*>(wr + 16 + 2 * zq);
+      Visit d;
+      d.w0 = wy * wz.x;
+      d.w1 = wy * wz.y;
+      d.v0 = *reinterpret_cast<const float4*>(&S.pv[j][8 * eh]);
+      d.v1 = *reinterpret_cast<const float4*>(&S.pv[j][8 * eh + 4]);
+      return d;
+    };
+    auto apply = [&](const Visit& d) {
+      const float2 v[4] = {make_float2(d.v0.x, d.v0.y), make_float2(d.v0.z, d.v0.w), make_float2(d.v1.x, d.v1.y),
+                           make_float2(d.v1.z, d.v1.w)};
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        fma2_bcast(acc[0][k], d.w0, v[k]);
+        fma2_bcast(acc[1][k], d.w1, v[k]);
+      }
+    };
+#pragma unroll 1
+    for (int mw = 0; mw < MW; ++mw) {
+      unsigned bits = S.fmask[warp][mw];
+      while (bits) {
+        const int j0 = mw * 32 + __ffs(bits) - 1;
+        bits &= bits - 1;
+        const Visit d0 = fetch(j0);
+        if (bits) {
+          const int j1 = mw * 32 + __ffs(bits) - 1;
+          bits &= bits - 1;
+          const Visit d1 = fetch(j1);
+          apply(d0);
+          apply(d1);
+        } else {
+          apply(d0);
+        }
+      }
+    }
+#pragma unroll 1
+    for (int mw = 0; mw < MW; ++mw) {
+      unsigned bits = S.smask[mw];
+      while (bits) {
+        const int j = mw * 32 + __ffs(bits) - 1;
+        bits &= bits - 1;
+        __syncwarp();  // the previous record has been read
+        if (lane == 0) {
+          float x3[3] = {0.f, 0.f, 0.f};
+          for (int e = 1; e < 3; ++e) x3[e] = load_coord(g, locs, S.pidx[j], e);
+          lane_rec<5>(g, x3, o, false, slow[warp]);
+        }
+        __syncwarp();
+        const Rec<5>& Q = slow[warp];
+        const float4 v0 = *reinterpret_cast<const float4*>(&S.pv[j][8 * eh]);
+        const float4 v1 = *reinterpret_cast<const float4*>(&S.pv[j][8 * eh + 4]);
+        const float2 v[4] = {make_float2(v0.x, v0.y), make_float2(v0.z, v0.w), make_float2(v1.x, v1.y),
+                             make_float2(v1.z, v1.w)};
+        if (Q.m[0] > 0)
+          for (int kyy = 0; kyy < Q.m[1]; ++kyy) {
+            if (Q.lc[1][kyy] != y) continue;
+            for (int kz = 0; kz < Q.m[2]; ++kz) {
+              const int z = Q.lc[2][kz];
+              const float w = Q.wv[1][kyy] * Q.wv[2][kz];
+#pragma unroll
+              for (int i = 0; i < 2; ++i) {
+                if (z != 2 * zq + i) continue;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) fma2_bcast(acc[i][k], w, v[k]);
+              }
+            }
+          }
+      }
+    }
+  }
+  // write-out from registers: a split tile's part to its partial slot
+  // ([y][z][entry], 16 floats per cell); a whole tile to the grid, 16
+  // contiguous bytes (two z) of an entry's row per lane
+  if (it.w >= 0) {
+    float* dst = partial + ((long long)it.w * gridDim.y + cg) * TFL;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      float4* d = reinterpret_cast<float4*>(dst + (y * 16 + 2 * zq + i) * VS + 8 * eh);
+      d[0] = make_float4(acc[i][0].x, acc[i][0].y, acc[i][1].x, acc[i][1].y);
+      d[1] = make_float4(acc[i][2].x, acc[i][2].y, acc[i][3].x, acc[i][3].y);
+    }
+    return;
+  }
+  const int gy = o[1] + y;
+  if (gy >= g.N[1]) return;
+  const long long gvol = (long long)g.N[1] * g.N[2];
+  // 16-byte stores need an even Z extent (row starts at even elements) and an aligned base
+  const bool vec = o[2] + 16 <= g.N[2] && (g.N[2] & 1) == 0 && (reinterpret_cast<uintptr_t>(gridv) & 15) == 0;
+  const int z = 2 * zq;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int c = 4 * eh + k;
+    if (c >= ncoil) continue;
+    float* row = gridv + ((long long)(c0 + c) * gvol + (long long)gy * g.N[2] + o[2]) * 2;
+    const float2 a = acc[0][k], bb = acc[1][k];
+    if (vec) {
+      *reinterpret_cast<float4*>(row + 2 * z) = make_float4(a.x, a.y, bb.x, bb.y);
+    } else {
+      if (o[2] + z < g.N[2]) *reinterpret_cast<float2*>(row + 2 * z) = a;
+      if (o[2] + z + 1 < g.N[2]) *reinterpret_cast<float2*>(row + 2 * z + 2) = bb;
+    }
+  }
+}
+
 // Gather: CTA = 8 warps sharing one 12^3 x 8-entry region ([entry][x][y][z],
 // loaded by one TMA bulk tensor copy when the region needs no wrap), two CTAs
 // per SM. Each warp takes every 8th point of the item, building the records
@@ -2356,6 +2616,7 @@ extern "C" int tlgb_interp_plan_build(const tlgb_interp_desc* d, const float* lo
 namespace tlgb {
 namespace {
 bool fast3(const Geo& g, int cg);
+bool fast2(const Geo& g, int cg);
 
 // Gridding scratch: the partial tiles of split tiles, then (3D 8-entry path
 // only) the point values transposed to point-major order.
@@ -2363,7 +2624,7 @@ void adj_scratch_parts(const Geo& g, const tlgb_interp_plan_info* info, size_t& 
   const int cg = adj_cg(g);
   const int64_t ncg = cdiv(std::max<long long>(g.nbatch, 1), cg);
   partial_bytes = align_up((size_t)info->n_partials * ncg * tile_floats(g, cg) * sizeof(float), 256);
-  tv_bytes = (fast3(g, cg) && info->off_records > 0) ? (size_t)ncg * g.npts * 8 * 8 : 0;
+  tv_bytes = ((fast3(g, cg) || fast2(g, cg)) && info->off_records > 0) ? (size_t)ncg * g.npts * 8 * 8 : 0;
 }
 }  // namespace
 }  // namespace tlgb
@@ -2517,6 +2778,36 @@ int launch_adj_f3(const Geo& g, const tlgb_interp_plan_info* info, const char* P
   return TLGB_OK;
 }
 
+int launch_adj_f2(const Geo& g, const tlgb_interp_plan_info* info, const char* P, const float* locs,
+                  const void* vals, void* grid, void* scratch, cudaStream_t s) {
+  const int64_t ncg = cdiv(g.nbatch, 8);
+  const size_t sm = adj_f2_smem();
+  TLGB_TRY(set_smem(adj_f2_kernel, sm));
+  if (((uintptr_t)(P + info->off_records) & 15) || ((uintptr_t)scratch & 15))
+    TLGB_FAIL(TLGB_ERR_INVALID, "interp adjoint: plan and scratch must be 16-byte aligned");
+  const float4* tv = nullptr;
+  if (g.tv_off >= 0 && g.npts > 0) {
+    float2* t = reinterpret_cast<float2*>(static_cast<char*>(scratch) + g.tv_off);
+    dim3 gt((unsigned)cdiv(g.npts, 32), (unsigned)ncg);
+    transpose_vals_kernel<<<gt, 256, 0, s>>>((const float2*)vals, g.npts, g.nbatch, t);
+    TLGB_CHECK_LAUNCH();
+    tv = reinterpret_cast<const float4*>(t);
+  }
+  dim3 grd((unsigned)info->n_adj_items, (unsigned)ncg);
+  adj_f2_kernel<<<grd, 256, sm, s>>>(g, (const int4*)(P + info->off_adj_items), (const int32_t*)(P + info->off_entries),
+                                    (const PRec*)(P + info->off_records), locs, (const float*)vals, tv, (float*)grid,
+                                    (float*)scratch);
+  TLGB_CHECK_LAUNCH();
+  if (info->n_split_tiles > 0) {
+    // parts in the generic [y][z][entry] layout of a 16 x 16 x 8-entry tile
+    dim3 g2((unsigned)info->n_split_tiles, (unsigned)ncg);
+    adj_reduce_kernel<<<g2, NTHR, 0, s>>>(g, (const int4*)(P + info->off_split), (const float*)scratch, (float*)grid,
+                                          8, (int)ncg);
+    TLGB_CHECK_LAUNCH();
+  }
+  return TLGB_OK;
+}
+
 template <int N, int NDIM, int NTB>
 int launch_fwd_t(const Geo& g, int cg, const tlgb_interp_plan_info* info, const char* P, const float* locs,
                  const void* grid, void* out, cudaStream_t s) {
@@ -2532,6 +2823,8 @@ int launch_adj_t(const Geo& g, int cg, const tlgb_interp_plan_info* info, const 
                  const void* vals, void* grid, void* scratch, cudaStream_t s) {
   if constexpr (N == 4 && NDIM == 3 && NTB == 5)
     if (fast3(g, cg) && info->off_records > 0) return launch_adj_f3(g, info, P, locs, vals, grid, scratch, s);
+  if constexpr (NDIM == 2 && NTB == 5)
+    if (fast2(g, cg) && info->off_records > 0) return launch_adj_f2(g, info, P, locs, vals, grid, scratch, s);
   return launch_adj_t2<N, NDIM, NTB, false>(g, cg, info, P, locs, vals, grid, scratch, s);
 }
 
