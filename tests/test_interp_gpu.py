@@ -105,7 +105,8 @@ def test_dense_centre_against_oracle(ndim, n, npts, nb, pad):
 @pytest.mark.parametrize("shape", [(40, 36, 48), (40, 36, 45)])
 @pytest.mark.parametrize("nb", [8, 11])
 @pytest.mark.parametrize("pad", ["circular", "zero"])
-def test_eight_entry_3d_paths_against_oracle(shape, nb, pad):
+@pytest.mark.parametrize("kernel", ["kaiser_bessel", "spline"])
+def test_eight_entry_3d_paths_against_oracle(shape, nb, pad, kernel):
     """3D, 8 complex entries per group: the TMA-staged gather (even Z) and its
     plain-load fallback (odd Z, wrapping edge regions), a ragged last group,
     dense split tiles, points across every edge and exact-integer points."""
@@ -121,7 +122,7 @@ def test_eight_entry_3d_paths_against_oracle(shape, nb, pad):
     img = torch.complex(torch.randn(nb, *shape, generator=gen), torch.randn(nb, *shape, generator=gen))
     pts = torch.complex(torch.randn(nb, npts, generator=gen), torch.randn(nb, npts, generator=gen))
     beta = OI.nufft_beta(4.0, 1.25)
-    kw = dict(kernel="kaiser_bessel", pad_mode=pad)
+    kw = dict(kernel=kernel, pad_mode=pad)
     _ext.device_status(clear=True)
     fwd = T.ungrid(img.to(DEV), locs.to(DEV), 4.0, kernel_params=dict(beta=beta), **kw).cpu()
     adj = T.grid(pts.to(DEV), locs.to(DEV), shape, 4.0, kernel_params=dict(beta=beta), **kw).cpu()
@@ -137,7 +138,8 @@ def test_eight_entry_3d_paths_against_oracle(shape, nb, pad):
 @pytest.mark.parametrize("shape", [(160, 144), (90, 61)])
 @pytest.mark.parametrize("nb", [8, 11])
 @pytest.mark.parametrize("pad", ["circular", "zero"])
-def test_eight_entry_2d_paths_against_oracle(shape, nb, pad):
+@pytest.mark.parametrize("kernel", ["kaiser_bessel", "spline"])
+def test_eight_entry_2d_paths_against_oracle(shape, nb, pad, kernel):
     """2D, 8 complex entries per group: the TMA-staged gather (even Z) and its
     plain-load fallback (odd Z, wrapping edge regions), a ragged last group,
     dense tiles, points across every edge and exact-integer points."""
@@ -153,7 +155,7 @@ def test_eight_entry_2d_paths_against_oracle(shape, nb, pad):
     img = torch.complex(torch.randn(nb, *shape, generator=gen), torch.randn(nb, *shape, generator=gen))
     pts = torch.complex(torch.randn(nb, npts, generator=gen), torch.randn(nb, npts, generator=gen))
     beta = OI.nufft_beta(4.0, 1.25)
-    kw = dict(kernel="kaiser_bessel", pad_mode=pad)
+    kw = dict(kernel=kernel, pad_mode=pad)
     _ext.device_status(clear=True)
     fwd = T.ungrid(img.to(DEV), locs.to(DEV), 4.0, kernel_params=dict(beta=beta), **kw).cpu()
     adj = T.grid(pts.to(DEV), locs.to(DEV), shape, 4.0, kernel_params=dict(beta=beta), **kw).cpu()

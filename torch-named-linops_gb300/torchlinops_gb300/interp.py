@@ -113,7 +113,7 @@ class InterpolatePlan:
         self.npts = prod(locs.shape[:-1])
         locs_c = locs.detach().reshape(-1, ndim).to(torch.float32).contiguous()
         self.beta, self.norm = float(beta), int(norm)
-        # 3D plans also hold each point's tap weights, so they are built for one (kernel, norm, beta)
+        # 2D and 3D plans also hold each point's tap weights, so they are built for one (kernel, norm, beta)
         d = _desc(ndim, self.grid_size, self.width, kernel, self.norm, pad_mode, self.beta, False, 1, self.npts)
         L = _ext.lib()
         pb, tb = ctypes.c_size_t(0), ctypes.c_size_t(0)
