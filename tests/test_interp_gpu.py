@@ -263,6 +263,38 @@ def test_trajectory_gradient(ndim, kernel, norm):
     assert rel_l2(L2.grad.cpu(), ref2) < 2e-5
 
 
+@pytest.mark.parametrize("nb", [8, 11])
+@pytest.mark.parametrize("pad", ["circular", "zero"])
+@pytest.mark.parametrize("kernel", ["kaiser_bessel", "spline"])
+def test_trajectory_gradient_2d_eight_entry_path(nb, pad, kernel):
+    """d/dlocs of both operators on the 2D 8-entry path (gradient records,
+    TMA-staged regions, one partial per coil group added in order), against
+    the FP64 autograd restatement. Points stay clear of tap-window edges,
+    where the kernels' derivatives are singular (Kaiser-Bessel) or undefined
+    (spline); in z they reach the upper edge, where circular windows wrap."""
+    gen = torch.Generator().manual_seed(nb + len(pad) + len(kernel))
+    size = (48, 40)
+    locs = _safe_points(4000, 40, 4.0, gen, 2)
+    npts = locs.shape[0]
+    img = torch.complex(torch.randn(nb, *size, generator=gen), torch.randn(nb, *size, generator=gen))
+    a = torch.complex(torch.randn(nb, npts, generator=gen), torch.randn(nb, npts, generator=gen))
+    beta = OI.nufft_beta(4.0, 1.25)
+    kw = dict(kernel=kernel, pad_mode=pad)
+    L = locs.to(DEV).requires_grad_(True)
+    out = T.interpolate(img.to(DEV), L, 4.0, kernel_params=dict(beta=beta), **kw)
+    (a.to(DEV).conj() * out).real.sum().backward()
+    ref = OI.grad_locs_interp(img, a, locs, 4.0, kernel, 1, pad, beta)
+    assert rel_l2(L.grad.cpu(), ref) < 1e-4
+    # the gridding operator: grid := cotangent, a := point values
+    vals = a
+    b = torch.complex(torch.randn(nb, *size, generator=gen), torch.randn(nb, *size, generator=gen))
+    L2 = locs.to(DEV).requires_grad_(True)
+    g = T.interpolate_adjoint(vals.to(DEV), L2, size, 4.0, kernel_params=dict(beta=beta), **kw)
+    (b.to(DEV).conj() * g).real.sum().backward()
+    ref2 = OI.grad_locs_adjoint(vals, b, locs, size, 4.0, kernel, 1, pad, beta)
+    assert rel_l2(L2.grad.cpu(), ref2) < 1e-4
+
+
 def test_trajectory_gradient_finite_differences():
     """d/dx by central differences of the FP64 oracle (h = 1e-4 grid units)."""
     gen = torch.Generator().manual_seed(21)

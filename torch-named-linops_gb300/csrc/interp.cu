@@ -36,6 +36,7 @@
 #include <mutex>
 #include <numeric>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "common.cuh"
@@ -2273,6 +2274,236 @@ __global__ void __launch_bounds__(256) grad_reduce_kernel(const float* __restric
   grad[i] = s;
 }
 
+// ------------------------------------------------ 2D trajectory gradient
+//
+// Per-point gradient records for 2D geometries (built per call, since the
+// trajectory may change between calls): the weights and derivative weights
+// of the first 4 valid taps in y and z (zero beyond), the first valid tap's
+// position (wrapped in circular mode) and the tap counts (cy | cz << 4; a
+// zero count marks a point without taps). The taps follow tap_eval; weights
+// and derivatives are kern_value and kern_deriv / r, as in warp_point_taps.
+struct __align__(16) GRec2 {
+  float4 w[2], dw[2];
+  int st[2];
+  int cnt;
+  int pad;
+};
+static_assert(sizeof(GRec2) == 80, "80-byte gradient records");
+
+__global__ void __launch_bounds__(256) grad_records2_kernel(Geo g, const float* __restrict__ locs,
+                                                            GRec2* __restrict__ out) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= g.npts) return;
+  GRec2 R;
+  int cnt = 0;
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const int e = 1 + i;
+    float w[4] = {0.f, 0.f, 0.f, 0.f}, dw[4] = {0.f, 0.f, 0.f, 0.f};
+    int c = 0, st = 0;
+    const float x = load_coord(g, locs, p, e);
+    if (coord_ok(x)) {
+      const int lower = lower_of(g, e, x);
+      int s = -1;
+#pragma unroll
+      for (int k = 0; k < 5; ++k) {
+        const Tap t = tap_eval(g, e, x, lower, k);
+        if (!t.valid) continue;
+        if (s < 0) s = k;
+        if (c < 4) {
+          w[c] = kern_value(g.kernel, fabsf(t.d), g.beta);
+          dw[c] = kern_deriv(g.kernel, t.d, g.beta) / g.r[e];
+        }
+        ++c;
+      }
+      if (c > 0) {
+        st = lower + s;
+        if (g.pad == TLGB_PAD_CIRCULAR) st = wrapi(st, g.N[e]);
+      }
+    }
+    R.w[i] = make_float4(w[0], w[1], w[2], w[3]);
+    R.dw[i] = make_float4(dw[0], dw[1], dw[2], dw[3]);
+    R.st[i] = st;
+    cnt |= c << (4 * i);
+  }
+  R.cnt = cnt;
+  R.pad = 0;
+  out[p] = R;
+}
+
+// d/d(y, z) of sum_b Re(conj(a[b, p]) ungrid(grid)[b, p]) for one coil group
+// (blockIdx.y) of a 2D geometry with 8 complex entries per group: CTA = 8
+// warps sharing the 20 x 20 x 8-entry region of one 16 x 16 tile, as
+// fwd_f2_kernel. Lanes = (entry, z-tap): a lane sums its entry's 4 y-taps
+// for both derivatives, then all 32 lanes add up. With several coil groups
+// the group's sums go to its partial slot (added in order afterwards).
+__global__ void __launch_bounds__(256, 3) grad_f2_kernel(const __grid_constant__ CUtensorMap tmap, int use_tma, Geo g,
+                                                         const int4* __restrict__ items,
+                                                         const int32_t* __restrict__ entries,
+                                                         const GRec2* __restrict__ grecs,
+                                                         const float* __restrict__ locs,
+                                                         const float* __restrict__ gridv, const float2* __restrict__ a,
+                                                         float* __restrict__ grad, float* __restrict__ partial) {
+  constexpr int CG = 8, S = 20, VOL = S * S, NW = 8;
+  constexpr uint32_t RBYTES = VOL * CG * 8;
+  extern __shared__ __align__(128) unsigned char smem[];
+  float2* reg = reinterpret_cast<float2*>(smem);                  // [8][20][20]
+  GRec2* rec = reinterpret_cast<GRec2*>(smem + RBYTES);           // [8 warps][8]
+  PTaps<true>* slow = reinterpret_cast<PTaps<true>*>(rec + 64);   // [NW]
+  uint64_t* bar = reinterpret_cast<uint64_t*>(slow + NW);
+  const int4 it = items[blockIdx.x];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int cg = blockIdx.y;
+  const int c0 = cg * CG;
+  float* dst = gridDim.y == 1 ? grad : partial + (long long)cg * g.npts * 2;
+  int o[3];
+  {
+    int t = it.x;
+    o[2] = (t % g.nt[2]) * g.T[2];
+    t /= g.nt[2];
+    o[1] = (t % g.nt[1]) * g.T[1];
+    o[0] = 0;
+  }
+  const bool wraps = g.pad == TLGB_PAD_CIRCULAR && (o[1] + S > g.N[1] || o[2] + S > g.N[2]);
+  const bool tma = use_tma && !wraps;
+  if (tma) {
+    if (tid == 0) {
+      mbar_init(bar, 1);
+      fence_mbar_init();
+    }
+    __syncthreads();
+    if (tid == 0) {
+      mbar_arrive_expect_tx(bar, RBYTES);
+      tma_load_4d(reg, &tmap, bar, o[2], o[1], 0, c0);
+    }
+  } else {
+    const int ncoil = (int)min((long long)CG, g.nbatch - c0);
+    const long long gvol = (long long)g.N[1] * g.N[2];
+    for (int idx = tid; idx < CG * VOL; idx += NW * 32) {
+      const int z = idx % S;
+      const int r = idx / S;
+      const int y = r % S, c = r / S;
+      int gy = o[1] + y, gz = o[2] + z;
+      bool in = c < ncoil;
+      if (g.pad == TLGB_PAD_CIRCULAR) {
+        gy = wrapi(gy, g.N[1]);
+        gz = wrapi(gz, g.N[2]);
+      } else {
+        in = in && gy < g.N[1] && gz < g.N[2];
+      }
+      reg[idx] = in ? __ldg(reinterpret_cast<const float2*>(gridv) + (long long)(c0 + c) * gvol +
+                           (long long)gy * g.N[2] + gz)
+                    : make_float2(0.f, 0.f);
+    }
+  }
+  const int c = lane >> 2, kz = lane & 3;
+  int kyo[4], rowoff[4];
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    kyo[t] = (t + c) & 3;
+    rowoff[t] = kyo[t] * S;
+  }
+  GRec2* wrec = rec + warp * 8;
+  const int npt = it.z - it.y;
+  // records of the warp's next 8 points: lanes 0-7 copy them into the
+  // warp's slots; pad = region base | fast << 20 | ok << 21, cnt unchanged
+  auto build_records = [&](int base) {
+    const int j = base + 8 * lane;
+    if (lane < 8 && j < npt) {
+      const int p = entries[it.y + j];
+      GRec2 R = grecs[p];
+      const int cy = R.cnt & 15, cz = (R.cnt >> 4) & 15;
+      const bool ok = cy && cz;
+      int f[2];
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        int d = R.st[i] - o[1 + i];
+        if (g.pad == TLGB_PAD_CIRCULAR && d < 0) d += g.N[1 + i];
+        f[i] = d;
+      }
+      const bool fast = ok && cy <= 4 && cz <= 4 && f[0] >= 0 && f[0] < 16 && f[1] >= 0 && f[1] < 16;
+      R.pad = (fast ? (f[0] * S + f[1]) : 0) | ((fast ? 1 : 0) << 20) | ((ok ? 1 : 0) << 21);
+      R.st[0] = p;  // the point index replaces the start (no longer needed)
+      wrec[lane] = R;
+    }
+    __syncwarp();
+  };
+  build_records(warp);  // while the region copy is in flight
+  {
+    bool ok = true;
+    if (tma && tid == 0) ok = mbar_wait_bounded(bar, 0, 1u << 22);
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) atomicExch(&g_tlgb_status, 1);
+      return;
+    }
+  }
+  auto finish = [&](float ry, float rz, int p) {
+#pragma unroll
+    for (int m = 1; m < 32; m <<= 1) {
+      ry += __shfl_xor_sync(0xffffffffu, ry, m);
+      rz += __shfl_xor_sync(0xffffffffu, rz, m);
+    }
+    if (lane == 0) *reinterpret_cast<float2*>(dst + (long long)p * 2) = make_float2(ry, rz);
+  };
+  for (int base = warp; base < npt; base += 8 * NW) {
+    if (base != warp) {
+      __syncwarp();  // the previous mini-batch has been read
+      build_records(base);
+    }
+    const int nb = min(8, (npt - base + NW - 1) / NW);
+    for (int i = 0; i < nb; ++i) {
+      const GRec2& R = wrec[i];
+      const int p = R.st[0];
+      const int info = R.pad;
+      if (!((info >> 21) & 1)) {
+        if (lane == 0) *reinterpret_cast<float2*>(dst + (long long)p * 2) = make_float2(0.f, 0.f);
+        continue;
+      }
+      const float2 av = c0 + c < g.nbatch ? __ldg(a + (long long)(c0 + c) * g.npts + p) : make_float2(0.f, 0.f);
+      float2 gy = make_float2(0.f, 0.f), gz = make_float2(0.f, 0.f);
+      if ((info >> 20) & 1) {
+        const float wz = (&R.w[1].x)[kz], dwz = (&R.dw[1].x)[kz];
+        const float* wy = &R.w[0].x;
+        const float* dwy = &R.dw[0].x;
+        const float2* ab = reg + c * VOL + (info & 1023) + kz;
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          const float2 v = ab[rowoff[t]];
+          const float a1 = dwy[kyo[t]] * wz, a2 = wy[kyo[t]] * dwz;
+          gy.x = fmaf(a1, v.x, gy.x);
+          gy.y = fmaf(a1, v.y, gy.y);
+          gz.x = fmaf(a2, v.x, gz.x);
+          gz.y = fmaf(a2, v.y, gz.y);
+        }
+      } else {
+        // 5-tap windows: the warp evaluates the taps, as interp_grad_kernel
+        PTaps<true>& pt = slow[warp];
+        if (warp_point_taps<1, true>(g, locs, p, pt, lane)) {
+          const int l1 = pt.start[1] - o[1], l2 = pt.start[2] - o[2];
+          for (int kb = 0; kb < pt.n[1]; ++kb) {
+            int yy = l1 + kb;
+            if (g.pad == TLGB_PAD_CIRCULAR && yy < 0) yy += g.N[1];
+            for (int kc = kz; kc < pt.n[2]; kc += 4) {
+              int zz = l2 + kc;
+              if (g.pad == TLGB_PAD_CIRCULAR && zz < 0) zz += g.N[2];
+              if (yy < 0 || yy >= S || zz < 0 || zz >= S) continue;
+              const float2 v = reg[c * VOL + yy * S + zz];
+              const float a1 = pt.dw[1][kb] * pt.w[2][kc], a2 = pt.w[1][kb] * pt.dw[2][kc];
+              gy.x = fmaf(a1, v.x, gy.x);
+              gy.y = fmaf(a1, v.y, gy.y);
+              gz.x = fmaf(a2, v.x, gz.x);
+              gz.y = fmaf(a2, v.y, gz.y);
+            }
+          }
+        }
+        __syncwarp();
+      }
+      // Re(conj(a) g)
+      finish(av.x * gy.x + av.y * gy.y, av.x * gz.x + av.y * gz.y, p);
+    }
+  }
+}
+
 // ------------------------------------------------------------- host helpers
 
 struct PlanLayout {
@@ -2474,6 +2705,20 @@ int grad_splits(const Geo& g, const tlgb_interp_plan_info* info) {
 
 size_t grad_scratch_bytes(const Geo& g, int nsplit) {
   return nsplit > 1 ? (size_t)nsplit * g.npts * g.ndim * sizeof(float) : 0;
+}
+
+bool fast2(const Geo& g, int cg);
+
+// The 2D 8-entry gradient (grad_f2_kernel): complex values, norm 1, 8
+// entries per coil group. Its scratch holds the per-point gradient records
+// and, with more than one coil group, one partial slot per group.
+bool grad_fast2(const Geo& g) { return g.cplx && g.norm == 1 && g.nbatch >= 8 && fast2(g, 8); }
+
+size_t grad2_records_bytes(const Geo& g) { return align_up((size_t)g.npts * sizeof(GRec2), 256); }
+
+size_t grad2_scratch_bytes(const Geo& g) {
+  const long long ncg = cdiv(g.nbatch, 8);
+  return grad2_records_bytes(g) + (ncg > 1 ? (size_t)ncg * g.npts * 2 * sizeof(float) : 0);
 }
 
 int check_plan(const Geo& g, const tlgb_interp_plan_info* info, const void* plan) {
@@ -2719,26 +2964,29 @@ bool fast2(const Geo& g, int cg) {
          g.NT[2] == 5;
 }
 
+// [batch][Y][Z] complex64 as a 4D map {Z, Y, 1, batch}, box 20 x 20 x 1 x 8
+// (the staged region of a 16 x 16 tile); 0 when TMA cannot be used
+int region_map2(const Geo& g, const void* grid, CUtensorMap& tmap) {
+  memset(&tmap, 0, sizeof(tmap));
+  auto enc = tensor_map_encoder();
+  const uint64_t zb = (uint64_t)g.N[2] * 8;
+  if (!enc || (zb % 16) != 0 || ((uintptr_t)grid % 16) != 0) return 0;
+  const cuuint64_t dims[4] = {(cuuint64_t)g.N[2], (cuuint64_t)g.N[1], 1, (cuuint64_t)g.nbatch};
+  const cuuint64_t strides[3] = {zb, zb * g.N[1], zb * g.N[1]};
+  const cuuint32_t box[4] = {20, 20, 1, 8};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  const CUresult r = enc(&tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4, const_cast<void*>(grid), dims, strides, box, estr,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? 1 : 0;
+}
+
 int launch_fwd_f2(const Geo& g, const tlgb_interp_plan_info* info, const char* P, const float* locs,
                   const void* grid, void* out, cudaStream_t s) {
   const int64_t ncg = cdiv(g.nbatch, 8);
   const size_t sm = 20 * 20 * 8 * 8 + 64 * sizeof(R3) + 8 * sizeof(Rec<5>) + 8;
-  // [batch][Y][Z] complex64 as a 4D map {Z, Y, 1, batch}, box 20 x 20 x 1 x 8
   CUtensorMap tmap;
-  memset(&tmap, 0, sizeof(tmap));
-  int use_tma = 0;
-  auto enc = tensor_map_encoder();
-  const uint64_t zb = (uint64_t)g.N[2] * 8;
-  if (enc && (zb % 16) == 0 && ((uintptr_t)grid % 16) == 0) {
-    const cuuint64_t dims[4] = {(cuuint64_t)g.N[2], (cuuint64_t)g.N[1], 1, (cuuint64_t)g.nbatch};
-    const cuuint64_t strides[3] = {zb, zb * g.N[1], zb * g.N[1]};
-    const cuuint32_t box[4] = {20, 20, 1, 8};
-    const cuuint32_t estr[4] = {1, 1, 1, 1};
-    const CUresult r = enc(&tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4, const_cast<void*>(grid), dims, strides, box, estr,
-                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                           CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    use_tma = (r == CUDA_SUCCESS) ? 1 : 0;
-  }
+  const int use_tma = region_map2(g, grid, tmap);
   TLGB_TRY(set_smem(fwd_f2_kernel, sm));
   dim3 grd((unsigned)info->n_fwd_items, (unsigned)ncg);
   fwd_f2_kernel<<<grd, 256, sm, s>>>(tmap, use_tma, g, (const int4*)(P + info->off_fwd_items),
@@ -2869,9 +3117,39 @@ int launch_adj(const Geo& g, const tlgb_interp_plan_info* info, const char* P, c
   return small ? dispatch_adj_n<1, 5>(g, cg, info, P, locs, vals, grid, scratch, s) : dispatch_adj_n<1, 16>(g, cg, info, P, locs, vals, grid, scratch, s);
 }
 
+int launch_grad_f2(const Geo& g, const tlgb_interp_plan_info* info, const char* P, const float* locs,
+                   const void* grid, const void* a, float* grad, void* scratch, cudaStream_t s) {
+  const long long ncg = cdiv(g.nbatch, 8);
+  GRec2* recs = static_cast<GRec2*>(scratch);
+  float* partial = reinterpret_cast<float*>(static_cast<char*>(scratch) + grad2_records_bytes(g));
+  grad_records2_kernel<<<(unsigned)cdiv(g.npts, 256), 256, 0, s>>>(g, locs, recs);
+  TLGB_CHECK_LAUNCH();
+  const long long n = (long long)g.npts * 2;
+  if (ncg > 1 && info->n_home < g.npts)  // points without taps get no partial writes
+    TLGB_CUDA(cudaMemsetAsync(partial, 0, (size_t)ncg * n * sizeof(float), s));
+  CUtensorMap tmap;
+  const int use_tma = region_map2(g, grid, tmap);
+  const size_t sm = 20 * 20 * 8 * 8 + 64 * sizeof(GRec2) + 8 * sizeof(PTaps<true>) + 8;
+  TLGB_TRY(set_smem(grad_f2_kernel, sm));
+  dim3 grd((unsigned)info->n_fwd_items, (unsigned)ncg);
+  grad_f2_kernel<<<grd, 256, sm, s>>>(tmap, use_tma, g, (const int4*)(P + info->off_fwd_items),
+                                      (const int32_t*)(P + info->off_entries), recs, locs, (const float*)grid,
+                                      (const float2*)a, grad, partial);
+  TLGB_CHECK_LAUNCH();
+  if (ncg > 1) {
+    grad_reduce_kernel<<<(unsigned)cdiv(n, 256), 256, 0, s>>>(partial, (int)ncg, n, grad);
+    TLGB_CHECK_LAUNCH();
+  }
+  return TLGB_OK;
+}
+
 template <typename V, int NORM>
 int launch_grad(const Geo& g, const tlgb_interp_plan_info* info, const char* P, const float* locs, const void* grid,
                 const void* a, float* grad, void* scratch, size_t scratch_bytes, cudaStream_t s) {
+  if constexpr (std::is_same<V, float2>::value && NORM == 1)
+    if (grad_fast2(g) && info->off_records > 0 && scratch && scratch_bytes >= grad2_scratch_bytes(g) &&
+        ((uintptr_t)scratch & 15) == 0)
+      return launch_grad_f2(g, info, P, locs, grid, a, grad, scratch, s);
   const int cg = grad_cg(g, sizeof(PTaps<true>));
   const size_t sm = grad_smem(g, cg, sizeof(PTaps<true>)) + kFwdChunk * 3 * sizeof(float);
   auto* k = interp_grad_kernel<V, NORM>;
@@ -2934,7 +3212,7 @@ extern "C" int tlgb_interp_grad_scratch_size(const tlgb_interp_desc* d, const tl
   Geo g;
   TLGB_TRY(make_geo(d, g));
   if (!info || !bytes) TLGB_FAIL(TLGB_ERR_INVALID, "null pointer");
-  *bytes = grad_scratch_bytes(g, grad_splits(g, info));
+  *bytes = grad_fast2(g) && info->off_records > 0 ? grad2_scratch_bytes(g) : grad_scratch_bytes(g, grad_splits(g, info));
   return TLGB_OK;
 }
 
