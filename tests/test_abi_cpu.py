@@ -88,3 +88,26 @@ def test_product_path_has_no_cpu_fallback():
         T.unfold(x, (2, 2), (1, 1))
     with pytest.raises(ValueError):
         T.interpolate(x, locs, 4.0, kernel="gaussian")
+
+
+@pytest.mark.parametrize("gs,ps", [((256, 256), (320, 320)), ((205, 205, 205), (256, 256, 256)),
+                                   ((24, 20), (30, 25)), ((33,), (41,))])
+@pytest.mark.parametrize("pad_mode", ["circular", "zero"])
+def test_prep_locs_keeps_the_reference_rounding(gs, ps, pad_mode):
+    """The NUFFT's location rescaling (host-side torch ops) gives the
+    reference's float32 coordinates bit for bit: per dimension, multiply by
+    Np/N, add Np//2, clamp or wrap (linops/nufft.py:242-334), whether it runs
+    on all dimensions at once or one dimension at a time."""
+    from torchlinops_gb300 import linops
+
+    g = torch.Generator().manual_seed(len(gs) + ps[-1])
+    locs = (torch.rand(50000, len(gs), generator=g) - 0.5) * torch.tensor(gs, dtype=torch.float32) * 1.02
+    ref = locs.clone()
+    for i in range(-len(gs), 0):
+        ref[..., i] *= ps[i] / gs[i]
+        ref[..., i] += ps[i] // 2
+        if pad_mode == "zero":
+            ref[..., i] = torch.clamp(ref[..., i], 0, ps[i] - 1)
+        else:
+            ref[..., i] = torch.remainder(ref[..., i], torch.tensor(ps[i]))
+    assert torch.equal(linops.prep_locs(locs, gs, ps, pad_mode), ref)

@@ -549,17 +549,28 @@ def nufft_beta(width: float, oversamp: float) -> float:
 
 
 def prep_locs(locs: Tensor, grid_size, padded_size, pad_mode="circular") -> Tensor:
-    """Scale centred locs in [-N/2, N/2] to the padded grid (nufft.py:242-334)."""
+    """Scale centred locs in [-N/2, N/2] to the padded grid (nufft.py:242-334).
+
+    The same float operations per coordinate as the reference (multiply by
+    Np/N, add Np//2, then clamp or wrap), done on all dimensions at once when
+    their sizes agree (one kernel per operation instead of several per
+    dimension)."""
+    if pad_mode not in ("zero", "circular"):
+        raise ValueError(f"Unrecognized padding mode during prep: {pad_mode}")
+    nd = len(grid_size)
+    same = len(set(zip(grid_size, padded_size))) == 1
+    if same and locs.shape[-1] == nd:
+        n, p = grid_size[0], padded_size[0]
+        out = locs * (p / n) + p // 2
+        return torch.clamp(out, 0, p - 1) if pad_mode == "zero" else torch.remainder(out, p)
     out = locs.clone()
-    for i in range(-len(grid_size), 0):
+    for i in range(-nd, 0):
         out[..., i] *= padded_size[i] / grid_size[i]
         out[..., i] += padded_size[i] // 2
         if pad_mode == "zero":
             out[..., i] = torch.clamp(out[..., i], 0, padded_size[i] - 1)
-        elif pad_mode == "circular":
-            out[..., i] = torch.remainder(out[..., i], torch.tensor(padded_size[i], device=locs.device))
         else:
-            raise ValueError(f"Unrecognized padding mode during prep: {pad_mode}")
+            out[..., i] = torch.remainder(out[..., i], padded_size[i])
     return out
 
 
