@@ -639,6 +639,25 @@ class NUFFT(Chain):
         self.interp = interp
 
 
+_APOD: "OrderedDict[tuple, Tensor]" = OrderedDict()
+
+
+def _apod_on(device, grid_size, padded, oversamp: float, width: float, beta: float) -> Tensor:
+    """The apodization weights on ``device``, computed once per sizes and
+    kernel (the functional transforms would otherwise rebuild them on the
+    host and copy them over on every call)."""
+    key = (str(device), tuple(grid_size), tuple(padded), float(oversamp), float(width), float(beta))
+    w = _APOD.get(key)
+    if w is None:
+        w = apodize_weights(grid_size, padded, oversamp, width, beta).to(device)
+        _APOD[key] = w
+        while len(_APOD) > 16:
+            _APOD.popitem(last=False)
+    else:
+        _APOD.move_to_end(key)
+    return w
+
+
 _PREPARED_LOCS: "OrderedDict[tuple, tuple]" = OrderedDict()
 
 
@@ -672,8 +691,7 @@ def nufft(x: Tensor, locs: Tensor, oversamp: float = 1.25, width: float = 4.0) -
     ndim = locs.shape[-1]
     padded = tuple(int(s * oversamp) for s in grid_size)
     beta = nufft_beta(width, oversamp)
-    x = pad_shift(x, grid_size, padded, apod=apodize_weights(grid_size, padded, oversamp, width, beta).to(x.device),
-                  modulate=True)
+    x = pad_shift(x, grid_size, padded, apod=_apod_on(x.device, grid_size, padded, oversamp, width, beta), modulate=True)
     x = torch.fft.fftn(x, dim=tuple(range(-ndim, 0)), norm="ortho")
     x = I.interpolate(x, _prepared_locs(locs, grid_size, padded), width, kernel="kaiser_bessel",
                       kernel_params=dict(beta=beta))
@@ -691,5 +709,5 @@ def nufft_adjoint(x: Tensor, locs: Tensor, grid_size, oversamp: float = 1.25, wi
     x = I.interpolate_adjoint(x, _prepared_locs(locs, grid_size, padded), padded, width, kernel="kaiser_bessel",
                               kernel_params=dict(beta=beta))
     x = torch.fft.ifftn(x, dim=tuple(range(-ndim, 0)), norm="ortho")
-    return crop_shift(x, grid_size, padded, apod=apodize_weights(grid_size, padded, oversamp, width, beta).to(x.device),
+    return crop_shift(x, grid_size, padded, apod=_apod_on(x.device, grid_size, padded, oversamp, width, beta),
                       modulate=True)
