@@ -464,16 +464,18 @@ def bench_nufft2d(dev, peak):
     s = torch.cuda.current_stream(dev)
 
     def timed(fn, reps=10):
+        # median of per-call CUDA-event times (a call includes host work:
+        # autograd, plan lookups), so one slow call does not skew the figure
         for _ in range(3):
             fn()
         torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(s)
-        for _ in range(reps):
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+        for e0, e1 in ev:
+            e0.record(s)
             fn()
-        e1.record(s)
+            e1.record(s)
         torch.cuda.synchronize()
-        return e0.elapsed_time(e1) / reps
+        return statistics.median(e0.elapsed_time(e1) for e0, e1 in ev)
 
     def fwd():
         with torch.no_grad():

@@ -1197,14 +1197,17 @@ __device__ __forceinline__ float2 mul2_bcast(float s, float2 v) {
 // registers.
 constexpr int kAB = 256;
 
+// Rows are padded (28 and 20 floats) so that the staging threads' 16-byte
+// stores, one row per thread, spread over all banks.
 struct AdjStage {
-  float wrow[kAB][24];  // tap weights at tile-local x (0-7), y (8-15), z (16-23)
-  float pv[kAB][16];    // point values, 8 entries complex
+  float wrow[kAB][28];  // tap weights at tile-local x (0-7), y (8-15), z (16-23)
+  float pv[kAB][20];    // point values, 8 entries complex (16 floats)
   int pidx[kAB];
   unsigned fmask[8][kAB / 32];  // per plane: entries on the row path with taps there
   unsigned smask[kAB / 32];     // entries on the generic path (all planes)
 };
 
+static_assert(kAB == 256, "one staged pair per thread of the 8 warps; every warp owns a mask word");
 constexpr size_t adj_f3_smem() { return sizeof(AdjStage) + 8 * sizeof(Rec<5>); }
 
 __global__ void __launch_bounds__(256, 3) adj_f3_kernel(Geo g, const int4* __restrict__ items,
@@ -1468,11 +1471,12 @@ __device__ __forceinline__ unsigned grid_view2(const Geo& g, const PRec& R, cons
 // there. Each warp applies its slab's pairs in plan order, two per step, then
 // the pairs that need the generic record (5 taps, a window wrapping inside
 // the tile, a non-finite value), also in order.
-constexpr int kAB2 = 256;
+constexpr int kAB2 = 224;
 
+// Rows padded as in AdjStage (36 and 20 floats); 224 pairs keep 4 CTAs per SM.
 struct AdjStage2 {
-  float wrow[kAB2][32];  // tap weights at tile-local y (0-15) and z (16-31)
-  float pv[kAB2][16];    // point values, 8 entries complex
+  float wrow[kAB2][36];  // tap weights at tile-local y (0-15) and z (16-31)
+  float pv[kAB2][20];    // point values, 8 entries complex (16 floats)
   int pidx[kAB2];
   unsigned fmask[8][kAB2 / 32];  // per slab: pairs on the row path with taps there
   unsigned smask[kAB2 / 32];     // pairs on the generic path (all slabs)
@@ -1564,13 +1568,14 @@ __global__ void __launch_bounds__(256, 4) adj_f2_kernel(Geo g, const int4* __res
       }
       const bool ok = (view >> 28) & 1, fast = ((view >> 27) & 1) && finite;
       const int fy = view & 15, my = (view >> 4) & 7;
+      // warps past kAB2 / 32 stage no pairs and own no mask word
 #pragma unroll
       for (int w = 0; w < NW; ++w) {
         const unsigned bal = __ballot_sync(0xffffffffu, ok && fast && fy <= 2 * w + 1 && fy + my > 2 * w);
-        if (lane == 0) S.fmask[w][warp] = bal;
+        if (lane == 0 && warp < MW) S.fmask[w][warp] = bal;
       }
       const unsigned bs = __ballot_sync(0xffffffffu, ok && !fast);
-      if (lane == 0) S.smask[warp] = bs;
+      if (lane == 0 && warp < MW) S.smask[warp] = bs;
     }
     __syncthreads();
     struct Visit {
