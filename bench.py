@@ -438,7 +438,7 @@ def bench_blocks(dev, peak, args):
     torch.cuda.empty_cache()
     return {
         "unfold": {"ms": u_ms, "GBps": nbytes / (u_ms / 1e3) / 1e9, "frac": nbytes / (u_ms / 1e3) / 1e9 / peak,
-                   "workload": "16x160^3 c64, block 8^3, stride 4"},
+                   "workload": f"{BLK_SHAPE[0]}x160^3 c64, block 8^3, stride 4"},
         "fold": {"ms": f_ms, "GBps": nbytes / (f_ms / 1e3) / 1e9, "frac": nbytes / (f_ms / 1e3) / 1e9 / peak},
     }
 
@@ -588,9 +588,19 @@ def main():
     ap.add_argument("--cg-steps", type=int, default=500, help="preconditioner training steps (4 samples each)")
     ap.add_argument("--grid", type=int, default=N_GRID, help="grid edge (smaller cases for profiling)")
     ap.add_argument("--points", type=int, default=N_PTS, help="number of points (smaller cases for profiling)")
+    ap.add_argument("--blocks-batch", type=int, default=BLK_SHAPE[0],
+                    help="array entries of the unfold/fold workload (smaller cases for profiling)")
+    ap.add_argument("--nufft2d-only", action="store_true",
+                    help="profiling: run only the 2D NUFFT timing and print its figures (not the bench line)")
     args = ap.parse_args()
     _resize(args.grid, args.points)
+    globals()["BLK_SHAPE"] = (args.blocks_batch,) + BLK_SHAPE[1:]
     args.warmup = max(args.warmup, 3)
+    if args.nufft2d_only:
+        dev = torch.device("cuda", 0)
+        torch.cuda.set_device(dev)
+        print(json.dumps({"nufft2d": bench_nufft2d(dev, measured_peaks()[0])}), flush=True)
+        return
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)
