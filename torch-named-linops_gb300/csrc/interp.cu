@@ -48,7 +48,6 @@ namespace {
 constexpr int NTMAX = 16;  // taps per dimension supported (width < 15)
 constexpr int NWARP = 8;   // warps per CTA
 constexpr int NTHR = 32 * NWARP;
-constexpr int PB = 64;     // points per adjoint batch
 constexpr int CGMAX = 8;   // batch entries per coil group
 
 struct Geo {
@@ -530,7 +529,7 @@ __global__ void __launch_bounds__(NW * 32, 1) interp_fwd_kernel(Geo g, const int
                                                                 const float* __restrict__ locs,
                                                                 const float* __restrict__ gridv,
                                                                 float* __restrict__ out, int CG) {
-  extern __shared__ __align__(16) unsigned char smem[];
+  extern __shared__ __align__(128) unsigned char smem[];
   const int es = g.cplx ? 2 : 1;
   const int4 it = items[blockIdx.x];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -712,7 +711,7 @@ __global__ void __launch_bounds__(32) interp_adj_kernel(Geo g, const int4* __res
                                                         const float* __restrict__ locs,
                                                         const float* __restrict__ vals, float* __restrict__ gridv,
                                                         float* __restrict__ partial, int CG) {
-  extern __shared__ __align__(16) unsigned char smem[];
+  extern __shared__ __align__(128) unsigned char smem[];
   const int es = g.cplx ? 2 : 1;
   const int4 it = items[blockIdx.x];
   const int lane = threadIdx.x;
@@ -2148,7 +2147,7 @@ __global__ void __launch_bounds__(NTHR) interp_grad_kernel(Geo g, const int4* __
                                                               const V* __restrict__ gridv, const V* __restrict__ a,
                                                               float* __restrict__ grad, int CG, int chunk,
                                                               float* __restrict__ partial) {
-  extern __shared__ __align__(16) unsigned char smem[];
+  extern __shared__ __align__(128) unsigned char smem[];
   const int4 it = items[blockIdx.x];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int tc[3];
