@@ -77,3 +77,28 @@ def test_fixed_scratch_rejects_plans_beyond_its_buffer():
     st = _fixed_call(desc, _P, locs, vals, out)
     assert st == _ext.TLGB_ERR_WORKSPACE
     assert b"fixed" in _ext.lib().tlgb_last_error()
+
+
+@pytest.mark.parametrize("ndim", [3, 2])
+def test_fixed_scratch_without_room_for_the_transposed_values(ndim):
+    """When the point-major copy of the values does not fit beside the
+    partial tiles in the fixed buffer (600,000 points x 64 bytes > 32 MiB),
+    the 8-entry gridding kernels stage the values straight from [entry][point]
+    order: the same values in the same order, so the same grid bit for bit."""
+    gen = torch.Generator().manual_seed(5 + ndim)
+    # uniform points: few or no split tiles, so the partial tiles fit
+    n, npts, nb = (128 if ndim == 3 else 160), 600_000, 8
+    locs = (torch.rand(npts, ndim, generator=gen) * n).float().to(DEV)
+    vals = torch.randn(nb, npts, dtype=torch.complex64, generator=gen).to(DEV)
+    beta = T.kaiser_bessel_beta(4.0, 1.25)
+    size = (n,) * ndim
+    ref = T.grid(vals, locs, size, 4.0, kernel_params=dict(beta=beta))
+    plan = interp.get_plan(locs, size, 4.0, "kaiser_bessel", "circular", beta)
+    desc = interp._desc(ndim, size, (4.0,) * ndim, "kaiser_bessel", 1, "circular", beta, True, nb, npts)
+    out = torch.full((nb, *size), float("nan"), dtype=torch.complex64, device=DEV)
+    st = _fixed_call(desc, plan, locs, vals, out)
+    if st == _ext.TLGB_ERR_WORKSPACE:
+        pytest.skip("this plan's partial tiles alone exceed the fixed buffer")
+    assert st == _ext.TLGB_OK, _ext.lib().tlgb_last_error()
+    torch.cuda.synchronize()
+    assert torch.equal(out, ref)
