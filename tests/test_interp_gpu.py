@@ -295,6 +295,29 @@ def test_trajectory_gradient_2d_eight_entry_path(nb, pad, kernel):
     assert rel_l2(L2.grad.cpu(), ref2) < 1e-4
 
 
+@pytest.mark.parametrize("ndim,norm,nb", [(3, 1, 24), (2, 2, 20)])
+def test_trajectory_gradient_split_over_coil_groups(ndim, norm, nb):
+    """The generic gradient kernel with several coil groups of 8 entries,
+    split over CTAs with partial sums added in a fixed order, against the
+    FP64 autograd restatement."""
+    gen = torch.Generator().manual_seed(40 + ndim)
+    n = 24 if ndim == 3 else 48
+    size = (n,) * ndim
+    locs = _safe_points(3000, n, 4.0, gen, ndim)
+    img = torch.complex(torch.randn(nb, *size, generator=gen), torch.randn(nb, *size, generator=gen))
+    a = torch.complex(torch.randn(nb, 3000, generator=gen), torch.randn(nb, 3000, generator=gen))
+    kp = dict(beta=OI.nufft_beta(4.0, 1.25))
+    L = locs.to(DEV).requires_grad_(True)
+    out = T.interpolate(img.to(DEV), L, 4.0, norm=norm, kernel_params=kp)
+    (a.to(DEV).conj() * out).real.sum().backward()
+    ref = OI.grad_locs_interp(img, a, locs, 4.0, "kaiser_bessel", norm, "circular", kp["beta"])
+    assert rel_l2(L.grad.cpu(), ref) < 1e-4
+    L2 = locs.to(DEV).requires_grad_(True)
+    out2 = T.interpolate(img.to(DEV), L2, 4.0, norm=norm, kernel_params=kp)
+    (a.to(DEV).conj() * out2).real.sum().backward()
+    assert torch.equal(L.grad, L2.grad)  # fixed order of the partial sums
+
+
 def test_trajectory_gradient_finite_differences():
     """d/dx by central differences of the FP64 oracle (h = 1e-4 grid units)."""
     gen = torch.Generator().manual_seed(21)
