@@ -1209,7 +1209,7 @@ struct AdjStage {
 static_assert(kAB == 256, "one staged pair per thread of the 8 warps; every warp owns a mask word");
 constexpr size_t adj_f3_smem() { return sizeof(AdjStage) + 8 * sizeof(Rec<5>); }
 
-__global__ void __launch_bounds__(256, 3) adj_f3_kernel(Geo g, const int4* __restrict__ items,
+__global__ void __launch_bounds__(256, 4) adj_f3_kernel(Geo g, const int4* __restrict__ items,
                                                         const int32_t* __restrict__ entries,
                                                         const PRec* __restrict__ precs,
                                                         const float* __restrict__ locs, const float* __restrict__ vals,
@@ -1303,8 +1303,8 @@ __global__ void __launch_bounds__(256, 3) adj_f3_kernel(Geo g, const int4* __res
     }
     __syncthreads();
     // row path: every lane updates its 4 cells x 4 entries (zero weights
-    // outside the window); two entries per step, loads first, updates in
-    // entry order
+    // outside the window), one entry at a time in entry order (at 64
+    // registers 4 CTAs fit per SM; that beats two entries per step at 3)
     struct Visit {
       float2 wa, wb;  // weights of the lane's z slots
       float4 v0, v1;  // the lane's 4 entries, complex
@@ -1336,16 +1336,7 @@ __global__ void __launch_bounds__(256, 3) adj_f3_kernel(Geo g, const int4* __res
       while (bits) {
         const int j0 = mw * 32 + __ffs(bits) - 1;
         bits &= bits - 1;
-        const Visit d0 = fetch(j0);
-        if (bits) {
-          const int j1 = mw * 32 + __ffs(bits) - 1;
-          bits &= bits - 1;
-          const Visit d1 = fetch(j1);
-          apply(d0);
-          apply(d1);
-        } else {
-          apply(d0);
-        }
+        apply(fetch(j0));
       }
     }
     // generic path: exact-integer coordinates (5 taps) or a window wrapping
