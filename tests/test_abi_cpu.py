@@ -111,3 +111,45 @@ def test_prep_locs_keeps_the_reference_rounding(gs, ps, pad_mode):
         else:
             ref[..., i] = torch.remainder(ref[..., i], torch.tensor(ps[i]))
     assert torch.equal(linops.prep_locs(locs, gs, ps, pad_mode), ref)
+
+
+def _header_prototypes():
+    """{name: [parameter type, ...]} of the functions declared in tlgb.h."""
+    txt = open(os.path.join(ROOT, "include", "tlgb.h")).read()
+    txt = re.sub(r"/\*.*?\*/", " ", txt, flags=re.S)
+    protos = {}
+    for m in re.finditer(r"\b(?:int|size_t|const char\s*\*)\s+(tlgb_[a-z0-9_]+)\s*\(([^)]*)\)\s*;", txt):
+        params = " ".join(m.group(2).split())
+        if params in ("", "void"):
+            protos[m.group(1)] = []
+            continue
+        types = []
+        for p in params.split(","):
+            p = p.strip()
+            # drop the parameter name
+            p = re.sub(r"\b[a-z_][a-z0-9_]*$", "", p).strip() if not p.endswith("*") else p
+            types.append(p)
+        protos[m.group(1)] = types
+    return protos
+
+
+def _ctype_matches(c_type: str, ct) -> bool:
+    if "*" in c_type or c_type == "tlgb_stream_t":
+        return ct in (ctypes.c_void_p, ctypes.c_char_p) or getattr(ct, "__name__", "").startswith("LP_")
+    table = {"int64_t": ctypes.c_int64, "int32_t": ctypes.c_int32, "size_t": ctypes.c_size_t, "float": ctypes.c_float,
+             "double": ctypes.c_double, "int": ctypes.c_int}
+    want = table.get(c_type.replace("const ", "").strip())
+    return want is not None and ctypes.sizeof(want) == ctypes.sizeof(ct) and (want is ct or want == ct)
+
+
+def test_ctypes_signatures_match_the_header():
+    """Every binding in _ext has the declared number of parameters, each of a
+    matching kind and width (pointer, 32/64-bit integer, size_t, float)."""
+    protos = _header_prototypes()
+    assert protos
+    assert set(protos) == set(_ext._SIGNATURES), set(protos) ^ set(_ext._SIGNATURES)
+    for name, ctypes_args in ((n, s[0]) for n, s in _ext._SIGNATURES.items()):
+        c_args = protos[name]
+        assert len(c_args) == len(ctypes_args), f"{name}: header {len(c_args)} params, ctypes {len(ctypes_args)}"
+        for i, (c, ct) in enumerate(zip(c_args, ctypes_args)):
+            assert _ctype_matches(c, ct), f"{name} parameter {i}: header {c!r}, ctypes {ct}"
