@@ -62,7 +62,11 @@ enum { TLGB_PAD_CIRCULAR = 0, TLGB_PAD_ZERO = 1 };
 /* Problem description shared by every interpolation call.
  * Layouts (C order): grid values [nbatch, grid_size[0..ndim-1]], point values
  * [nbatch, npts], locs [npts, ndim] float32 in grid units ('ij' order).
- * is_complex: values are complex64 stored as interleaved (re, im) float32. */
+ * is_complex: values are complex64 stored as interleaved (re, im) float32.
+ * nbatch is at most TLGB_INTERP_MAX_BATCH per call (larger batches return
+ * TLGB_ERR_UNSUPPORTED before any launch; split them, as consecutive batch
+ * entries are independent). */
+#define TLGB_INTERP_MAX_BATCH 524280 /* 65535 launch rows of 8 entries */
 typedef struct tlgb_interp_desc {
   int32_t ndim;         /* 1, 2 or 3 */
   int32_t kernel;       /* TLGB_KERNEL_* */
@@ -187,7 +191,10 @@ enum { TLGB_F32 = 0, TLGB_F64 = 1, TLGB_C64 = 2, TLGB_C128 = 3 };
  * device) is the row-major offset inside one block of the j-th kept element
  * (ascending) and mask_inv[k] (int32, device, prod(block) entries) is the
  * index j of block offset k, or -1 where the mask is false. Both NULL means
- * no mask. nblocks[e] = (im_size[e]-block[e])/stride[e]+1. */
+ * no mask. nblocks[e] = (im_size[e]-block[e])/stride[e]+1. One call handles
+ * below 2^31 rows of blocks (nbatch * nblocks[0] * nblocks[1]) and below 2^31
+ * array planes (nbatch * im_size[0] of a 3D array); above that it returns
+ * TLGB_ERR_UNSUPPORTED before any launch. */
 typedef struct tlgb_blocks_desc {
   int32_t ndim;
   int32_t dtype;       /* TLGB_F32 ... TLGB_C128 */

@@ -153,3 +153,45 @@ def test_ctypes_signatures_match_the_header():
         assert len(c_args) == len(ctypes_args), f"{name}: header {len(c_args)} params, ctypes {len(ctypes_args)}"
         for i, (c, ct) in enumerate(zip(c_args, ctypes_args)):
             assert _ctype_matches(c, ct), f"{name} parameter {i}: header {c!r}, ctypes {ct}"
+
+
+def test_launch_limits_are_host_errors():
+    """Sizes whose launch grid would overflow are rejected on the host before
+    any launch, with TLGB_ERR_UNSUPPORTED: an interpolation batch above
+    TLGB_INTERP_MAX_BATCH (the Python layer splits such batches), a block op
+    with 2^31 rows of blocks or array planes, a pad/crop volume of 2^38
+    voxels."""
+    from torchlinops_gb300 import interp as I
+
+    L = _ext.lib()
+    txt = open(os.path.join(ROOT, "include", "tlgb.h")).read()
+    assert I.MAX_BATCH == int(re.search(r"#define TLGB_INTERP_MAX_BATCH (\d+)", txt).group(1)) == 8 * 65535
+    assert _size(_desc(nbatch=I.MAX_BATCH))[0] == 0
+    assert _size(_desc(nbatch=I.MAX_BATCH + 1))[0] == _ext.TLGB_ERR_UNSUPPORTED
+    assert b"batch" in L.tlgb_last_error()
+
+    d = _ext.BlocksDesc()
+    d.ndim, d.dtype, d.nbatch = 1, 0, 1 << 31
+    d.im_size[0], d.block[0], d.stride[0] = 8, 4, 4
+    d.nnz = 4
+    p = ctypes.c_void_p(16)
+    assert L.tlgb_unfold(ctypes.byref(d), p, p, None) == _ext.TLGB_ERR_UNSUPPORTED
+    assert L.tlgb_fold(ctypes.byref(d), p, p, None) == _ext.TLGB_ERR_UNSUPPORTED
+    assert b"batch" in L.tlgb_last_error()
+
+    big = (ctypes.c_int64 * 3)(1 << 29, 1 << 29, 1 << 29)
+    zero = (ctypes.c_int64 * 3)(0, 0, 0)
+    st = L.tlgb_pad_shift_c64(p, 1, 3, big, big, zero, zero, 0, None, None, 0, p, None)
+    assert st == _ext.TLGB_ERR_UNSUPPORTED
+    st = L.tlgb_crop_shift_c64(p, 1, 3, big, big, zero, zero, 0, None, None, 0, 1.0, None, 0.0, p, None)
+    assert st == _ext.TLGB_ERR_UNSUPPORTED
+
+
+def test_batch_ranges():
+    from torchlinops_gb300 import interp as I
+
+    M = I.MAX_BATCH
+    assert I._batch_chunks(0) == [(0, 0)]
+    assert I._batch_chunks(5) == [(0, 5)]
+    assert I._batch_chunks(M) == [(0, M)]
+    assert I._batch_chunks(2 * M + 3) == [(0, M), (M, 2 * M), (2 * M, 2 * M + 3)]

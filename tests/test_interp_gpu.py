@@ -318,6 +318,37 @@ def test_trajectory_gradient_split_over_coil_groups(ndim, norm, nb):
     assert torch.equal(L.grad, L2.grad)  # fixed order of the partial sums
 
 
+def test_batch_above_one_call_is_split():
+    """A batch of MAX_BATCH + 3 entries (above one call of the C ABI) runs as
+    two calls of MAX_BATCH and 3 entries: the forward and adjoint against the
+    FP64 oracle on the entries either side of the split, and the trajectory
+    gradient, a sum over the whole batch, against the FP64 restatement. The
+    last 3 cotangent rows are scaled by 300 so that both calls carry a large
+    share of the gradient."""
+    from torchlinops_gb300 import interp as I
+
+    M = I.MAX_BATCH
+    nb, n, npts = M + 3, 16, 3
+    gen = torch.Generator().manual_seed(12)
+    locs = _safe_points(npts, n, 4.0, gen, 1)
+    img = torch.randn(nb, n, dtype=torch.complex64, generator=gen)
+    pts = torch.randn(nb, npts, dtype=torch.complex64, generator=gen)
+    pts[M:] *= 300
+    beta = OI.nufft_beta(4.0, 1.25)
+    kp = dict(beta=beta)
+    idx = torch.tensor([0, M - 1, M, M + 2])
+    L = locs.to(DEV).requires_grad_(True)
+    fwd = T.interpolate(img.to(DEV), L, 4.0, kernel_params=kp)
+    assert fwd.shape == (nb, npts)
+    assert rel_l2(fwd.detach().cpu()[idx], OI.ungrid(img[idx], locs, 4.0, beta=beta, dtype=torch.float64)) < TOL
+    adj = T.interpolate_adjoint(pts.to(DEV), locs.to(DEV), (n,), 4.0, kernel_params=kp).cpu()
+    assert adj.shape == (nb, n)
+    assert rel_l2(adj[idx], OI.grid(pts[idx], locs, (n,), 4.0, beta=beta, dtype=torch.float64)) < TOL
+    (pts.to(DEV).conj() * fwd).real.sum().backward()
+    ref = OI.grad_locs_interp(img, pts, locs, 4.0, "kaiser_bessel", 1, "circular", beta)
+    assert rel_l2(L.grad.cpu(), ref) < 1e-4
+
+
 def test_trajectory_gradient_finite_differences():
     """d/dx by central differences of the FP64 oracle (h = 1e-4 grid units)."""
     gen = torch.Generator().manual_seed(21)

@@ -275,6 +275,10 @@ int check_desc(const tlgb_blocks_desc* d, BlkGeo& g, int& esize) {
   // 32-bit index arithmetic inside one slab / plane
   if (g.nb[2] * bvol >= (1ll << 31) || g.im[1] * g.im[2] >= (1ll << 31) || g.im[0] >= (1ll << 31))
     TLGB_FAIL(TLGB_ERR_UNSUPPORTED, "block op too large for 32-bit slab indexing");
+  // one CTA per slab (unfold) or array plane (fold): grid x below 2^31
+  const int64_t lim = (1ll << 31) - 1;
+  if (g.nbatch > 0 && (g.nbatch > lim / (g.nb[0] * g.nb[1]) || g.nbatch > lim / g.im[0]))
+    TLGB_FAIL(TLGB_ERR_UNSUPPORTED, "block op batch too large for one launch: split the batch");
   return TLGB_OK;
 }
 

@@ -151,6 +151,9 @@ int make_pad_geo(int32_t ndim, const int64_t* n, const int64_t* np, const int64_
     G.np[e] = (int)pe;
     G.off[e] = (int)oe;
     G.sh[e] = (int)se;
+    // one thread per padded voxel: grid x below 2^31 CTAs of 256
+    if (G.npvol > ((1ll << 38) - 1) / pe)
+      TLGB_FAIL(TLGB_ERR_UNSUPPORTED, "pad/crop: padded volume too large for one launch");
     G.nvol *= ne;
     G.npvol *= pe;
   }

@@ -2519,6 +2519,9 @@ int make_geo(const tlgb_interp_desc* d, Geo& g) {
   if (d->norm != 1 && d->norm != 2) TLGB_FAIL(TLGB_ERR_INVALID, "norm must be 1 or 2");
   if (d->pad_mode != TLGB_PAD_CIRCULAR && d->pad_mode != TLGB_PAD_ZERO) TLGB_FAIL(TLGB_ERR_INVALID, "unknown pad mode");
   if (d->npts < 0 || d->nbatch < 0) TLGB_FAIL(TLGB_ERR_INVALID, "negative size");
+  // the 8-entry kernels launch one grid row per 8 batch entries (at most 65535)
+  if (d->nbatch > TLGB_INTERP_MAX_BATCH)
+    TLGB_FAIL(TLGB_ERR_UNSUPPORTED, "batch above 524280 entries in one call: split the batch");
   memset(&g, 0, sizeof(g));
   g.ndim = d->ndim;
   const int off = 3 - d->ndim;

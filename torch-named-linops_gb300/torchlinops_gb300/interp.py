@@ -175,6 +175,16 @@ def get_plan(locs: Tensor, grid_size, width, kernel: str, pad_mode: str, beta: f
     return plan
 
 
+# batch entries per C-ABI call (TLGB_INTERP_MAX_BATCH in include/tlgb.h)
+MAX_BATCH = 524280
+
+
+def _batch_chunks(nbatch: int) -> list[tuple[int, int]]:
+    """[begin, end) ranges of at most MAX_BATCH batch entries (one empty range
+    for an empty batch); batch entries are independent."""
+    return [(b, min(b + MAX_BATCH, nbatch)) for b in range(0, nbatch, MAX_BATCH)] or [(0, 0)]
+
+
 def _check_values(vals: Tensor) -> bool:
     if vals.dtype == torch.complex64:
         return True
@@ -220,15 +230,19 @@ def ungrid(
     out = torch.empty(nbatch, npts, dtype=vals.dtype, device=dev)
     d = _desc(ndim, grid_size, width, kernel, norm, pad_mode, beta, is_complex, nbatch, npts)
     v = _as_f32_view(vals, is_complex)
+    if nbatch > MAX_BATCH:
+        v = v.reshape(nbatch, -1)
     lc = _locs_f32(locs)
     with torch.cuda.device(dev):
-        _ext.check(
-            _ext.lib().tlgb_interp_forward(
-                ctypes.byref(d), ctypes.byref(plan.info), _ext.ptr(plan.buffer), _ext.ptr(lc), _ext.ptr(v),
-                _ext.ptr(out), _ext.stream_ptr(dev),
-            ),
-            "ungrid",
-        )
+        for b0, b1 in _batch_chunks(nbatch):
+            d.nbatch = b1 - b0
+            _ext.check(
+                _ext.lib().tlgb_interp_forward(
+                    ctypes.byref(d), ctypes.byref(plan.info), _ext.ptr(plan.buffer), _ext.ptr(lc),
+                    _ext.ptr(v[b0:b1] if nbatch > MAX_BATCH else v), _ext.ptr(out[b0:b1]), _ext.stream_ptr(dev),
+                ),
+                "ungrid",
+            )
     return out.reshape(*batch_shape, *locs_batch_shape)
 
 
@@ -268,22 +282,28 @@ def grid(
     is_complex = _check_values(vals)
     beta = kernel_params["beta"] if kernel == "kaiser_bessel" else 1.0
     plan = get_plan(locs, grid_size, width, kernel, pad_mode, beta, norm)
-    d = _desc(ndim, grid_size, width, kernel, norm, pad_mode, beta, is_complex, nbatch, npts)
+    # the first batch range is the largest: its scratch serves every range
+    d = _desc(ndim, grid_size, width, kernel, norm, pad_mode, beta, is_complex, min(nbatch, MAX_BATCH), npts)
     L = _ext.lib()
     sb = ctypes.c_size_t(0)
     _ext.check(L.tlgb_interp_adjoint_scratch_size(ctypes.byref(d), ctypes.byref(plan.info), ctypes.byref(sb)), "grid")
     out = torch.empty(nbatch, *grid_size, dtype=vals.dtype, device=dev)
     scratch = torch.empty(max(sb.value, 1), dtype=torch.uint8, device=dev)
     v = _as_f32_view(vals, is_complex)
+    if nbatch > MAX_BATCH:
+        v = v.reshape(nbatch, -1)
     lc = _locs_f32(locs)
     with torch.cuda.device(dev):
-        _ext.check(
-            L.tlgb_interp_adjoint(
-                ctypes.byref(d), ctypes.byref(plan.info), _ext.ptr(plan.buffer), _ext.ptr(lc), _ext.ptr(v),
-                _ext.ptr(out), _ext.ptr(scratch), sb.value, _ext.stream_ptr(dev),
-            ),
-            "grid",
-        )
+        for b0, b1 in _batch_chunks(nbatch):
+            d.nbatch = b1 - b0
+            _ext.check(
+                L.tlgb_interp_adjoint(
+                    ctypes.byref(d), ctypes.byref(plan.info), _ext.ptr(plan.buffer), _ext.ptr(lc),
+                    _ext.ptr(v[b0:b1] if nbatch > MAX_BATCH else v), _ext.ptr(out[b0:b1]), _ext.ptr(scratch),
+                    sb.value, _ext.stream_ptr(dev),
+                ),
+                "grid",
+            )
     return out.reshape(*batch_shape, *grid_size)
 
 
@@ -301,10 +321,14 @@ def _grad_locs(gridvals: Tensor, a: Tensor, locs: Tensor, width, kernel, norm, p
         a = a.to(gridvals.dtype)
     beta = kernel_params["beta"] if kernel == "kaiser_bessel" else 1.0
     plan = get_plan(locs, grid_size, width, kernel, pad_mode, beta, norm)
-    d = _desc(ndim, grid_size, width, kernel, norm, pad_mode, beta, is_complex, nbatch, npts)
+    d = _desc(ndim, grid_size, width, kernel, norm, pad_mode, beta, is_complex, min(nbatch, MAX_BATCH), npts)
     g = _as_f32_view(gridvals, is_complex)
     av = _as_f32_view(a.reshape(nbatch, npts), is_complex)
+    chunks = _batch_chunks(nbatch)
+    if len(chunks) > 1:
+        g = g.reshape(nbatch, -1)
     out = torch.empty(npts, ndim, dtype=torch.float32, device=dev)
+    part = torch.empty_like(out) if len(chunks) > 1 else out
     lc = _locs_f32(locs)
     L = _ext.lib()
     sb = ctypes.c_size_t(0)
@@ -312,13 +336,20 @@ def _grad_locs(gridvals: Tensor, a: Tensor, locs: Tensor, width, kernel, norm, p
                "trajectory gradient")
     scratch = torch.empty(max(sb.value, 1), dtype=torch.uint8, device=dev)
     with torch.cuda.device(dev):
-        _ext.check(
-            L.tlgb_interp_grad_locs(
-                ctypes.byref(d), ctypes.byref(plan.info), _ext.ptr(plan.buffer), _ext.ptr(lc), _ext.ptr(g),
-                _ext.ptr(av), _ext.ptr(out), _ext.ptr(scratch), sb.value, _ext.stream_ptr(dev),
-            ),
-            "trajectory gradient",
-        )
+        # the gradient sums over the batch: one call per batch range, the
+        # ranges' results added in order
+        for i, (b0, b1) in enumerate(chunks):
+            d.nbatch = b1 - b0
+            _ext.check(
+                L.tlgb_interp_grad_locs(
+                    ctypes.byref(d), ctypes.byref(plan.info), _ext.ptr(plan.buffer), _ext.ptr(lc),
+                    _ext.ptr(g[b0:b1] if len(chunks) > 1 else g), _ext.ptr(av[b0:b1]),
+                    _ext.ptr(out if i == 0 else part), _ext.ptr(scratch), sb.value, _ext.stream_ptr(dev),
+                ),
+                "trajectory gradient",
+            )
+            if i > 0:
+                out += part
     return out.reshape(locs.shape).to(locs.dtype)
 
 
