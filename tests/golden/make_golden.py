@@ -171,6 +171,44 @@ def make_nufft(F, out_dir):
     np.savez_compressed(os.path.join(out_dir, "nufft.npz"), **out)
 
 
+TOEPLITZ_SPECS = {
+    # name: (grid_size, points, batch of the image, density weights)
+    "2d": ((16, 16), 60, (), False),
+    "2d_batch_dcf": ((12, 16), 45, (3,), True),
+    # 14 pads to 17, and the 2x grid's 28 to 35, not 2 * 17: the reference
+    # rescales the points to 34 cells on a 35-cell grid (its PSF is then off)
+    "2d_odd_pad": ((12, 14), 45, (2,), False),
+    "3d": ((8, 8, 8), 40, (), False),
+}
+
+
+def make_toeplitz(L, out_dir):
+    """The NUFFT's Toeplitz normal (linops/nufft.py:226-239, 395-494): the
+    PSF kernel (the Dense weight, centred k-space on the 2x grid) and the
+    normal operator applied to a seeded image, with and without a diagonal
+    weighting of the points (``inner``)."""
+    from torchlinops.linops.nufft import toeplitz_psf
+
+    out = {}
+    for name, (shape, npts, batch, dcf) in TOEPLITZ_SPECS.items():
+        gen = torch.Generator().manual_seed(7 + len(shape) + npts)
+        locs = (torch.rand(npts, len(shape), generator=gen) - 0.5) * torch.tensor(shape, dtype=torch.float32)
+        x = _rand(tuple(batch) + tuple(shape), True, gen)
+        A = L.NUFFT(locs, shape, output_shape=("K",), toeplitz=True)
+        inner = None
+        if dcf:
+            w = torch.rand(npts, generator=gen) + 0.5
+            inner = L.Diagonal(w, ioshape=("...", "K"))
+            out[f"{name}_dcf"] = _np(w)
+        T = A.normal(inner)
+        kern = toeplitz_psf(A, inner)
+        out[f"{name}_locs"] = _np(locs)
+        out[f"{name}_x"] = _np(x)
+        out[f"{name}_kernel"] = _np(kern.weight.reshape(kern.weight.shape[-len(shape):]))
+        out[f"{name}_normal"] = _np(T(x).reshape(x.shape))
+    np.savez_compressed(os.path.join(out_dir, "toeplitz.npz"), **out)
+
+
 def make_kernels(K, out_dir):
     x = torch.linspace(-1.2, 1.2, 241)
     out = {"x": _np(x)}
@@ -245,18 +283,25 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference/src")
     ap.add_argument("--out", default=HERE)
+    ap.add_argument("--only", choices=["toeplitz"], default=None, help="write only this fixture")
     args = ap.parse_args()
     sys.path.insert(0, os.path.join(HERE, "_stubs"))
     sys.path.insert(0, args.ref)
     torch.set_num_threads(os.cpu_count() or 1)
     import torchlinops.functional as F
+    import torchlinops.linops as L
     from torchlinops.functional._interp import kernels as K
 
     t0 = time.time()
+    if args.only == "toeplitz":
+        make_toeplitz(L, args.out)
+        print(f"wrote toeplitz.npz in {time.time() - t0:.1f}s")
+        return
     make_kernels(K, args.out)
     make_edgecases(F, args.out)
     make_config1(F, args.out)
     make_nufft(F, args.out)
+    make_toeplitz(L, args.out)
     n_i = make_interp(F, args.out)
     n_b = make_blocks(F, args.out)
     print(f"wrote {n_i} interp cases, {n_b} block cases in {time.time() - t0:.1f}s")

@@ -131,3 +131,28 @@ def test_nufft_oracle_matches_reference_golden(name):
     for dtype, tol in ((torch.float32, 2e-6), (torch.float64, 1e-5)):
         assert rel_l2(ON.nufft(x, locs, dtype=dtype), fwd) < tol
         assert rel_l2(ON.nufft_adjoint(y, locs, tuple(x.shape[-locs.shape[-1]:]), dtype=dtype), adj) < tol
+
+
+TOEPLITZ = {"2d": (16, 16), "2d_batch_dcf": (12, 16), "2d_odd_pad": (12, 14), "3d": (8, 8, 8)}
+
+
+@pytest.mark.parametrize("name", sorted(TOEPLITZ))
+def test_toeplitz_oracle_matches_reference_golden(name):
+    """The Toeplitz PSF kernel and normal operator of the oracle (float32
+    mirror and FP64) against the reference's NUFFT(toeplitz=True).normal(inner)
+    and toeplitz_psf outputs, including a diagonal point weighting with a
+    batched image and the odd-padding case whose rescaled points and larger
+    grid disagree by one cell."""
+    from oracle import nufft as ON
+
+    d = np.load(f"{GOLDEN}/toeplitz.npz")
+    shape = TOEPLITZ[name]
+    locs = torch.from_numpy(d[f"{name}_locs"])
+    x = to_torch(d[f"{name}_x"], True)
+    w = torch.from_numpy(d[f"{name}_dcf"]) if f"{name}_dcf" in d.files else None
+    kern = to_torch(d[f"{name}_kernel"], True)
+    normal = to_torch(d[f"{name}_normal"], True)
+    for dtype, tol in ((torch.float32, 2e-6), (torch.float64, 1e-5)):
+        K = ON.toeplitz_kernel(locs, shape, weight=w, dtype=dtype)
+        assert rel_l2(K, kern) < tol
+        assert rel_l2(ON.toeplitz_normal(x, K, shape), normal) < tol

@@ -20,6 +20,8 @@ re-pointing its functional calls (see the integration notes of this repo).
   (pad, ifftshift / fftshift, crop, apodization and coil maps in one pass)
 * ``Diagonal``, ``Scalar``, ``Pad``, ``FFT`` <- linops/{diagonal,scalar,pad_last,fft}.py
 * ``nufft`` / ``nufft_adjoint`` <- functional/_nufft.py:16-112
+* ``ToeplitzNormal``, ``toeplitz_psf`` <- linops/nufft.py:226-239, 395-568
+  (``NUFFT(..., toeplitz=True).normal(inner)``)
 """
 
 from __future__ import annotations
@@ -52,6 +54,8 @@ __all__ = [
     "ArrayToBlocks",
     "BlocksToArray",
     "NUFFT",
+    "ToeplitzNormal",
+    "toeplitz_psf",
     "nufft",
     "nufft_adjoint",
     "cfftn",
@@ -626,6 +630,7 @@ class NUFFT(Chain):
         scale_factor = width**ndim * (prod(grid_size) / prod(padded_size)) ** 0.5
         scale = Scalar(torch.tensor(1.0 / scale_factor, device=device))
         super().__init__(padshift, fft, interp, scale, name="NUFFT")
+        self.options = options
         self.apodize_weight = weight
         self.scale_factor = scale_factor
         self.padded_size = padded_size
@@ -637,6 +642,111 @@ class NUFFT(Chain):
         self.pad = padshift
         self.fft = fft
         self.interp = interp
+
+    def normal(self, inner: Optional[NamedLinop] = None) -> NamedLinop:
+        """With the ``toeplitz`` option, the Toeplitz embedding of
+        ``self.H @ inner @ self`` (nufft.py:226-239) for ``inner`` None or a
+        diagonal weighting of the points; otherwise (and for other ``inner``
+        operators) the chain itself, forward then adjoint."""
+        if self.options.get("toeplitz", False):
+            weight = _point_weight(inner, self.locs_prepared.shape[:-1])
+            if weight is not False:
+                return ToeplitzNormal(self, weight, self.options.get("toeplitz_oversamp", 2.0),
+                                      self.options.get("toeplitz_dtype"))
+        return super().normal(inner)
+
+
+def scale_int(t, scale_factor: float) -> tuple[int, ...]:
+    return tuple(int(scale_factor * s) for s in t)
+
+
+def rescale_locs(locs: Tensor, c0, w0, c1, w1) -> Tensor:
+    """(loc - c0) * w1 / w0 + c1 per coordinate, with the reference's float
+    operations in the locations' dtype (nufft.py:538-568)."""
+    return torch.stack([(locs[..., d] - c0[d]) * w1[d] / w0[d] + c1[d] for d in range(locs.shape[-1])], dim=-1)
+
+
+def _point_weight(inner: Optional[NamedLinop], points_shape):
+    """The per-point weight of a diagonal ``inner`` (None for no inner), or
+    False when ``inner`` is not a weighting of the points alone."""
+    if inner is None:
+        return None
+    if isinstance(inner, Diagonal):
+        w = inner.weight.detach()
+        try:
+            if torch.broadcast_shapes(w.shape, tuple(points_shape)) == tuple(points_shape):
+                return w
+        except RuntimeError:
+            pass
+    return False
+
+
+@torch.no_grad()
+def toeplitz_psf(nufft: NUFFT, weight: Optional[Tensor] = None, oversamp: float = 2.0,
+                 dtype: Optional[torch.dtype] = None) -> Tensor:
+    """The Toeplitz kernel of ``nufft.H @ diag(weight) @ nufft``: centred
+    k-space on the ``oversamp`` x grid (nufft.py:395-494, the weight of its
+    ``Dense``). It is the adjoint NUFFT of the weights (ones by default) on
+    the larger grid, whose points are the prepared points rescaled from the
+    padded grid Np to ``int(oversamp * Np)`` cells, through an unnormalised
+    centred FFT, times ``oversamp^D / sqrt(prod(grid))``. As in the
+    reference, the larger NUFFT pads its grid to ``int(1.25 * int(oversamp *
+    N))`` cells, one more than the points' range when ``1.25 * N`` has a
+    fractional part of at least 1/2."""
+    dtype = torch.complex64 if dtype is None else dtype
+    if dtype != torch.complex64:
+        raise TypeError(f"Toeplitz kernels are complex64, got {dtype}")
+    grid_size = nufft.grid_size
+    ndim = len(grid_size)
+    new_grid = scale_int(grid_size, oversamp)
+    width = nufft.padded_size
+    new_width = scale_int(width, oversamp)
+    new_locs = rescale_locs(nufft.locs_prepared.detach(), tuple(w // 2 for w in width), width,
+                            tuple(w // 2 for w in new_width), new_width)
+    big = NUFFT(new_locs, new_grid, oversamp=nufft.oversamp, width=nufft.width, do_prep_locs=False)
+    points = tuple(new_locs.shape[:-1])
+    if weight is None:
+        w = torch.ones(points, dtype=dtype, device=new_locs.device)
+    else:
+        w = torch.broadcast_to(weight.to(device=new_locs.device, dtype=dtype), points).contiguous()
+    otf = big.H(w)
+    dim = tuple(range(-ndim, 0))
+    return cfftn(otf, dim=dim, norm=None) * (oversamp**ndim / prod(new_grid) ** 0.5)
+
+
+class ToeplitzNormal(NamedLinop):
+    """``nufft.H @ diag(weight) @ nufft`` by Toeplitz embedding
+    (nufft.py:226-239): zero pad to the ``oversamp`` x grid, orthonormal
+    centred FFT, multiply by the PSF kernel, inverse FFT, crop. Here the pad
+    and ifftshift are one gather (``pad_shift``), the FFTs are uncentred
+    cuFFT, the kernel is held in uncentred order, and fftshift and crop are
+    one gather (``crop_shift``): no shift pass runs. Leading batch dims share
+    the kernel."""
+
+    def __init__(self, nufft: NUFFT, weight: Optional[Tensor] = None, oversamp: float = 2.0,
+                 dtype: Optional[torch.dtype] = None):
+        super().__init__()
+        self.kernel = toeplitz_psf(nufft, weight, oversamp, dtype)
+        ndim = len(nufft.grid_size)
+        self.dim = tuple(range(-ndim, 0))
+        self.im_size = tuple(nufft.grid_size)
+        self.pad_im_size = scale_int(nufft.grid_size, oversamp)
+        self.kernel_uncentred = torch.fft.ifftshift(self.kernel, dim=self.dim).contiguous()
+
+    @staticmethod
+    def _apply(t, x, k):
+        z = pad_shift(x, t.im_size, t.pad_im_size)
+        z = torch.fft.fftn(z, dim=t.dim, norm="ortho")
+        z = torch.fft.ifftn(z * k, dim=t.dim, norm="ortho")
+        return crop_shift(z, t.im_size, t.pad_im_size)
+
+    @staticmethod
+    def fn(t, x, /):
+        return ToeplitzNormal._apply(t, x, t.kernel_uncentred)
+
+    @staticmethod
+    def adj_fn(t, x, /):
+        return ToeplitzNormal._apply(t, x, t.kernel_uncentred.conj())
 
 
 _APOD: "OrderedDict[tuple, Tensor]" = OrderedDict()
