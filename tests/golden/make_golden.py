@@ -7,9 +7,13 @@ Run in a container that has the reference source:
 It imports the reference's functional API with a no-op ``jaxtyping`` stub
 (``tests/golden/_stubs``) and runs its pure-torch CPU path (``ungrid_torch``,
 ``grid_torch``, ``_unfold_torch``, ``_fold_torch``, ``kaiser_bessel_torch``)
-on small seeded inputs, writing ``tests/golden/*.npz``. The fixtures are the
-parity pins for the oracle (``tests/test_oracle_golden.py``) and, on the GPU,
-for the CUDA kernels (``tests/test_interp_gpu.py``, ``tests/test_blocks_gpu.py``).
+on small seeded inputs, writing ``tests/golden/*.npz``. ``toeplitz.npz`` comes
+from its linops: ``NUFFT(..., toeplitz=True).normal(inner)`` and
+``toeplitz_psf`` (``--only toeplitz`` rewrites just that file). The fixtures
+are the parity pins for the oracle (``tests/test_oracle_golden.py``) and, on
+the GPU, for the CUDA kernels (``tests/test_interp_gpu.py``,
+``tests/test_blocks_gpu.py``, ``tests/test_linops_gpu.py``,
+``tests/test_toeplitz_gpu.py``).
 """
 
 from __future__ import annotations

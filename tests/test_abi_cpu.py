@@ -1,5 +1,8 @@
-"""C-ABI library checks that need no GPU: it loads, exports every symbol that
-include/tlgb.h declares, and validates descriptors on the host."""
+"""Checks that need no GPU: the C-ABI library loads, exports every symbol
+that include/tlgb.h declares with the declared parameters, and validates
+descriptors and launch sizes on the host; the Python layer's host-side logic
+(location rescaling with the reference's rounding, batch ranges, the
+Toeplitz normal's inner operators) runs as the reference's does."""
 
 import ctypes
 import os
@@ -195,3 +198,38 @@ def test_batch_ranges():
     assert I._batch_chunks(5) == [(0, 5)]
     assert I._batch_chunks(M) == [(0, M)]
     assert I._batch_chunks(2 * M + 3) == [(0, M), (M, 2 * M), (2 * M, 2 * M + 3)]
+
+
+@pytest.mark.parametrize("gs", [(16, 16), (12, 14), (205, 205, 205), (33,)])
+def test_toeplitz_rescaling_keeps_the_reference_rounding(gs):
+    """The Toeplitz kernel's point rescaling (host-side torch ops): from the
+    padded grid Np to int(2 Np) cells, (loc - Np//2) * 2Np / Np + 2Np//2 per
+    coordinate in float32 (linops/nufft.py:538-568), and the 2x sizes
+    (scale_int, nufft.py:497-498)."""
+    from torchlinops_gb300 import linops
+
+    ps = tuple(int(1.25 * s) for s in gs)
+    g = torch.Generator().manual_seed(sum(gs))
+    locs = torch.rand(20000, len(gs), generator=g) * torch.tensor(ps, dtype=torch.float32)
+    nw = linops.scale_int(ps, 2.0)
+    assert nw == tuple(int(2.0 * p) for p in ps)
+    ref = torch.stack([(locs[:, d] - ps[d] // 2) * nw[d] / ps[d] + nw[d] // 2 for d in range(len(gs))], dim=-1)
+    got = linops.rescale_locs(locs, tuple(p // 2 for p in ps), ps, tuple(w // 2 for w in nw), nw)
+    assert got.dtype == torch.float32 and torch.equal(got, ref)
+
+
+def test_toeplitz_inner_operators():
+    """NUFFT.normal(inner) embeds for no inner or a diagonal weighting of the
+    points (a weight that broadcasts to the points' shape); other inner
+    operators take the explicit chain."""
+    from torchlinops_gb300 import linops
+
+    pts = (40, 3)
+    assert linops._point_weight(None, pts) is None
+    w = torch.rand(40, 3)
+    assert linops._point_weight(linops.Diagonal(w), pts) is not False
+    assert linops._point_weight(linops.Diagonal(torch.rand(3)), pts) is not False
+    assert linops._point_weight(linops.Scalar(2.0), pts) is not False
+    assert linops._point_weight(linops.Diagonal(torch.rand(8, 40, 3)), pts) is False  # per-coil weights
+    assert linops._point_weight(linops.Diagonal(torch.rand(7)), pts) is False
+    assert linops._point_weight(linops.Pad((8, 8), (4, 4)), pts) is False
