@@ -233,3 +233,32 @@ def test_toeplitz_inner_operators():
     assert linops._point_weight(linops.Diagonal(torch.rand(8, 40, 3)), pts) is False  # per-coil weights
     assert linops._point_weight(linops.Diagonal(torch.rand(7)), pts) is False
     assert linops._point_weight(linops.Pad((8, 8), (4, 4)), pts) is False
+
+
+def test_cached_entries_go_with_their_locations():
+    """Plan and prepared-location caches drop an entry when its locations
+    tensor is freed (plans hold device memory), keep a newer entry under the
+    same key, and evict the oldest beyond their size."""
+    import gc
+    from collections import OrderedDict
+
+    from torchlinops_gb300 import interp as I
+
+    cache = OrderedDict()
+    a, b = torch.zeros(3), torch.zeros(4)
+    I.remember(cache, ("a",), a, "plan a", 2)
+    I.remember(cache, ("b",), b, "plan b", 2)
+    assert list(cache) == [("a",), ("b",)]
+    del a
+    gc.collect()
+    assert list(cache) == [("b",)]
+    c = torch.zeros(5)
+    I.remember(cache, ("b",), c, "plan c", 2)
+    del b
+    gc.collect()
+    assert cache[("b",)][2] == "plan c"
+    d, e = torch.zeros(1), torch.zeros(1)
+    I.remember(cache, ("d",), d, "plan d", 2)
+    I.remember(cache, ("e",), e, "plan e", 2)
+    assert list(cache) == [("d",), ("e",)]
+    assert cache[("e",)][0]() is e and cache[("e",)][1] == e._version

@@ -145,6 +145,22 @@ def clear_plan_cache() -> None:
     _PLAN_CACHE.clear()
 
 
+def remember(cache: "OrderedDict[tuple, tuple]", key: tuple, locs: Tensor, value, size: int) -> None:
+    """cache[key] = (weak reference to locs, locs' version, value), most
+    recent last. The entry is dropped when locs is freed (a plan holds device
+    memory that a dead trajectory could never use again) and the oldest
+    entries beyond ``size`` are evicted."""
+
+    def drop(ref, cache=cache, key=key):
+        hit = cache.get(key)
+        if hit is not None and hit[0] is ref:
+            del cache[key]
+
+    cache[key] = (weakref.ref(locs, drop), locs._version, value)
+    while len(cache) > size:
+        cache.popitem(last=False)
+
+
 def get_plan(locs: Tensor, grid_size, width, kernel: str, pad_mode: str, beta: float = 1.0,
              norm: int = 1) -> InterpolatePlan:
     """Cached plan for ``locs``: rebuilt when ``locs`` changes in place."""
@@ -169,9 +185,7 @@ def get_plan(locs: Tensor, grid_size, width, kernel: str, pad_mode: str, beta: f
             return plan
         del _PLAN_CACHE[key]
     plan = InterpolatePlan(locs, grid_size, width, kernel, pad_mode, beta, norm)
-    _PLAN_CACHE[key] = (weakref.ref(locs), locs._version, plan)
-    while len(_PLAN_CACHE) > _PLAN_CACHE_SIZE:
-        _PLAN_CACHE.popitem(last=False)
+    remember(_PLAN_CACHE, key, locs, plan, _PLAN_CACHE_SIZE)
     return plan
 
 

@@ -28,7 +28,6 @@ from __future__ import annotations
 
 import ctypes
 import math
-import weakref
 from collections import OrderedDict
 from copy import copy
 from math import prod
@@ -788,9 +787,7 @@ def _prepared_locs(locs: Tensor, grid_size, padded) -> Tensor:
             return out
         del _PREPARED_LOCS[key]
     out = prep_locs(locs.detach(), grid_size, padded)
-    _PREPARED_LOCS[key] = (weakref.ref(locs), locs._version, out)
-    while len(_PREPARED_LOCS) > 16:
-        _PREPARED_LOCS.popitem(last=False)
+    I.remember(_PREPARED_LOCS, key, locs, out, 16)
     return out
 
 
