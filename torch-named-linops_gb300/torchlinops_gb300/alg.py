@@ -45,10 +45,13 @@ _SCRATCH: dict = {}
 
 
 def _scratch(dev: torch.device) -> Tensor:
-    s = _SCRATCH.get(dev)
+    """The float64 reductions' partial sums, one buffer per (device, stream):
+    reductions issued on different streams may run at the same time."""
+    key = (dev, torch.cuda.current_stream(dev).cuda_stream)
+    s = _SCRATCH.get(key)
     if s is None:
         s = torch.empty(int(_ext.lib().tlgb_cg_scratch_bytes()), dtype=torch.uint8, device=dev)
-        _SCRATCH[dev] = s
+        _SCRATCH[key] = s
     return s
 
 
