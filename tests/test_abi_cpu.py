@@ -262,3 +262,40 @@ def test_cached_entries_go_with_their_locations():
     I.remember(cache, ("e",), e, "plan e", 2)
     assert list(cache) == [("d",), ("e",)]
     assert cache[("e",)][0]() is e and cache[("e",)][1] == e._version
+
+
+def test_cached_plans_order_other_streams_after_their_build(monkeypatch):
+    """A cached plan used from another stream makes that stream wait for the
+    build's event and records the stream on the plan's buffer; the build
+    stream itself and captured streams add nothing."""
+    from torchlinops_gb300 import interp as I
+
+    calls = []
+
+    class Stream:
+        def __init__(self, handle):
+            self.cuda_stream = handle
+
+        def wait_event(self, event):
+            calls.append(("wait", self.cuda_stream, event))
+
+    class Buffer:
+        def record_stream(self, stream):
+            calls.append(("keep", stream.cuda_stream))
+
+    plan = I.InterpolatePlan.__new__(I.InterpolatePlan)
+    plan.device, plan.stream, plan.ready, plan.buffer = "cuda:0", Stream(1), "built", Buffer()
+    cur, capturing = [Stream(1)], [False]
+    monkeypatch.setattr(torch.cuda, "current_stream", lambda device=None: cur[0])
+    monkeypatch.setattr(torch.cuda, "is_current_stream_capturing", lambda: capturing[0])
+    plan.use_on_current_stream()
+    assert calls == []
+    cur[0] = Stream(2)
+    plan.use_on_current_stream()
+    assert calls == [("wait", 2, "built"), ("keep", 2)]
+    capturing[0] = True
+    plan.use_on_current_stream()
+    assert len(calls) == 2
+    # the torch calls the method makes
+    assert all(hasattr(torch.cuda.Stream, m) for m in ("wait_event", "cuda_stream"))
+    assert hasattr(torch.Tensor, "record_stream") and hasattr(torch.cuda.Event, "record")

@@ -130,7 +130,22 @@ class InterpolatePlan:
                 ),
                 "interpolation plan",
             )
+            # the build's last kernels are still in flight on this stream
+            self.stream = torch.cuda.current_stream(dev)
+            self.ready = torch.cuda.Event()
+            self.ready.record(self.stream)
         del tmp
+
+    def use_on_current_stream(self) -> None:
+        """Plans are cached across streams: another stream waits for the
+        build (no host synchronisation) and keeps the plan's memory from
+        being reused while its own work may still read it. Under stream
+        capture nothing is added (plans are built before capture: a build
+        synchronises its stream)."""
+        cur = torch.cuda.current_stream(self.device)
+        if cur.cuda_stream != self.stream.cuda_stream and not torch.cuda.is_current_stream_capturing():
+            cur.wait_event(self.ready)
+            self.buffer.record_stream(cur)
 
     @property
     def n_entries(self) -> int:
@@ -182,6 +197,7 @@ def get_plan(locs: Tensor, grid_size, width, kernel: str, pad_mode: str, beta: f
         ref, version, plan = hit
         if ref() is locs and version == locs._version:
             _PLAN_CACHE.move_to_end(key)
+            plan.use_on_current_stream()
             return plan
         del _PLAN_CACHE[key]
     plan = InterpolatePlan(locs, grid_size, width, kernel, pad_mode, beta, norm)
