@@ -1,11 +1,21 @@
-"""The oracle's own CPU checks that no golden fixture covers: the float64 CG
-and the bin-permutation restatement (structure and invariants)."""
+"""The oracle's own CPU checks that no golden fixture covers: the float64 CG,
+the bin-permutation restatement (structure and invariants), and FP64
+identities of the interpolation, block and NUFFT restatements (adjoint
+pairs, linearity, the Toeplitz normal against the explicit normal)."""
 
 import numpy as np
+import pytest
 import torch
 
 from oracle import binning as OB
+from oracle import blocks as OBL
 from oracle import cg as OCG
+from oracle import interp as OI
+from oracle import nufft as ON
+
+
+def _vdot(a, b):
+    return complex(torch.vdot(a.flatten().to(torch.complex128), b.flatten().to(torch.complex128)))
 
 
 def test_float64_cg_solves_spd():
@@ -31,3 +41,72 @@ def test_binning_invariants():
     # a W=4 window spans at most 2 tiles of 8 per axis: at most 8 pairs per point
     assert np.bincount(pts).max() <= 8
     assert 2.0 < len(keys) / 3000 < 4.0
+
+
+@pytest.mark.parametrize("shape", [(37,), (19, 23), (9, 10, 11)])
+@pytest.mark.parametrize("kernel,norm", [("kaiser_bessel", 1), ("spline", 1), ("kaiser_bessel", 2)])
+@pytest.mark.parametrize("pad", ["circular", "zero"])
+def test_interp_oracle_adjoint_pair(shape, kernel, norm, pad):
+    """<ungrid(x), y> = <x, grid(y)> in FP64, points anywhere including the
+    edges (wrapped or cut) and exact-integer coordinates."""
+    gen = torch.Generator().manual_seed(len(shape) * 10 + norm)
+    nd = len(shape)
+    locs = torch.rand(200, nd, generator=gen, dtype=torch.float64) * torch.tensor(shape, dtype=torch.float64)
+    locs[:10] = torch.floor(locs[:10])
+    x = torch.randn(2, *shape, dtype=torch.complex128, generator=gen)
+    y = torch.randn(2, 200, dtype=torch.complex128, generator=gen)
+    beta = OI.nufft_beta(4.0, 1.25)
+    fx = OI.ungrid(x, locs, 4.0, kernel, norm, pad, beta, dtype=torch.float64)
+    gy = OI.grid(y, locs, shape, 4.0, kernel, norm, pad, beta, dtype=torch.float64)
+    lhs, rhs = _vdot(fx, y), _vdot(x, gy)
+    assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
+
+
+@pytest.mark.parametrize("shape,block,stride", [((15, 14), (3, 4), (2, 3)), ((10, 9, 8), (4, 3, 2), (2, 2, 2)), ((20,), (5,), (5,))])
+def test_blocks_oracle_adjoint_pair_and_masking(shape, block, stride):
+    """<unfold(x), y> = <x, fold(y)> exactly in FP64 (sums of products), with
+    and without a mask; the mask keeps exactly its entries."""
+    gen = torch.Generator().manual_seed(sum(shape))
+    x = torch.randn(3, *shape, dtype=torch.float64, generator=gen)
+    u = OBL.unfold(x, block, stride)
+    y = torch.randn(u.shape, dtype=torch.float64, generator=gen)
+    assert abs(float((u * y).sum() - (x * OBL.fold(y, shape, block, stride)).sum())) < 1e-10
+    mask = torch.rand(block, generator=gen) > 0.4
+    um = OBL.unfold(x, block, stride, mask)
+    assert torch.equal(um, u[..., mask])
+    ym = torch.randn(um.shape, dtype=torch.float64, generator=gen)
+    assert abs(float((um * ym).sum() - (x * OBL.fold(ym, shape, block, stride, mask)).sum())) < 1e-10
+
+
+@pytest.mark.parametrize("shape", [(16, 16), (12, 14), (8, 8, 8)])
+def test_nufft_oracle_adjoint_pair(shape):
+    gen = torch.Generator().manual_seed(len(shape) + shape[-1])
+    locs = (torch.rand(120, len(shape), generator=gen, dtype=torch.float64) - 0.5) * torch.tensor(shape,
+                                                                                                  dtype=torch.float64)
+    x = torch.randn(*shape, dtype=torch.complex128, generator=gen)
+    y = torch.randn(120, dtype=torch.complex128, generator=gen)
+    lhs = _vdot(ON.nufft(x, locs), y)
+    rhs = _vdot(x, ON.nufft_adjoint(y, locs, shape))
+    assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
+
+
+def test_toeplitz_oracle_against_the_explicit_normal():
+    """At sizes where 1.25 N is a whole number of cells the Toeplitz normal is
+    the explicit nufft_adjoint(nufft(x)) up to the interpolation error of
+    both (about 1%); linear in x; a point weighting w gives the explicit
+    nufft_adjoint(w * nufft(x)) to the same accuracy."""
+    gen = torch.Generator().manual_seed(5)
+    shape = (16, 16)
+    locs = (torch.rand(300, 2, generator=gen, dtype=torch.float64) - 0.5) * 16
+    x = torch.randn(*shape, dtype=torch.complex128, generator=gen)
+    z = torch.randn(*shape, dtype=torch.complex128, generator=gen)
+    K = ON.toeplitz_kernel(locs, shape)
+    t = ON.toeplitz_normal(x, K, shape)
+    e = ON.nufft_adjoint(ON.nufft(x, locs), locs, shape)
+    assert float((t - e).norm() / e.norm()) < 0.03
+    lin = ON.toeplitz_normal(2 * x - 3j * z, K, shape)
+    assert torch.allclose(lin, 2 * t - 3j * ON.toeplitz_normal(z, K, shape), rtol=1e-12, atol=1e-12)
+    w = torch.rand(300, generator=gen, dtype=torch.float64) + 0.5
+    tw = ON.toeplitz_normal(x, ON.toeplitz_kernel(locs, shape, weight=w), shape)
+    ew = ON.nufft_adjoint(w * ON.nufft(x, locs), locs, shape)
+    assert float((tw - ew).norm() / ew.norm()) < 0.03
