@@ -5,7 +5,8 @@
  * throws; tlgb_last_error() gives the message of the last failing call made
  * on the calling host thread. All device pointers are raw CUDA device memory;
  * every launch goes on the given stream and no call synchronises the device,
- * except tlgb_interp_plan_build (it reads the bin histogram back once).
+ * except tlgb_interp_plan_build (it reads the bin histogram back once) and
+ * tlgb_index_plan_build (it reads its bounds check back once).
  *
  * Reference interfaces each entry replaces (paths in the torchlinops source):
  *   tlgb_interp_forward    -> ungrid / _ungrid, functional/_interp/ungrid.py:37,70
@@ -18,6 +19,8 @@
  *                             functional/_interp/ungrid.py:135-160
  *   tlgb_unfold            -> unfold / _unfold, functional/_unfold/unfold.py:31,72
  *   tlgb_fold              -> fold / _fold,     functional/_unfold/fold.py:32,66
+ *   tlgb_index_forward     -> index,            functional/_index/index.py:17
+ *   tlgb_index_adjoint     -> index_adjoint,    functional/_index/index.py:75
  */
 #ifndef TLGB_H_
 #define TLGB_H_
@@ -151,9 +154,13 @@ int tlgb_interp_adjoint(const tlgb_interp_desc* d, const tlgb_interp_plan_info* 
  *    with TLGB_ERR_WORKSPACE before anything is launched. The point-major
  *    copy of the values is made only when it fits beside them; otherwise
  *    the values are read in place (same result, bit for bit).
- *  - The first call on a device looks up the buffer's device address (with
- *    that device current) and remembers it; make that first call before any
- *    stream capture.
+ *  - The first call in each CUDA context (the primary context of a device,
+ *    or a context the caller created with the driver API) looks up the
+ *    buffer's device address in that context and remembers it. Under CUDA's
+ *    lazy module loading that first lookup may also load the module, which
+ *    is when the 32 MiB buffer is allocated on the GPU: make the first call
+ *    at start-up, before reserving the rest of the device memory, and before
+ *    any stream capture.
  *  - Every call shares the one buffer and it keeps the last call's contents;
  *    nothing in it has to start at zero, because every partial tile is
  *    written in full before it is read. Calls whose work overlaps on the GPU
@@ -183,8 +190,19 @@ int tlgb_interp_grad_locs(const tlgb_interp_desc* d, const tlgb_interp_plan_info
 /* ArrayToBlocks / BlocksToArray (unfold / fold), 1D-3D.                      */
 /* ------------------------------------------------------------------------ */
 
-/* Element types of the block ops. Complex types are pairs of the real type. */
-enum { TLGB_F32 = 0, TLGB_F64 = 1, TLGB_C64 = 2, TLGB_C128 = 3 };
+/* Element types of the block and sampling ops. Complex types are pairs of
+ * the real type. The integer and raw types are for the sampling ops only
+ * (raw: 1- or 2-byte elements that tlgb_index_forward copies unchanged). */
+enum {
+  TLGB_F32 = 0,
+  TLGB_F64 = 1,
+  TLGB_C64 = 2,
+  TLGB_C128 = 3,
+  TLGB_I32 = 4,
+  TLGB_I64 = 5,
+  TLGB_RAW8 = 6,
+  TLGB_RAW16 = 7
+};
 
 /* array [nbatch, im_size...]  <->  blocks [nbatch, nblocks..., block...]
  * or, with a mask, blocks [nbatch, nblocks..., nnz] where mask_idx[j] (int32,
@@ -214,6 +232,54 @@ int tlgb_unfold(const tlgb_blocks_desc* d, const void* array, void* blocks, tlgb
  * prod(ceil(block/stride))) block entries in ascending block order, starting
  * from zero -- deterministic; every element of `array` is written. */
 int tlgb_fold(const tlgb_blocks_desc* d, const void* blocks, void* array, tlgb_stream_t stream);
+
+/* ------------------------------------------------------------------------ */
+/* Sampling at integer locations (Sampling linop; NUFFT mode "sampling").      */
+/* Replaces index / index_adjoint, functional/_index/index.py:17,75, whose    */
+/* adjoint is index_add_ (multi_grid, :141-184): float atomics on a GPU.       */
+/* ------------------------------------------------------------------------ */
+
+#define TLGB_INDEX_MAX_DIM 8
+
+/* vals [nbatch, grid_size...] <-> samples [nbatch, npts]; the sample m sits
+ * at cell (idx[0][m], ..., idx[ndim-1][m]) of the grid, each index taken
+ * modulo its size (Python's non-negative modulo, so -size <= idx < size).
+ * Below 2^31 cells and 2^31 - 1 samples. */
+typedef struct tlgb_index_desc {
+  int32_t ndim;  /* indexed (trailing) dims, 1..TLGB_INDEX_MAX_DIM */
+  int32_t dtype; /* TLGB_F32 ... TLGB_RAW16 */
+  int64_t nbatch;
+  int64_t grid_size[TLGB_INDEX_MAX_DIM];
+  int64_t npts;
+} tlgb_index_desc;
+
+typedef struct tlgb_index_plan_info {
+  int64_t ncells, npts;
+  int64_t off_flat;  /* byte offsets of the plan sections: the cell of each sample, */
+  int64_t off_perm;  /* the samples sorted by cell (ascending within a cell),       */
+  int64_t off_cells; /* and the first sorted position of every cell (ncells + 1)   */
+  int64_t plan_bytes;
+} tlgb_index_plan_info;
+
+int tlgb_index_plan_size(const tlgb_index_desc* d, size_t* plan_bytes, size_t* tmp_bytes);
+
+/* idx: [ndim][npts] int64 device indices. Ravels them, sorts the samples by
+ * cell (stable) and sizes each cell's run. Synchronises `stream` once; an
+ * index outside [-size, size) returns TLGB_ERR_INVALID with the first such
+ * dimension in the message (the reference raises IndexError). */
+int tlgb_index_plan_build(const tlgb_index_desc* d, const int64_t* idx, void* plan, size_t plan_bytes, void* tmp,
+                          size_t tmp_bytes, tlgb_index_plan_info* info, tlgb_stream_t stream);
+
+/* out[b, m] = vals[b, cell(m)]: a copy (any element type). */
+int tlgb_index_forward(const tlgb_index_desc* d, const tlgb_index_plan_info* info, const void* plan,
+                       const void* vals, void* out, tlgb_stream_t stream);
+
+/* out[b, c] = sum of vals[b, m] over the samples m of cell c, in ascending m,
+ * starting from zero: the order of a sequential index_add_, so bit-identical
+ * to it and run to run (no atomics). Every cell is written. Float, complex
+ * and integer element types. */
+int tlgb_index_adjoint(const tlgb_index_desc* d, const tlgb_index_plan_info* info, const void* plan,
+                       const void* vals, void* out, tlgb_stream_t stream);
 
 /* ------------------------------------------------------------------------ */
 /* Conjugate gradients with float64 scalars.                                   */

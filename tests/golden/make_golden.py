@@ -2,7 +2,9 @@
 
 Run in a container that has the reference source:
 
-    python tests/golden/make_golden.py --ref /root/reference/src
+    python tests/golden/make_golden.py --ref <torch-named-linops checkout>/src
+
+(or set ``TORCHLINOPS_SRC`` to that directory instead of passing ``--ref``).
 
 It imports the reference's functional API with a no-op ``jaxtyping`` stub
 (``tests/golden/_stubs``) and runs its pure-torch CPU path (``ungrid_torch``,
@@ -275,6 +277,49 @@ def make_blocks(F, out_dir):
     return len(cases)
 
 
+def make_index(F, out_dir):
+    """Sampling ops: the reference's known answer (_index/tests/test_index.py:26-34),
+    collisions in 1D/2D/3D with negative indices, real, complex and integer
+    values, a broadcast index and a sliced index for the gather."""
+    cases = {}
+    gen = torch.Generator().manual_seed(2024)
+
+    def rnd_idx(shape, size):
+        return torch.randint(-size, size, shape, generator=gen)
+
+    def add(name, vals, idx, grid, fwd_vals=None):
+        rec = dict(vals=_np(vals), out=_np(F.index_adjoint(vals, idx, grid)))
+        for d, i in enumerate(idx):
+            rec[f"idx{d}"] = i.numpy()
+        if fwd_vals is not None:
+            rec["grid_vals"] = _np(fwd_vals)
+            rec["fwd"] = _np(F.index(fwd_vals, idx))
+        rec["meta"] = json.dumps(dict(grid=list(grid), ndim=len(idx), dtype=str(vals.dtype)))
+        cases[name] = rec
+
+    add("known1d", torch.tensor([[5.0, 4.0, -1.0], [5.0, 4.0, -1.0]]), (torch.tensor([1, 3, 2]),), (4,))
+    i1 = (rnd_idx((2000,), 37),)
+    add("collide1d_f32", torch.randn(3, 2000, generator=gen), i1, (37,), torch.randn(3, 37, generator=gen))
+    add("collide1d_i64", torch.randint(-50, 50, (2, 2000), generator=gen), i1, (37,))
+    i2 = (rnd_idx((50, 40), 23), rnd_idx((50, 40), 31))
+    v2 = torch.complex(torch.randn(2, 4, 50, 40, generator=gen), torch.randn(2, 4, 50, 40, generator=gen))
+    g2 = torch.complex(torch.randn(2, 4, 23, 31, generator=gen), torch.randn(2, 4, 23, 31, generator=gen))
+    add("collide2d_c64", v2, i2, (23, 31), g2)
+    i3 = (rnd_idx((5000,), 9), rnd_idx((5000,), 11), rnd_idx((5000,), 13))
+    add("collide3d_f64", torch.randn(2, 5000, generator=gen, dtype=torch.float64), i3, (9, 11, 13),
+        torch.randn(2, 9, 11, 13, generator=gen, dtype=torch.float64))
+    # gathers only: a broadcast index and a sliced one
+    gv = torch.randn(3, 7, 5, generator=gen)
+    ib = (torch.tensor([1, 0, 6, -2])[:, None], torch.tensor([4, 2, 0])[None, :])
+    cases["bcast_fwd"] = dict(grid_vals=_np(gv), idx0=ib[0].numpy(), idx1=ib[1].numpy(), fwd=_np(F.index(gv, ib)),
+                              meta=json.dumps(dict(grid=[7, 5], ndim=2, dtype="torch.float32")))
+    gs = torch.arange(8).reshape(2, 4)
+    cases["slice_fwd"] = dict(grid_vals=gs.numpy(), fwd=F.index(gs, (slice(None), slice(1, 4))).numpy(),
+                              meta=json.dumps(dict(grid=[2, 4], ndim=2, dtype="torch.int64", slices=[[None, None], [1, 4]])))
+    np.savez_compressed(os.path.join(out_dir, "index_cases.npz"), **_flatten(cases))
+    return len(cases)
+
+
 def _flatten(cases):
     flat = {}
     for k, rec in cases.items():
@@ -285,10 +330,13 @@ def _flatten(cases):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference/src")
+    ap.add_argument("--ref", default=os.environ.get("TORCHLINOPS_SRC"),
+                    help="the reference's src/ directory (default: $TORCHLINOPS_SRC)")
     ap.add_argument("--out", default=HERE)
-    ap.add_argument("--only", choices=["toeplitz"], default=None, help="write only this fixture")
+    ap.add_argument("--only", choices=["toeplitz", "index"], default=None, help="write only this fixture")
     args = ap.parse_args()
+    if not args.ref:
+        ap.error("give the reference's src/ directory with --ref or TORCHLINOPS_SRC")
     sys.path.insert(0, os.path.join(HERE, "_stubs"))
     sys.path.insert(0, args.ref)
     torch.set_num_threads(os.cpu_count() or 1)
@@ -301,6 +349,10 @@ def main():
         make_toeplitz(L, args.out)
         print(f"wrote toeplitz.npz in {time.time() - t0:.1f}s")
         return
+    if args.only == "index":
+        n = make_index(F, args.out)
+        print(f"wrote {n} index cases in {time.time() - t0:.1f}s")
+        return
     make_kernels(K, args.out)
     make_edgecases(F, args.out)
     make_config1(F, args.out)
@@ -308,7 +360,8 @@ def main():
     make_toeplitz(L, args.out)
     n_i = make_interp(F, args.out)
     n_b = make_blocks(F, args.out)
-    print(f"wrote {n_i} interp cases, {n_b} block cases in {time.time() - t0:.1f}s")
+    n_x = make_index(F, args.out)
+    print(f"wrote {n_i} interp cases, {n_b} block cases, {n_x} index cases in {time.time() - t0:.1f}s")
 
 
 if __name__ == "__main__":

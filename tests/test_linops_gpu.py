@@ -120,6 +120,33 @@ def test_cg_on_nufft_normal_equations():
     assert info2.converged and info2.true_rel_residual < 2e-4
 
 
+@pytest.mark.parametrize("learned", [False, True])
+def test_cg_true_residual_decides_convergence(learned):
+    """A solve whose recursive residual reaches rtol while its true residual
+    does not is not converged: it continues as plain CG from its iterate. The
+    operator here changes after the iterations of the first solve (as an
+    operator whose rounding drifts would), so the recursive residual belongs
+    to a different system than the final check."""
+    gen = torch.Generator().manual_seed(9)
+    n = 512
+    d1 = (torch.rand(n, generator=gen) * 9 + 1).to(DEV)
+    d2 = d1 * (1 + 0.01 * torch.randn(n, generator=gen).to(DEV))
+    b = torch.randn(n, dtype=torch.complex64, generator=gen).to(DEV)
+    M = (lambda r: (r / d1).to(r.dtype)) if learned else None
+    _, first = alg.cg_solve(lambda v: d1 * v, b, rtol=1e-4, max_iters=200, M=M)
+    assert first.converged and first.restarts == 0
+    calls = [0]
+
+    def A(v):  # d1 for the iterations of the first solve, d2 from the final check on
+        calls[0] += 1
+        return (d1 if calls[0] <= first.iters else d2) * v
+
+    x, info = alg.cg_solve(A, b, rtol=1e-4, max_iters=200, M=M)
+    assert info.restarts >= 1
+    assert info.converged and info.true_rel_residual <= 1e-4
+    assert float(alg.norm64((b - d2 * x).contiguous())) / float(alg.norm64(b)) <= 1e-4
+
+
 def test_cg_matches_float64_oracle():
     """alg.cg_solve (float32 vectors, float64 scalars) against textbook CG in
     float64 on the CPU (oracle/cg.py): the same solution to 1e-4."""

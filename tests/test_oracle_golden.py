@@ -156,3 +156,35 @@ def test_toeplitz_oracle_matches_reference_golden(name):
         K = ON.toeplitz_kernel(locs, shape, weight=w, dtype=dtype)
         assert rel_l2(K, kern) < tol
         assert rel_l2(ON.toeplitz_normal(x, K, shape), normal) < tol
+
+
+INDEX = load_cases("index_cases.npz")
+
+
+def _index_case(rec):
+    m = rec["meta"]
+    cplx = "complex" in m["dtype"]
+    idx = tuple(torch.from_numpy(rec[f"idx{d}"]) for d in range(m["ndim"]) if f"idx{d}" in rec)
+    return m, cplx, idx
+
+
+@pytest.mark.parametrize("case", sorted(INDEX))
+def test_index_oracle_matches_reference(case):
+    """oracle.index against the reference's own index / index_adjoint: bit-exact
+    (the CPU index_add_ sums each cell's samples in ascending order)."""
+    from oracle import index as OX
+
+    rec = INDEX[case]
+    m, cplx, idx = _index_case(rec)
+    if "vals" in rec:
+        out = OX.index_adjoint(to_torch(rec["vals"], cplx), idx, m["grid"])
+        assert torch.equal(out, to_torch(rec["out"], cplx))
+    if "fwd" in rec and idx:
+        assert torch.equal(OX.index(to_torch(rec["grid_vals"], cplx), idx), to_torch(rec["fwd"], cplx))
+
+
+def test_index_oracle_bounds_error():
+    from oracle import index as OX
+
+    with pytest.raises(IndexError, match=r"idx\[1\]"):
+        OX.index_adjoint(torch.ones(3), (torch.tensor([0, 1, 2]), torch.tensor([0, 5, 1])), (3, 5))

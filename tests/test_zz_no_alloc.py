@@ -23,6 +23,7 @@ from torchlinops_gb300 import _ext, interp
 pytestmark = pytest.mark.gpu
 DEV = "cuda"
 TOL = 1e-5
+FIXED_BYTES = 32 << 20  # TLGB_ADJOINT_FIXED_SCRATCH_BYTES
 
 
 def _dense_case():
@@ -95,10 +96,16 @@ def test_fixed_scratch_without_room_for_the_transposed_values(ndim):
     ref = T.grid(vals, locs, size, 4.0, kernel_params=dict(beta=beta))
     plan = interp.get_plan(locs, size, 4.0, "kaiser_bessel", "circular", beta)
     desc = interp._desc(ndim, size, (4.0,) * ndim, "kaiser_bessel", 1, "circular", beta, True, nb, npts)
+    # the case is the one this test exists for: the partial tiles fit in the
+    # fixed buffer, the partial tiles and the point-major values together do not
+    sb = ctypes.c_size_t(0)
+    assert _ext.lib().tlgb_interp_adjoint_scratch_size(ctypes.byref(desc), ctypes.byref(plan.info),
+                                                       ctypes.byref(sb)) == _ext.TLGB_OK
+    values_bytes = npts * 64  # one group of 8 complex entries per point
+    partial_bytes = sb.value - values_bytes
+    assert 0 <= partial_bytes <= FIXED_BYTES < sb.value
     out = torch.full((nb, *size), float("nan"), dtype=torch.complex64, device=DEV)
     st = _fixed_call(desc, plan, locs, vals, out)
-    if st == _ext.TLGB_ERR_WORKSPACE:
-        pytest.skip("this plan's partial tiles alone exceed the fixed buffer")
     assert st == _ext.TLGB_OK, _ext.lib().tlgb_last_error()
     torch.cuda.synchronize()
     assert torch.equal(out, ref)

@@ -3097,8 +3097,8 @@ int dispatch_adj_n(const Geo& g, int cg, const tlgb_interp_plan_info* info, cons
   }
 }
 
-int launch_fwd(const Geo& g, const tlgb_interp_plan_info* info, const char* P, const float* locs, const void* grid,
-               void* out, cudaStream_t s) {
+int launch_fwd_rows(const Geo& g, const tlgb_interp_plan_info* info, const char* P, const float* locs,
+                    const void* grid, void* out, cudaStream_t s) {
   const int cg = fwd_cg(g);
   const bool small = ntb_for(g) == 5;
   if (g.ndim == 3) return small ? dispatch_fwd_n<3, 5>(g, cg, info, P, locs, grid, out, s) : dispatch_fwd_n<3, 9>(g, cg, info, P, locs, grid, out, s);
@@ -3106,8 +3106,28 @@ int launch_fwd(const Geo& g, const tlgb_interp_plan_info* info, const char* P, c
   return small ? dispatch_fwd_n<1, 5>(g, cg, info, P, locs, grid, out, s) : dispatch_fwd_n<1, 16>(g, cg, info, P, locs, grid, out, s);
 }
 
+// Launch grids have at most 65535 rows of batch groups. Wide 3D kernels
+// stage fewer than 8 entries per group (their region would not fit shared
+// memory), so a batch below TLGB_INTERP_MAX_BATCH can still need more rows:
+// batch entries are independent, so such a batch is launched in parts.
+int launch_fwd(const Geo& g, const tlgb_interp_plan_info* info, const char* P, const float* locs, const void* grid,
+               void* out, cudaStream_t s) {
+  const int64_t per = (int64_t)65535 * fwd_cg(g);
+  if (g.nbatch <= per) return launch_fwd_rows(g, info, P, locs, grid, out, s);
+  const int64_t vs = value_size(g), vol = (int64_t)g.N[0] * g.N[1] * g.N[2];
+  for (int64_t b0 = 0; b0 < g.nbatch; b0 += per) {
+    Geo gc = g;
+    gc.nbatch = std::min(per, (int64_t)g.nbatch - b0);
+    TLGB_TRY(launch_fwd_rows(gc, info, P, locs, static_cast<const char*>(grid) + b0 * vol * vs,
+                             static_cast<char*>(out) + b0 * g.npts * vs, s));
+  }
+  return TLGB_OK;
+}
+
 int launch_adj(const Geo& g, const tlgb_interp_plan_info* info, const char* P, const float* locs, const void* vals,
                void* grid, void* scratch, cudaStream_t s) {
+  // adj_cg is min(nbatch, 8): TLGB_INTERP_MAX_BATCH keeps the grid at <= 65535 rows
+  if (cdiv(g.nbatch, adj_cg(g)) > 65535) TLGB_FAIL(TLGB_ERR_UNSUPPORTED, "interp adjoint: too many batch groups");
   const int cg = adj_cg(g);
   const bool small = ntb_for(g) == 5;
   if (g.ndim == 3) return small ? dispatch_adj_n<3, 5>(g, cg, info, P, locs, vals, grid, scratch, s) : dispatch_adj_n<3, 9>(g, cg, info, P, locs, vals, grid, scratch, s);
@@ -3257,23 +3277,55 @@ static __device__ __align__(256) unsigned char g_adjoint_fixed_scratch[tlgb::kFi
 namespace tlgb {
 namespace {
 
-constexpr int kMaxDevices = 256;
+// The buffer's device address differs per CUDA context: the primary context
+// of each device, and any context a caller made itself with the driver API
+// (FFI hosts often do). The address is looked up once per context, with that
+// context current, and remembered; the first lookup in a context may load the
+// module there, which is when the buffer is allocated on that GPU.
 std::mutex g_fixed_mu;
-void* g_fixed_addr[kMaxDevices] = {};
+std::vector<std::pair<CUcontext, void*>> g_fixed_addr;
 
-// Device address of the fixed buffer on the current device, looked up once
-// per device (with that device current) and remembered.
-int fixed_scratch_address(void** out) {
-  int dev = 0;
-  TLGB_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kMaxDevices) TLGB_FAIL(TLGB_ERR_UNSUPPORTED, "device ordinal out of range");
-  std::lock_guard<std::mutex> lock(g_fixed_mu);
-  if (g_fixed_addr[dev] == nullptr) {
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+
+CtxGetCurrentFn ctx_get_current() {
+  static CtxGetCurrentFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
     void* p = nullptr;
-    TLGB_CUDA(cudaGetSymbolAddress(&p, g_adjoint_fixed_scratch));
-    g_fixed_addr[dev] = p;
-  }
-  *out = g_fixed_addr[dev];
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<CtxGetCurrentFn>(p);
+  });
+  return fn;
+}
+
+// Device address of the fixed buffer in the current context.
+int fixed_scratch_address(void** out) {
+  CtxGetCurrentFn get = ctx_get_current();
+  if (!get) TLGB_FAIL(TLGB_ERR_CUDA, "cuCtxGetCurrent is not available from the driver");
+  CUcontext ctx = nullptr;
+  if (get(&ctx) != CUDA_SUCCESS) TLGB_FAIL(TLGB_ERR_CUDA, "cuCtxGetCurrent failed");
+  std::lock_guard<std::mutex> lock(g_fixed_mu);
+  if (ctx != nullptr)
+    for (const auto& e : g_fixed_addr)
+      if (e.first == ctx) {
+        *out = e.second;
+        return TLGB_OK;
+      }
+  // with no context current, this first runtime call makes the current
+  // device's primary context current on this thread
+  void* p = nullptr;
+  TLGB_CUDA(cudaGetSymbolAddress(&p, g_adjoint_fixed_scratch));
+  if (ctx == nullptr && (get(&ctx) != CUDA_SUCCESS || ctx == nullptr))
+    TLGB_FAIL(TLGB_ERR_CUDA, "no current CUDA context");
+  for (const auto& e : g_fixed_addr)
+    if (e.first == ctx) {
+      *out = e.second;
+      return TLGB_OK;
+    }
+  g_fixed_addr.emplace_back(ctx, p);
+  *out = p;
   return TLGB_OK;
 }
 

@@ -1,10 +1,11 @@
 """GB300-native (sm_103a) interpolation and block kernels for torchlinops.
 
 A drop-in for the data-parallel hot path of torch-named-linops 0.7.4: the
-Interpolate linop's Kaiser-Bessel / spline ungridding and gridding in 1D-3D
-and the ArrayToBlocks / BlocksToArray pair, with the reference's functional
-signatures. All compute runs in the hand-written CUDA library ``libtlgb.so``
-(C ABI in ``include/tlgb.h``); there is no CPU fallback.
+Interpolate linop's Kaiser-Bessel / spline ungridding and gridding in 1D-3D,
+the ArrayToBlocks / BlocksToArray pair, and the Sampling linop's integer
+index / index_adjoint, with the reference's functional signatures. All
+compute runs in the hand-written CUDA library ``libtlgb.so`` (C ABI in
+``include/tlgb.h``); there is no CPU fallback.
 """
 
 from .blocks import (
@@ -15,6 +16,7 @@ from .blocks import (
     get_norm_weights,
     unfold,
 )
+from .index import index, index_adjoint
 from .interp import (
     clear_plan_cache,
     get_plan,

@@ -81,6 +81,32 @@ class BlocksDesc(ctypes.Structure):
     ]
 
 
+INDEX_MAX_DIM = 8
+# element types of the sampling ops (include/tlgb.h); raw types are copied only
+TLGB_I32, TLGB_I64, TLGB_RAW8, TLGB_RAW16 = 4, 5, 6, 7
+
+
+class IndexDesc(ctypes.Structure):
+    _fields_ = [
+        ("ndim", ctypes.c_int32),
+        ("dtype", ctypes.c_int32),
+        ("nbatch", ctypes.c_int64),
+        ("grid_size", ctypes.c_int64 * INDEX_MAX_DIM),
+        ("npts", ctypes.c_int64),
+    ]
+
+
+class IndexPlanInfo(ctypes.Structure):
+    _fields_ = [
+        ("ncells", ctypes.c_int64),
+        ("npts", ctypes.c_int64),
+        ("off_flat", ctypes.c_int64),
+        ("off_perm", ctypes.c_int64),
+        ("off_cells", ctypes.c_int64),
+        ("plan_bytes", ctypes.c_int64),
+    ]
+
+
 class ConvDesc(ctypes.Structure):
     _fields_ = [
         ("D", ctypes.c_int32),
@@ -109,6 +135,10 @@ _SIGNATURES = {
     "tlgb_interp_adjoint_fixed": ([_P, _P, _P, _P, _P, _P, _P], ctypes.c_int),
     "tlgb_unfold": ([_P, _P, _P, _P], ctypes.c_int),
     "tlgb_fold": ([_P, _P, _P, _P], ctypes.c_int),
+    "tlgb_index_plan_size": ([_P, _P, _P], ctypes.c_int),
+    "tlgb_index_plan_build": ([_P, _P, _P, ctypes.c_size_t, _P, ctypes.c_size_t, _P, _P], ctypes.c_int),
+    "tlgb_index_forward": ([_P, _P, _P, _P, _P, _P], ctypes.c_int),
+    "tlgb_index_adjoint": ([_P, _P, _P, _P, _P, _P], ctypes.c_int),
     "tlgb_cg_scratch_bytes": ([], ctypes.c_size_t),
     "tlgb_dot_f64": ([_P, _P, ctypes.c_int64, ctypes.c_int, _P, _P, ctypes.c_size_t, _P], ctypes.c_int),
     "tlgb_cg_set_pap": ([_P, _P, ctypes.c_int64, ctypes.c_int, _P, _P, ctypes.c_size_t, _P], ctypes.c_int),

@@ -235,7 +235,16 @@ def blocks_to_array(input, im_size, block_shape, stride=None, mask=None, out=Non
     return BlocksToArrayFn.apply(input, im_size, block_shape, stride, mask, out)
 
 
-def get_norm_weights(im_size, block_shape, stride=None, mask=None, device="cuda"):
-    """fold(unfold(ones)): 1/weights * fold(unfold(x)) == x where weights > 0."""
-    x = torch.ones(tuple(im_size), device=device)
-    return blocks_to_array(array_to_blocks(x, block_shape, stride, mask), im_size, block_shape, stride, mask)
+def get_norm_weights(im_size, block_shape, stride=None, mask=None, device="cpu"):
+    """fold(unfold(ones)): 1/weights * fold(unfold(x)) == x where weights > 0
+    (reference functional/_unfold/array_to_blocks.py:125-140, same arguments
+    and default device). The unfold and fold run on the CUDA kernels: on the
+    current CUDA device when ``device`` is not a CUDA device, and the weights
+    are returned on ``device``."""
+    device = torch.device(device)
+    work = device if device.type == "cuda" else torch.device("cuda", torch.cuda.current_device())
+    if mask is not None:
+        mask = mask.to(work)
+    x = torch.ones(tuple(im_size), device=work)
+    w = blocks_to_array(array_to_blocks(x, block_shape, stride, mask), im_size, block_shape, stride, mask)
+    return w.to(device)
