@@ -21,6 +21,8 @@
  *   tlgb_fold              -> fold / _fold,     functional/_unfold/fold.py:32,66
  *   tlgb_index_forward     -> index,            functional/_index/index.py:17
  *   tlgb_index_adjoint     -> index_adjoint,    functional/_index/index.py:75
+ *   tlgb_circular_pad      -> circular_pad,     functional/_interp/_circ_pad.py:10
+ *   tlgb_circular_pad_adjoint -> circular_pad_adjoint, _circ_pad.py:119
  */
 #ifndef TLGB_H_
 #define TLGB_H_
@@ -280,6 +282,35 @@ int tlgb_index_forward(const tlgb_index_desc* d, const tlgb_index_plan_info* inf
  * and integer element types. */
 int tlgb_index_adjoint(const tlgb_index_desc* d, const tlgb_index_plan_info* info, const void* plan,
                        const void* vals, void* out, tlgb_stream_t stream);
+
+/* ------------------------------------------------------------------------ */
+/* Circular padding of the trailing dims (Convolution linop, circular mode).  */
+/* Replaces circular_pad / circular_pad_adjoint,                              */
+/* functional/_interp/_circ_pad.py:10,119 (F.pad three dims at a time, and    */
+/* autograd through it for the adjoint).                                      */
+/* ------------------------------------------------------------------------ */
+
+#define TLGB_CIRCPAD_MAX_DIM 8
+
+/* in [nbatch, size...] -> out [nbatch, size[e] + pad_lo[e] + pad_hi[e] ...],
+ * dims listed leading to trailing; 0 <= pad <= size per dim (the padding
+ * wraps around at most once, as torch's circular F.pad requires). */
+typedef struct tlgb_circpad_desc {
+  int32_t ndim;  /* padded trailing dims, 1..TLGB_CIRCPAD_MAX_DIM */
+  int32_t dtype; /* TLGB_F32 ... TLGB_RAW16 (the adjoint: not the raw types) */
+  int64_t nbatch;
+  int64_t size[TLGB_CIRCPAD_MAX_DIM];
+  int64_t pad_lo[TLGB_CIRCPAD_MAX_DIM];
+  int64_t pad_hi[TLGB_CIRCPAD_MAX_DIM];
+} tlgb_circpad_desc;
+
+/* out[b, j] = in[b, (j - pad_lo) mod size] per dim: a copy. */
+int tlgb_circular_pad(const tlgb_circpad_desc* d, const void* in, void* out, tlgb_stream_t stream);
+
+/* The adjoint: out (unpadded) [b, i] = sum of in (padded) [b, j] over the j
+ * that tlgb_circular_pad copies from i, in ascending padded order
+ * (deterministic). Every element of out is written. */
+int tlgb_circular_pad_adjoint(const tlgb_circpad_desc* d, const void* in, void* out, tlgb_stream_t stream);
 
 /* ------------------------------------------------------------------------ */
 /* Conjugate gradients with float64 scalars.                                   */

@@ -320,6 +320,49 @@ def make_index(F, out_dir):
     return len(cases)
 
 
+def make_circpad(L, out_dir):
+    """Circular padding (functional/_interp/_circ_pad.py) and the Convolution
+    linop in circular mode (linops/convolution.py): the reference's own test
+    shapes (_interp/tests/test_circular_pad.py), asymmetric and zero pads,
+    batches, and a convolution forward / adjoint in 1D, 2D and 3D."""
+    from torchlinops.functional._interp._circ_pad import circular_pad, circular_pad_adjoint
+
+    cases = {}
+    gen = torch.Generator().manual_seed(77)
+    specs = {
+        "ref2d": ((15, 20), [4, 4, 2, 2], False),
+        "refnd": ((5, 15, 20, 19, 18), [1, 1, 2, 2, 3, 3, 5, 5], False),
+        "ref1d_c": ((3,), [1, 1], True),
+        "ref2d_c": ((3, 3), [2, 2, 1, 1], True),
+        "asym3d_c": ((2, 3, 9, 10, 11), [3, 2, 0, 4, 1, 1], True),
+        "full1d": ((4, 6), [6, 6], False),
+    }
+    for name, (shape, padding, cplx) in specs.items():
+        x = _rand(shape, cplx, gen)
+        y = circular_pad(x, padding)
+        z = _rand(tuple(y.shape), cplx, gen)
+        adj = circular_pad_adjoint(z, padding)
+        meta = dict(padding=padding, complex=cplx)
+        cases[name] = dict(x=_np(x), pad=_np(y), z=_np(z), adj=_np(adj.detach()), meta=json.dumps(meta))
+    conv_specs = {
+        "conv1d": ((3, 40), (5,)),
+        "conv2d_even": ((2, 3, 21, 18), (4, 3)),
+        "conv3d_c": ((2, 12, 13, 11), (3, 4, 3)),
+    }
+    for name, (xshape, kshape) in conv_specs.items():
+        cplx = name.endswith("_c")
+        kern = _rand(kshape, cplx, gen)
+        x = _rand(xshape, cplx, gen)
+        A = L.Convolution(kern, padding_mode="circular")
+        y = A(x)
+        z = _rand(tuple(y.shape), cplx, gen)
+        yh = A.H(z)
+        meta = dict(complex=cplx)
+        cases[name] = dict(kernel=_np(kern), x=_np(x), fwd=_np(y), z=_np(z), adj=_np(yh), meta=json.dumps(meta))
+    np.savez_compressed(os.path.join(out_dir, "circpad_cases.npz"), **_flatten(cases))
+    return len(cases)
+
+
 def _flatten(cases):
     flat = {}
     for k, rec in cases.items():
@@ -333,7 +376,7 @@ def main():
     ap.add_argument("--ref", default=os.environ.get("TORCHLINOPS_SRC"),
                     help="the reference's src/ directory (default: $TORCHLINOPS_SRC)")
     ap.add_argument("--out", default=HERE)
-    ap.add_argument("--only", choices=["toeplitz", "index"], default=None, help="write only this fixture")
+    ap.add_argument("--only", choices=["toeplitz", "index", "circpad"], default=None, help="write only this fixture")
     args = ap.parse_args()
     if not args.ref:
         ap.error("give the reference's src/ directory with --ref or TORCHLINOPS_SRC")
@@ -349,6 +392,10 @@ def main():
         make_toeplitz(L, args.out)
         print(f"wrote toeplitz.npz in {time.time() - t0:.1f}s")
         return
+    if args.only == "circpad":
+        n = make_circpad(L, args.out)
+        print(f"wrote {n} circular pad cases in {time.time() - t0:.1f}s")
+        return
     if args.only == "index":
         n = make_index(F, args.out)
         print(f"wrote {n} index cases in {time.time() - t0:.1f}s")
@@ -361,7 +408,9 @@ def main():
     n_i = make_interp(F, args.out)
     n_b = make_blocks(F, args.out)
     n_x = make_index(F, args.out)
-    print(f"wrote {n_i} interp cases, {n_b} block cases, {n_x} index cases in {time.time() - t0:.1f}s")
+    n_c = make_circpad(L, args.out)
+    print(f"wrote {n_i} interp cases, {n_b} block cases, {n_x} index cases, {n_c} circular pad cases in "
+          f"{time.time() - t0:.1f}s")
 
 
 if __name__ == "__main__":

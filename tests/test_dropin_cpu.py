@@ -45,6 +45,10 @@ FAKE = {
         def interpolate(*a, **k): return ungrid(*a, **k)
         def interpolate_adjoint(*a, **k): return grid(*a, **k)
     """),
+    "functional/_interp/_circ_pad.py": textwrap.dedent("""
+        def circular_pad(t, padding): return 'ref-pad'
+        def circular_pad_adjoint(t, padding): return 'ref-pad-adjoint'
+    """),
     "functional/_index/__init__.py": "",
     "functional/_index/index.py": textwrap.dedent("""
         __all__ = ['index', 'index_adjoint']
@@ -69,6 +73,7 @@ FAKE = {
     """),
     "linops/__init__.py": textwrap.dedent("""
         import fakelinops.functional as F
+        from ..functional._interp._circ_pad import circular_pad
         def interp_fn(x, locs): return F.interpolate(x, locs, 4.0)
     """),
 }
@@ -105,6 +110,7 @@ def test_patch_rebinds_every_by_name_site(fake_pkg):
     assert ("fakelinops.functional._interp.interp", "ungrid") in sites
     assert ("fakelinops.functional._unfold.array_to_blocks", "fold") in sites
     assert ("fakelinops.functional", "index_adjoint") in sites
+    assert ("fakelinops.linops", "circular_pad") in sites
     assert N.interpolate is T.interpolate and fakelinops.functional.unfold is T.unfold
     # run-time lookups from the linops and the functional NUFFT reach this package
     with pytest.raises(RuntimeError, match="CUDA tensors only"):
@@ -141,7 +147,8 @@ def test_patch_reroutes_the_reference_itself():
                       ("torchlinops.functional._unfold.array_to_blocks", "unfold"),
                       ("torchlinops.functional", "interpolate"),
                       ("torchlinops.functional", "array_to_blocks"),
-                      ("torchlinops.functional", "index_adjoint")]:
+                      ("torchlinops.functional", "index_adjoint"),
+                      ("torchlinops.linops.convolution", "circular_pad")]:
                 assert s in sites, s
             assert N.interpolate is T.interpolate
             locs = torch.rand(50, 2) * 10 - 5
@@ -157,6 +164,8 @@ def test_patch_reroutes_the_reference_itself():
                 L.ArrayToBlocks((16, 16), (4, 4), (2, 2))(x)  # linops/array_to_blocks.py:68
             with cuda_only:
                 L.Sampling((torch.tensor([1, 2]), torch.tensor([3, 4])), (16, 16)).H(torch.ones(2))
+            with cuda_only:
+                L.Convolution(torch.ones(3, 3), padding_mode="circular")(x)  # linops/convolution.py:126
         finally:
             dropin.unpatch("torchlinops")
         assert F.interpolate is not T.interpolate

@@ -188,3 +188,26 @@ def test_index_oracle_bounds_error():
 
     with pytest.raises(IndexError, match=r"idx\[1\]"):
         OX.index_adjoint(torch.ones(3), (torch.tensor([0, 1, 2]), torch.tensor([0, 5, 1])), (3, 5))
+
+
+CIRC = load_cases("circpad_cases.npz")
+
+
+@pytest.mark.parametrize("case", sorted(CIRC))
+def test_circpad_oracle_matches_reference(case):
+    """oracle.circpad against the reference's circular_pad (bit-exact: copies),
+    its autograd adjoint and its Convolution linop in circular mode."""
+    from oracle import circpad as OC
+
+    rec = CIRC[case]
+    m = rec["meta"]
+    cplx = m["complex"]
+    if "padding" in m:
+        x = to_torch(rec["x"], cplx)
+        assert torch.equal(OC.circular_pad(x, m["padding"]), to_torch(rec["pad"], cplx))
+        adj = OC.circular_pad_adjoint(to_torch(rec["z"], cplx), m["padding"])
+        assert rel_l2(adj, to_torch(rec["adj"], cplx)) < 1e-6
+    else:
+        k = to_torch(rec["kernel"], cplx)
+        assert rel_l2(OC.conv_circular(k, to_torch(rec["x"], cplx)), to_torch(rec["fwd"], cplx)) < 1e-6
+        assert rel_l2(OC.conv_circular(k, to_torch(rec["z"], cplx), adjoint=True), to_torch(rec["adj"], cplx)) < 1e-6

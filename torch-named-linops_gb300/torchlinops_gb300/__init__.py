@@ -16,6 +16,7 @@ from .blocks import (
     get_norm_weights,
     unfold,
 )
+from .circpad import circular_pad, circular_pad_adjoint
 from .index import index, index_adjoint
 from .interp import (
     clear_plan_cache,

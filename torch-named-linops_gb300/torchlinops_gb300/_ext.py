@@ -107,6 +107,20 @@ class IndexPlanInfo(ctypes.Structure):
     ]
 
 
+CIRCPAD_MAX_DIM = 8
+
+
+class CircPadDesc(ctypes.Structure):
+    _fields_ = [
+        ("ndim", ctypes.c_int32),
+        ("dtype", ctypes.c_int32),
+        ("nbatch", ctypes.c_int64),
+        ("size", ctypes.c_int64 * CIRCPAD_MAX_DIM),
+        ("pad_lo", ctypes.c_int64 * CIRCPAD_MAX_DIM),
+        ("pad_hi", ctypes.c_int64 * CIRCPAD_MAX_DIM),
+    ]
+
+
 class ConvDesc(ctypes.Structure):
     _fields_ = [
         ("D", ctypes.c_int32),
@@ -139,6 +153,8 @@ _SIGNATURES = {
     "tlgb_index_plan_build": ([_P, _P, _P, ctypes.c_size_t, _P, ctypes.c_size_t, _P, _P], ctypes.c_int),
     "tlgb_index_forward": ([_P, _P, _P, _P, _P, _P], ctypes.c_int),
     "tlgb_index_adjoint": ([_P, _P, _P, _P, _P, _P], ctypes.c_int),
+    "tlgb_circular_pad": ([_P, _P, _P, _P], ctypes.c_int),
+    "tlgb_circular_pad_adjoint": ([_P, _P, _P, _P], ctypes.c_int),
     "tlgb_cg_scratch_bytes": ([], ctypes.c_size_t),
     "tlgb_dot_f64": ([_P, _P, ctypes.c_int64, ctypes.c_int, _P, _P, ctypes.c_size_t, _P], ctypes.c_int),
     "tlgb_cg_set_pap": ([_P, _P, ctypes.c_int64, ctypes.c_int, _P, _P, ctypes.c_size_t, _P], ctypes.c_int),

@@ -8,7 +8,9 @@ modules bind by name at import time:
   (the functional ``nufft`` / ``nufft_adjoint`` call them at ``:54,101``);
 * ``functional/_interp/interp.py:7-8`` imports ``grid`` and ``ungrid`` (its
   autograd functions call them);
-* ``functional/_unfold/array_to_blocks.py:10-11`` imports ``fold`` and ``unfold``.
+* ``functional/_unfold/array_to_blocks.py:10-11`` imports ``fold`` and ``unfold``;
+* ``linops/convolution.py:9`` imports ``circular_pad`` (its circular mode,
+  ``:120-130,148-150``).
 
 The linops (``linops/interp.py:97-104``, ``linops/array_to_blocks.py:68-90,163-180``,
 ``linops/sampling.py:95-101``) call ``torchlinops.functional.<name>`` at run
@@ -17,7 +19,8 @@ by-name copies above on the reference's own path, so ``patch`` walks every
 loaded module of the package and replaces each attribute that *is* one of the
 reference's hot-path functions with this package's function of the same name.
 After it, ``NUFFT``, ``Interpolate``, ``.H``, ``.N``, ``Chain``, ``toeplitz_psf``,
-``ArrayToBlocks``, ``Sampling`` and ``conjugate_gradients`` run on these
+``ArrayToBlocks``, ``Sampling``, ``Convolution`` (circular padding) and
+``conjugate_gradients`` run on these
 kernels unchanged. ``unpatch`` restores every rebound attribute.
 
 One behaviour differs by design: CPU tensors raise instead of running a torch
@@ -31,6 +34,7 @@ import sys
 from types import ModuleType
 
 from . import blocks as _blocks
+from . import circpad as _circpad
 from . import interp as _interp
 from .index import index as _index_fwd
 from .index import index_adjoint as _index_adj
@@ -50,6 +54,8 @@ HOT_PATH = {
     ("functional._unfold.fold", "fold"): _blocks.fold,
     ("functional._index.index", "index"): _index_fwd,
     ("functional._index.index", "index_adjoint"): _index_adj,
+    ("functional._interp._circ_pad", "circular_pad"): _circpad.circular_pad,
+    ("functional._interp._circ_pad", "circular_pad_adjoint"): _circpad.circular_pad_adjoint,
 }
 
 # package name -> list of (module, attribute, original object)

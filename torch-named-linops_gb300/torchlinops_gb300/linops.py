@@ -40,7 +40,10 @@ from torch import Tensor
 
 from . import _ext
 from . import blocks as B
+from . import circpad as CP
 from . import interp as I
+from .index import index as _index_fwd
+from .index import index_adjoint as _index_adj
 
 __all__ = [
     "NamedLinop",
@@ -52,6 +55,8 @@ __all__ = [
     "Interpolate",
     "ArrayToBlocks",
     "BlocksToArray",
+    "Sampling",
+    "Convolution",
     "NUFFT",
     "ToeplitzNormal",
     "toeplitz_psf",
@@ -545,6 +550,92 @@ class BlocksToArray(NamedLinop):
 
     def adjoint(self):
         return ArrayToBlocks(self.grid_size, self.block_size, self.stride, self.mask)
+
+
+class Sampling(NamedLinop):
+    """Samples at integer locations (linops/sampling.py:16-101): (batch,
+    grid) -> (batch, idx batch), forward ``index``, adjoint the deterministic
+    ``index_adjoint``."""
+
+    def __init__(self, idx: tuple[Tensor, ...], input_size: tuple[int, ...]):
+        super().__init__()
+        if len(idx) != len(input_size):
+            raise ValueError(f"Input size {input_size} doesn't match index with length {len(idx)}.")
+        for d, (t, s) in enumerate(zip(idx, input_size)):
+            if (t < 0).any() or (t >= s).any():
+                raise ValueError(
+                    f"Sampling index must lie within range [0, {s - 1}] but got range [{t.min().item()}, {t.max().item()}] for dim {d}"
+                )
+        self.input_size = tuple(int(s) for s in input_size)
+        self.idx = nn.ParameterList([nn.Parameter(i, requires_grad=False) for i in idx])
+
+    @staticmethod
+    def fn(s, x, /):
+        return _index_fwd(x, tuple(s.idx))
+
+    @staticmethod
+    def adj_fn(s, x, /):
+        return _index_adj(x, tuple(s.idx), s.input_size)
+
+
+def _pad_to_odd(kernel: Tensor, ndim: int) -> Tensor:
+    # reference linops/convolution.py:355-378: one trailing zero per even dim
+    pad = []
+    for s in reversed(kernel.shape[-ndim:]):
+        pad += [0, 0 if s % 2 else 1]
+    return F.pad(kernel, pad, value=0)
+
+
+class Convolution(NamedLinop):
+    """Convolution with one kernel broadcast over every leading dim
+    (linops/convolution.py:19-164): 'zeros' or 'circular' padding, the kernel
+    centred at kernel_size // 2 and flipped (a true convolution). The
+    circular mode pads with this package's ``circular_pad`` and its adjoint
+    convolves the padded input with the flipped, conjugated kernel, as the
+    reference does; the convolutions themselves run in torch (cuDNN)."""
+
+    def __init__(self, kernel: Tensor, padding_mode: str = "zeros"):
+        super().__init__()
+        ndim = kernel.dim()
+        if ndim not in (1, 2, 3):
+            raise ValueError(f"ndim must be 1, 2, or 3, got {ndim}")
+        if padding_mode not in ("zeros", "circular"):
+            raise ValueError(f"Unrecognized padding_mode: {padding_mode}")
+        self.ndim = ndim
+        self.padding_mode = padding_mode
+        kernel = _pad_to_odd(kernel, ndim)
+        half = [(s // 2, s // 2) for s in kernel.shape[-ndim:]]
+        self._crop = tuple(slice(a, -b if b > 0 else None) for a, b in half)
+        self._pad = tuple(v for pair in reversed(half) for v in pair)
+        self.kernel = kernel
+        w = torch.flip(kernel, dims=tuple(range(-ndim, 0)))[None, None]
+        self._weight = nn.Parameter(w, requires_grad=False)
+
+    def _flat(self, x):
+        lead = x.shape[: x.ndim - self.ndim]
+        return x.reshape(-1, 1, *x.shape[x.ndim - self.ndim:]), lead
+
+    @staticmethod
+    def fn(c, x, /):
+        xf, lead = c._flat(x)
+        conv = (F.conv1d, F.conv2d, F.conv3d)[c.ndim - 1]
+        if c.padding_mode == "circular":
+            y = conv(CP.circular_pad(xf, c._pad), c._weight, padding=0)
+        else:
+            y = conv(xf, c._weight, padding="same")
+        return y.reshape(*lead, *y.shape[2:])
+
+    @staticmethod
+    def adj_fn(c, x, /):
+        xf, lead = c._flat(x)
+        if c.padding_mode == "circular":
+            w = torch.flip(c._weight, dims=tuple(range(-c.ndim, 0))).conj()
+            conv = (F.conv1d, F.conv2d, F.conv3d)[c.ndim - 1]
+            y = conv(CP.circular_pad(xf, c._pad), w, padding=0)
+        else:
+            conv_t = (F.conv_transpose1d, F.conv_transpose2d, F.conv_transpose3d)[c.ndim - 1]
+            y = conv_t(xf, c._weight.conj(), padding=0)[(slice(None), slice(None)) + c._crop]
+        return y.reshape(*lead, *y.shape[2:])
 
 
 def nufft_beta(width: float, oversamp: float) -> float:
