@@ -363,6 +363,27 @@ def make_circpad(L, out_dir):
     return len(cases)
 
 
+def make_nufft_sampling(L, out_dir):
+    """The NUFFT in its "sampling" mode (linops/nufft.py:185-200): pad, centred
+    FFT, then Sampling at rounded, wrapped k-space indices; forward and
+    adjoint in 2D and 3D, complex64, with repeated indices."""
+    out = {}
+    gen = torch.Generator().manual_seed(31)
+    for name, shape, npts in (("2d", (16, 20), 700), ("3d", (8, 10, 6), 900)):
+        locs = (torch.rand(npts, len(shape), generator=gen) - 0.5) * torch.tensor(shape, dtype=torch.float32)
+        x = _rand((2, *shape), True, gen)
+        A = L.NUFFT(locs, shape, output_shape=("K",), mode="sampling")
+        y = A(x)
+        z = _rand(tuple(y.shape), True, gen)
+        out[f"{name}_locs"] = locs.numpy()
+        out[f"{name}_x"] = _np(x)
+        out[f"{name}_fwd"] = _np(y)
+        out[f"{name}_z"] = _np(z)
+        out[f"{name}_adj"] = _np(A.H(z))
+    np.savez_compressed(os.path.join(out_dir, "nufft_sampling.npz"), **out)
+    return len(out) // 5
+
+
 def _flatten(cases):
     flat = {}
     for k, rec in cases.items():
@@ -376,7 +397,7 @@ def main():
     ap.add_argument("--ref", default=os.environ.get("TORCHLINOPS_SRC"),
                     help="the reference's src/ directory (default: $TORCHLINOPS_SRC)")
     ap.add_argument("--out", default=HERE)
-    ap.add_argument("--only", choices=["toeplitz", "index", "circpad"], default=None, help="write only this fixture")
+    ap.add_argument("--only", choices=["toeplitz", "index", "circpad", "nufft_sampling"], default=None, help="write only this fixture")
     args = ap.parse_args()
     if not args.ref:
         ap.error("give the reference's src/ directory with --ref or TORCHLINOPS_SRC")
@@ -391,6 +412,10 @@ def main():
     if args.only == "toeplitz":
         make_toeplitz(L, args.out)
         print(f"wrote toeplitz.npz in {time.time() - t0:.1f}s")
+        return
+    if args.only == "nufft_sampling":
+        n = make_nufft_sampling(L, args.out)
+        print(f"wrote {n} sampling-mode NUFFT cases in {time.time() - t0:.1f}s")
         return
     if args.only == "circpad":
         n = make_circpad(L, args.out)
@@ -409,6 +434,7 @@ def main():
     n_b = make_blocks(F, args.out)
     n_x = make_index(F, args.out)
     n_c = make_circpad(L, args.out)
+    make_nufft_sampling(L, args.out)
     print(f"wrote {n_i} interp cases, {n_b} block cases, {n_x} index cases, {n_c} circular pad cases in "
           f"{time.time() - t0:.1f}s")
 

@@ -83,3 +83,21 @@ def test_index_errors_match_reference():
         T.index(torch.ones(4, device=DEV), (torch.tensor([0], device=DEV),) * 2)
     with pytest.raises(ValueError, match="should correspond"):
         T.index_adjoint(torch.ones(2, 5, device=DEV), (torch.tensor([0, 1, 2], device=DEV),), (4,))
+
+
+@pytest.mark.parametrize("name", ["2d", "3d"])
+def test_nufft_sampling_mode_matches_reference(name):
+    """The NUFFT's "sampling" mode (reference linops/nufft.py:185-200): the
+    reference's own forward and adjoint (tests/golden/nufft_sampling.npz)."""
+    import numpy as np
+
+    from conftest import GOLDEN, rel_l2
+    from torchlinops_gb300 import linops
+
+    d = np.load(f"{GOLDEN}/nufft_sampling.npz")
+    locs = torch.from_numpy(d[f"{name}_locs"]).to(DEV)
+    x = to_torch(d[f"{name}_x"], True).to(DEV)
+    A = linops.NUFFT(locs, tuple(x.shape[1:]), mode="sampling")
+    assert rel_l2(A(x).cpu(), to_torch(d[f"{name}_fwd"], True)) < 1e-5
+    z = to_torch(d[f"{name}_z"], True).to(DEV)
+    assert rel_l2(A.H(z).cpu(), to_torch(d[f"{name}_adj"], True)) < 1e-5

@@ -586,6 +586,19 @@ def _pad_to_odd(kernel: Tensor, ndim: int) -> Tensor:
     return F.pad(kernel, pad, value=0)
 
 
+class _Fp32Conv:
+    """cuDNN convolutions in full float32: torch lets cuDNN use TF32 (10-bit
+    mantissas) by default, far coarser than this package's 1e-5 tolerance
+    against the reference's CPU float32 convolution."""
+
+    def __enter__(self):
+        self.prev = torch.backends.cudnn.allow_tf32
+        torch.backends.cudnn.allow_tf32 = False
+
+    def __exit__(self, *exc):
+        torch.backends.cudnn.allow_tf32 = self.prev
+
+
 class Convolution(NamedLinop):
     """Convolution with one kernel broadcast over every leading dim
     (linops/convolution.py:19-164): 'zeros' or 'circular' padding, the kernel
@@ -619,27 +632,47 @@ class Convolution(NamedLinop):
     def fn(c, x, /):
         xf, lead = c._flat(x)
         conv = (F.conv1d, F.conv2d, F.conv3d)[c.ndim - 1]
-        if c.padding_mode == "circular":
-            y = conv(CP.circular_pad(xf, c._pad), c._weight, padding=0)
-        else:
-            y = conv(xf, c._weight, padding="same")
+        with _Fp32Conv():
+            if c.padding_mode == "circular":
+                y = conv(CP.circular_pad(xf, c._pad), c._weight, padding=0)
+            else:
+                y = conv(xf, c._weight, padding="same")
         return y.reshape(*lead, *y.shape[2:])
 
     @staticmethod
     def adj_fn(c, x, /):
         xf, lead = c._flat(x)
-        if c.padding_mode == "circular":
-            w = torch.flip(c._weight, dims=tuple(range(-c.ndim, 0))).conj()
-            conv = (F.conv1d, F.conv2d, F.conv3d)[c.ndim - 1]
-            y = conv(CP.circular_pad(xf, c._pad), w, padding=0)
-        else:
-            conv_t = (F.conv_transpose1d, F.conv_transpose2d, F.conv_transpose3d)[c.ndim - 1]
-            y = conv_t(xf, c._weight.conj(), padding=0)[(slice(None), slice(None)) + c._crop]
+        with _Fp32Conv():
+            if c.padding_mode == "circular":
+                w = torch.flip(c._weight, dims=tuple(range(-c.ndim, 0))).conj()
+                conv = (F.conv1d, F.conv2d, F.conv3d)[c.ndim - 1]
+                y = conv(CP.circular_pad(xf, c._pad), w, padding=0)
+            else:
+                conv_t = (F.conv_transpose1d, F.conv_transpose2d, F.conv_transpose3d)[c.ndim - 1]
+                y = conv_t(xf, c._weight.conj(), padding=0)[(slice(None), slice(None)) + c._crop]
         return y.reshape(*lead, *y.shape[2:])
 
 
 def nufft_beta(width: float, oversamp: float) -> float:
     return I.kaiser_bessel_beta(width, oversamp)
+
+
+def prep_locs_sampling(locs: Tensor, grid_size, padded_size, pad_mode="circular") -> Tensor:
+    """Centred locs -> integer indices of the padded grid for the sampling
+    mode (nufft.py:316-333): scale, shift, then clamp (zero padding) or round
+    and wrap (circular), as int64."""
+    if pad_mode not in ("zero", "circular"):
+        raise ValueError(f"Unrecognized padding mode during prep: {pad_mode}")
+    out = locs.clone()
+    for i in range(-len(grid_size), 0):
+        out[..., i] *= padded_size[i] / grid_size[i]
+        out[..., i] += padded_size[i] // 2
+        if pad_mode == "zero":
+            out[..., i] = torch.clamp(out[..., i], 0, padded_size[i] - 1)
+        else:
+            out[..., i] = torch.round(out[..., i])
+            out[..., i] = torch.remainder(out[..., i], padded_size[i])
+    return out.to(torch.int64)
 
 
 def prep_locs(locs: Tensor, grid_size, padded_size, pad_mode="circular") -> Tensor:
@@ -696,11 +729,33 @@ class NUFFT(Chain):
         apodize_weights: Optional[Tensor] = None,
         **options,
     ):
-        if mode != "interpolate":
+        if mode not in ("interpolate", "sampling"):
             raise ValueError(f"Unrecognized NUFFT mode: {mode}")
         device = locs.device
         ndim = len(grid_size)
         padded_size = tuple(int(i * oversamp) for i in grid_size)
+        self.mode = mode
+        if mode == "sampling":
+            # pad -> centred FFT -> Sampling at rounded, wrapped k-space
+            # indices; no apodization or scaling (nufft.py:185-200)
+            locs_prepared = prep_locs_sampling(locs, grid_size, padded_size) if do_prep_locs else locs
+            if locs_prepared.is_complex() or locs_prepared.is_floating_point():
+                raise ValueError(f"Sampling linop requries integer-type locs but got {locs_prepared.dtype}")
+            padshift = PadShift(padded_size, grid_size, None)
+            fft = FFT(ndim=ndim, centered=False, norm="ortho")
+            interp = Sampling(tuple(locs_prepared[..., d] for d in range(ndim)), padded_size)
+            super().__init__(padshift, fft, interp, name="NUFFT")
+            self.options = options
+            self.apodize_weight = None
+            self.scale_factor = 1.0
+            self.padded_size = padded_size
+            self.locs_prepared = locs_prepared
+            self.locs = locs
+            self.grid_size = tuple(grid_size)
+            self.oversamp = oversamp
+            self.width = width
+            self.pad, self.fft, self.interp = padshift, fft, interp
+            return
         beta = nufft_beta(width, oversamp)
         if apodize_weights is None:
             weight = globals()["apodize_weights"](grid_size, padded_size, oversamp, width, beta).to(device)
@@ -738,7 +793,7 @@ class NUFFT(Chain):
         ``self.H @ inner @ self`` (nufft.py:226-239) for ``inner`` None or a
         diagonal weighting of the points; otherwise (and for other ``inner``
         operators) the chain itself, forward then adjoint."""
-        if self.options.get("toeplitz", False):
+        if self.options.get("toeplitz", False) and self.mode == "interpolate":
             weight = _point_weight(inner, self.locs_prepared.shape[:-1])
             if weight is not False:
                 return ToeplitzNormal(self, weight, self.options.get("toeplitz_oversamp", 2.0),
