@@ -52,10 +52,21 @@ int tlgb_version(void);
 /* Reads (and, if `clear`, resets) the device status word of the current
  * device. Kernels whose internal waits are bounded set a bit instead of
  * hanging when a wait gives up, and their outputs are then incomplete:
- * 1 = the TMA-staged gather, 2 = the tensor-core convolution. Synchronises
+ * 1 = the TMA-staged gather, 2 = the tensor-core convolution; in the
+ * range-checked debug build (libtlgb_checked.so), 4 = an index outside its
+ * range in a checked access. Synchronises
  * the device. *status = 0 means no kernel has reported an error since the
  * last clear. */
 int tlgb_device_status(int32_t* status, int32_t clear);
+
+/* Test hook for the failure path of the bounded waits, off by default.
+ * While `on` is nonzero, calls made afterwards launch the TMA-staged gathers
+ * and the 2D trajectory gradient without their region copy, and those
+ * kernels poll the copy's mbarrier once: the wait runs out with nothing in
+ * flight, the kernel sets status bit 1 and its CTAs return, leaving the
+ * output incomplete. Returns the previous setting. For tests of
+ * tlgb_device_status only; no counterpart in the reference. */
+int tlgb_test_skip_region_copy(int32_t on);
 
 /* ------------------------------------------------------------------------ */
 /* Interpolation: Kaiser-Bessel / spline ungridding and gridding, 1D-3D.      */

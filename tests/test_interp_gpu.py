@@ -103,13 +103,14 @@ def test_dense_centre_against_oracle(ndim, n, npts, nb, pad):
 
 
 @pytest.mark.parametrize("shape", [(40, 36, 48), (40, 36, 45)])
-@pytest.mark.parametrize("nb", [8, 11])
+@pytest.mark.parametrize("nb", [1, 2, 4, 8, 11])
 @pytest.mark.parametrize("pad", ["circular", "zero"])
 @pytest.mark.parametrize("kernel", ["kaiser_bessel", "spline"])
 def test_eight_entry_3d_paths_against_oracle(shape, nb, pad, kernel):
     """3D, 8 complex entries per group: the TMA-staged gather (even Z) and its
     plain-load fallback (odd Z, wrapping edge regions), a ragged last group,
-    dense split tiles, points across every edge and exact-integer points."""
+    batches below 8 entries run as one partly empty group, dense split
+    tiles, points across every edge and exact-integer points."""
     from torchlinops_gb300 import _ext
 
     gen = torch.Generator().manual_seed(nb + len(pad) + shape[2])
@@ -136,13 +137,14 @@ def test_eight_entry_3d_paths_against_oracle(shape, nb, pad, kernel):
 
 
 @pytest.mark.parametrize("shape", [(160, 144), (90, 61)])
-@pytest.mark.parametrize("nb", [8, 11])
+@pytest.mark.parametrize("nb", [1, 4, 8, 11])
 @pytest.mark.parametrize("pad", ["circular", "zero"])
 @pytest.mark.parametrize("kernel", ["kaiser_bessel", "spline"])
 def test_eight_entry_2d_paths_against_oracle(shape, nb, pad, kernel):
     """2D, 8 complex entries per group: the TMA-staged gather (even Z) and its
     plain-load fallback (odd Z, wrapping edge regions), a ragged last group,
-    dense tiles, points across every edge and exact-integer points."""
+    batches below 8 entries run as one partly empty group, dense tiles,
+    points across every edge and exact-integer points."""
     from torchlinops_gb300 import _ext
 
     gen = torch.Generator().manual_seed(nb + len(pad) + shape[1])

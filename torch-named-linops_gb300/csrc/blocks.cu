@@ -74,7 +74,7 @@ __global__ void __launch_bounds__(256) unfold_rows_kernel(const U* __restrict__ 
     const uint32_t b2 = fdiv(r1, div_B0);
     const uint32_t i0 = r1 - b2 * (uint32_t)g.B[0];
     const int64_t off = (int64_t)i0 * row_in + (int64_t)i1 * im2u + (int64_t)b2 * s2u + i2;
-    dst[u] = __ldg(src + off);
+    if (TLGB_IN_RANGE((src - in) + off, g.nbatch * plane_in)) dst[u] = __ldg(src + off);
   }
 }
 
@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(256) unfold_masked_kernel(const T* __restrict_
     const uint32_t i0 = fdiv(k01, div_B1);
     const uint32_t i1 = k01 - i0 * (uint32_t)g.B[1];
     const int64_t off = (int64_t)i0 * row_in + (int64_t)i1 * g.im[2] + (int64_t)b2 * g.s[2] + i2;
-    dst[u] = __ldg(src + off);
+    if (TLGB_IN_RANGE((src - in) + off, g.nbatch * g.im[0] * row_in)) dst[u] = __ldg(src + off);
   }
 }
 
@@ -179,7 +179,7 @@ __global__ void __launch_bounds__(256) fold_kernel(const T* __restrict__ in, T* 
             if (j < 0) continue;
           }
           (void)full_bvol;
-          Acc<T>::add(acc, __ldg(src + (blk01 + b2) * bvol + j));
+          if (TLGB_IN_RANGE((blk01 + b2) * bvol + j, nbl * bvol)) Acc<T>::add(acc, __ldg(src + (blk01 + b2) * bvol + j));
         }
       }
     }
@@ -389,3 +389,7 @@ extern "C" int tlgb_fold(const tlgb_blocks_desc* d, const void* blocks, void* ar
     default: return launch_fold<double2>(g, d->mask_inv, blocks, array, s);
   }
 }
+
+namespace tlgb {
+int blocks_checked_status(int* line, int clear) { return checked_status(line, clear); }
+}  // namespace tlgb

@@ -69,4 +69,37 @@ int conv_device_status(int* v, int clear);
 // Streaming multiprocessors of the current device (cached per device).
 int sm_count();
 
+// Debug builds (-DTLGB_CHECKED, the library libtlgb_checked.so) range-check
+// the index of selected global and shared-memory accesses: an index outside
+// [0, n) sets this translation unit's checked-failure word to the source line
+// (the first one wins) and the access is skipped. tlgb_device_status reports
+// such a failure as bit 4. Release builds compile the checks away.
+#ifdef TLGB_CHECKED
+static __device__ int g_tlgb_checked_line;
+static __device__ __forceinline__ bool checked_index(long long i, long long n, int line) {
+  if (i >= 0 && i < n) return true;
+  atomicCAS(&g_tlgb_checked_line, 0, line);
+  return false;
+}
+#define TLGB_IN_RANGE(i, n) (::tlgb::checked_index((long long)(i), (long long)(n), __LINE__))
+// this translation unit's failure word (0 = none), read and optionally cleared
+static inline int checked_status(int* line, int clear) {
+  TLGB_CUDA(cudaMemcpyFromSymbol(line, g_tlgb_checked_line, sizeof(int)));
+  if (clear) {
+    const int z = 0;
+    TLGB_CUDA(cudaMemcpyToSymbol(g_tlgb_checked_line, &z, sizeof(int)));
+  }
+  return TLGB_OK;
+}
+#else
+#define TLGB_IN_RANGE(i, n) true
+static inline int checked_status(int* line, int) {
+  *line = 0;
+  return TLGB_OK;
+}
+#endif
+
+// The blocks translation unit's checked-failure word (see above).
+int blocks_checked_status(int* line, int clear);
+
 }  // namespace tlgb

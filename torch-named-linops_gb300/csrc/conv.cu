@@ -28,11 +28,6 @@ constexpr int kTaps = 27;
 // row addresses of one ldmatrix phase fall in distinct banks
 __device__ __forceinline__ uint32_t swz(int j, int c) { return (uint32_t)(j * 32 + ((c ^ ((j >> 2) & 1)) << 4)); }
 
-__device__ __forceinline__ void ldsm_x4(uint32_t addr, uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3) {
-  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];"
-               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
-               : "r"(addr));
-}
 __device__ __forceinline__ void ldsm_x4_t(uint32_t addr, uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3) {
   asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0, %1, %2, %3}, [%4];"
                : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
@@ -63,71 +58,6 @@ __device__ __forceinline__ void load_halo(unsigned char* halo, const uint4* __re
     if (di >= 0 && di < D && hi >= 0 && hi < H && wi >= 0 && wi < W)
       v = __ldg(x + ((((long long)di * H + hi) * W + wi) * 2 + c));
     *reinterpret_cast<uint4*>(halo + r * kHaloW * kVoxBytes + swz(j, c)) = v;
-  }
-}
-
-// MODE 0: plain; 1: ReLU; 2: multiply by (aux > 0) (the ReLU mask of a
-// forward output, for the data gradient). OUTF32: float32 output.
-template <int MODE, bool OUTF32>
-__global__ void __launch_bounds__(128) conv3d_fwd_kernel(int D, int H, int W, const uint4* __restrict__ x,
-                                                         const uint4* __restrict__ wts,
-                                                         const __nv_bfloat16* __restrict__ aux, void* __restrict__ y) {
-  __shared__ __align__(128) unsigned char halo[kHaloRows * kHaloW * kVoxBytes];
-  __shared__ __align__(128) unsigned char wsm[kTaps * 16 * kVoxBytes];
-  const int w0 = blockIdx.x * kTileW, h = blockIdx.y, d = blockIdx.z;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  load_halo(halo, x, D, H, W, d, h, w0);
-  for (int i = threadIdx.x; i < kTaps * 16 * 2; i += blockDim.x) {
-    const int c = i & 1, n = (i >> 1) & 15, t = i >> 5;
-    *reinterpret_cast<uint4*>(wsm + t * 16 * kVoxBytes + swz(n, c)) = __ldg(wts + i);
-  }
-  __syncthreads();
-
-  float acc[2][4];
-#pragma unroll
-  for (int i = 0; i < 2; ++i)
-#pragma unroll
-    for (int k = 0; k < 4; ++k) acc[i][k] = 0.f;
-  // ldmatrix row roles: A (16 voxels x 16 ch): row = voxel, chunk = k half;
-  // B (16 out x 16 in, stored [n][k]): row = n
-  const int a_row = (lane & 7) + 8 * ((lane >> 3) & 1), a_chunk = lane >> 4;
-  const int b_row = (lane & 7) + 8 * (lane >> 4), b_chunk = (lane >> 3) & 1;
-  const uint32_t hbase = smem_addr(halo), wbase = smem_addr(wsm);
-#pragma unroll 1
-  for (int t = 0; t < kTaps; ++t) {
-    const int r = t / 3, kw = t % 3;
-    uint32_t a0, a1, a2, a3, b0, b1, b2, b3;
-    ldsm_x4(hbase + r * kHaloW * kVoxBytes + swz(warp * 16 + kw + a_row, a_chunk), a0, a1, a2, a3);
-    ldsm_x4(wbase + t * 16 * kVoxBytes + swz(b_row, b_chunk), b0, b1, b2, b3);
-    mma_bf16(acc[0], a0, a1, a2, a3, b0, b1);
-    mma_bf16(acc[1], a0, a1, a2, a3, b2, b3);
-  }
-  // D fragment: rows gid, gid + 8 (voxels), columns 2*tig, 2*tig + 1 (+ 8 for chunk 1)
-  const int gid = lane >> 2, tig = lane & 3;
-#pragma unroll
-  for (int hr = 0; hr < 2; ++hr) {
-    const int w = w0 + warp * 16 + gid + 8 * hr;
-    if (w >= W) continue;
-    const long long v = ((long long)d * H + h) * W + w;
-#pragma unroll
-    for (int ch = 0; ch < 2; ++ch) {
-      const int co = ch * 8 + 2 * tig;
-      float y0 = acc[ch][2 * hr], y1 = acc[ch][2 * hr + 1];
-      if (MODE == 1) {
-        y0 = fmaxf(y0, 0.f);
-        y1 = fmaxf(y1, 0.f);
-      } else if (MODE == 2) {
-        const __nv_bfloat162 m = *reinterpret_cast<const __nv_bfloat162*>(aux + v * 16 + co);
-        y0 = __bfloat162float(m.x) > 0.f ? y0 : 0.f;
-        y1 = __bfloat162float(m.y) > 0.f ? y1 : 0.f;
-      }
-      if (OUTF32) {
-        *reinterpret_cast<float2*>(reinterpret_cast<float*>(y) + v * 16 + co) = make_float2(y0, y1);
-      } else {
-        *reinterpret_cast<__nv_bfloat162*>(reinterpret_cast<__nv_bfloat16*>(y) + v * 16 + co) =
-            __floats2bfloat162_rn(y0, y1);
-      }
-    }
   }
 }
 
@@ -479,24 +409,8 @@ extern "C" int tlgb_conv3d_fwd(const tlgb_conv3d_desc* d, const void* x, const v
     if (d->mode == 1) return launch_conv_tc<1, false>(d, map, w, aux, y, s);
     return launch_conv_tc<2, false>(d, map, w, aux, y, s);
   }
-  // no tensor-map encoder from the driver: the mma.sync kernel
-  dim3 grid((unsigned)((d->W + kTileW - 1) / kTileW), (unsigned)d->H, (unsigned)d->D);
-  const uint4* xp = (const uint4*)x;
-  const uint4* wp = (const uint4*)w;
-  const __nv_bfloat16* ap = (const __nv_bfloat16*)aux;
-#define TLGB_CONV_LAUNCH(M, F) conv3d_fwd_kernel<M, F><<<grid, 128, 0, s>>>(d->D, d->H, d->W, xp, wp, ap, y)
-  if (d->out_f32) {
-    if (d->mode == 0) TLGB_CONV_LAUNCH(0, true);
-    else if (d->mode == 1) TLGB_CONV_LAUNCH(1, true);
-    else TLGB_CONV_LAUNCH(2, true);
-  } else {
-    if (d->mode == 0) TLGB_CONV_LAUNCH(0, false);
-    else if (d->mode == 1) TLGB_CONV_LAUNCH(1, false);
-    else TLGB_CONV_LAUNCH(2, false);
-  }
-#undef TLGB_CONV_LAUNCH
-  TLGB_CHECK_LAUNCH();
-  return TLGB_OK;
+  TLGB_FAIL(TLGB_ERR_UNSUPPORTED,
+            "conv3d: the driver offers no tensor-map encoder, which the TMA-fed tcgen05 kernel needs");
 }
 
 extern "C" int tlgb_conv3d_wgrad_scratch_size(const tlgb_conv3d_desc* d, size_t* bytes) {

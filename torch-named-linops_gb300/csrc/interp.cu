@@ -32,6 +32,7 @@
 //    evaluations per point visit are shared by every batch entry of the visit.
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <mutex>
 #include <numeric>
@@ -65,6 +66,7 @@ struct Geo {
   long long npts, nbatch;
   int wrap_safe;  // every active N >= NT: a window never overlaps itself
   long long tv_off;  // gridding: byte offset in scratch of the point-major values, -1 = none
+  int skip_copy;     // test hook (tlgb_test_skip_region_copy): TMA kernels skip their region copy
 };
 
 // ---------------------------------------------------------------- kernels math
@@ -1248,7 +1250,7 @@ __global__ void __launch_bounds__(256, 4) adj_f3_kernel(Geo g, const int4* __res
       // zero weights would not keep a NaN or Inf out of the other cells.
       unsigned view = 0;
       bool finite = true;
-      if (tid < nb) {
+      if (tid < nb && TLGB_IN_RANGE(entries[b + tid], g.npts)) {
         const int p = entries[b + tid];
         const PRec R = load_prec(precs, p);
         float4 v[4];
@@ -1722,8 +1724,10 @@ __global__ void __launch_bounds__(256, 2) fwd_f3_kernel(const __grid_constant__ 
     }
     __syncthreads();
     if (tid == 0) {
-      mbar_arrive_expect_tx(bar, RBYTES);
-      tma_load_4d(reg, &tmap, bar, o[2], o[1], o[0], c0);
+      if (!g.skip_copy) {  // test hook: nothing in flight, so the bounded wait runs out
+        mbar_arrive_expect_tx(bar, RBYTES);
+        tma_load_4d(reg, &tmap, bar, o[2], o[1], o[0], c0);
+      }
     }
   } else {
     // plain loads with wrap / zero fill: rows (entry, x, y) of 12 z
@@ -1797,7 +1801,7 @@ __global__ void __launch_bounds__(256, 2) fwd_f3_kernel(const __grid_constant__ 
     // the copy must have landed: one thread polls (bounded), the others
     // wait at the barrier without taking issue slots; then a CTA-wide vote
     bool ok = true;
-    if (tma && tid == 0) ok = mbar_wait_bounded(bar, 0, 1u << 22);
+    if (tma && tid == 0) ok = mbar_wait_bounded(bar, 0, g.skip_copy ? 1u : 1u << 22);
     if (__syncthreads_or(!ok)) {
       if (tid == 0) atomicExch(&g_tlgb_status, 1);
       return;
@@ -1813,6 +1817,8 @@ __global__ void __launch_bounds__(256, 2) fwd_f3_kernel(const __grid_constant__ 
       const float wz = (&R.w[2].x)[kz];
       const float* wy = &R.w[1].x;
       const float2* a = reg + c * VOL + (R.view & 2047) + kz;
+      // the box's farthest cell: 3 x, 3 y and the last z lane from the base
+      if (!TLGB_IN_RANGE((R.view & 2047) + kz + 3 * PLANE + 3 * S, VOL)) return make_float2(0.f, 0.f);
       float2 acc = make_float2(0.f, 0.f);
 #pragma unroll
       for (int t = 0; t < 4; ++t) {
@@ -1842,7 +1848,8 @@ __global__ void __launch_bounds__(256, 2) fwd_f3_kernel(const __grid_constant__ 
           for (int kx = 0; kx < Sr.m[0]; ++kx) {
             const float w = g.norm == 1 ? Sr.wv[0][kx] * Sr.wv[1][kyy] * Sr.wv[2][kzz]
                                         : radial_w(g, Sr.wv[0][kx], Sr.wv[1][kyy], Sr.wv[2][kzz]);
-            fma2_bcast(acc, w, reg[c * VOL + (Sr.lc[0][kx] * S + Sr.lc[1][kyy]) * S + Sr.lc[2][kzz]]);
+            const int ri = c * VOL + (Sr.lc[0][kx] * S + Sr.lc[1][kyy]) * S + Sr.lc[2][kzz];
+            if (TLGB_IN_RANGE(ri, CG * VOL)) fma2_bcast(acc, w, reg[ri]);
           }
       __syncwarp();
       return acc;
@@ -1853,7 +1860,7 @@ __global__ void __launch_bounds__(256, 2) fwd_f3_kernel(const __grid_constant__ 
       acc.y += __shfl_xor_sync(0xffffffffu, acc.y, 1);
       acc.x += __shfl_xor_sync(0xffffffffu, acc.x, 2);
       acc.y += __shfl_xor_sync(0xffffffffu, acc.y, 2);
-      if (kz == 0 && c0 + c < g.nbatch)
+      if (kz == 0 && c0 + c < g.nbatch && TLGB_IN_RANGE(p, g.npts))
         *reinterpret_cast<float2*>(out + ((long long)(c0 + c) * g.npts + p) * 2) = acc;
     };
     auto one = [&](const R3& R) {
@@ -1946,8 +1953,10 @@ __global__ void __launch_bounds__(256, 3) fwd_f2_kernel(const __grid_constant__ 
     }
     __syncthreads();
     if (tid == 0) {
-      mbar_arrive_expect_tx(bar, RBYTES);
-      tma_load_4d(reg, &tmap, bar, o[2], o[1], 0, c0);
+      if (!g.skip_copy) {  // test hook: nothing in flight, so the bounded wait runs out
+        mbar_arrive_expect_tx(bar, RBYTES);
+        tma_load_4d(reg, &tmap, bar, o[2], o[1], 0, c0);
+      }
     }
   } else {
     // plain loads with wrap / zero fill: rows (entry, y) of 20 z
@@ -2011,7 +2020,7 @@ __global__ void __launch_bounds__(256, 3) fwd_f2_kernel(const __grid_constant__ 
   build_records(warp);  // while the region copy is in flight
   {
     bool ok = true;
-    if (tma && tid == 0) ok = mbar_wait_bounded(bar, 0, 1u << 22);
+    if (tma && tid == 0) ok = mbar_wait_bounded(bar, 0, g.skip_copy ? 1u : 1u << 22);
     if (__syncthreads_or(!ok)) {
       if (tid == 0) atomicExch(&g_tlgb_status, 1);
       return;
@@ -2046,7 +2055,8 @@ __global__ void __launch_bounds__(256, 3) fwd_f2_kernel(const __grid_constant__ 
       for (int kzz = kz; kzz < Sr.m[2]; kzz += 4)
         for (int kyy = 0; kyy < Sr.m[1]; ++kyy) {
           const float w = Sr.wv[1][kyy] * Sr.wv[2][kzz];
-          const float2 v = reg[c * VOL + Sr.lc[1][kyy] * S + Sr.lc[2][kzz]];
+          const int ri = c * VOL + Sr.lc[1][kyy] * S + Sr.lc[2][kzz];
+          const float2 v = TLGB_IN_RANGE(ri, CG * VOL) ? reg[ri] : make_float2(0.f, 0.f);
           acc.x = fmaf(w, v.x, acc.x);
           acc.y = fmaf(w, v.y, acc.y);
         }
@@ -2368,8 +2378,10 @@ __global__ void __launch_bounds__(256, 3) grad_f2_kernel(const __grid_constant__
     }
     __syncthreads();
     if (tid == 0) {
-      mbar_arrive_expect_tx(bar, RBYTES);
-      tma_load_4d(reg, &tmap, bar, o[2], o[1], 0, c0);
+      if (!g.skip_copy) {  // test hook: nothing in flight, so the bounded wait runs out
+        mbar_arrive_expect_tx(bar, RBYTES);
+        tma_load_4d(reg, &tmap, bar, o[2], o[1], 0, c0);
+      }
     }
   } else {
     const int ncoil = (int)min((long long)CG, g.nbatch - c0);
@@ -2426,7 +2438,7 @@ __global__ void __launch_bounds__(256, 3) grad_f2_kernel(const __grid_constant__
   build_records(warp);  // while the region copy is in flight
   {
     bool ok = true;
-    if (tma && tid == 0) ok = mbar_wait_bounded(bar, 0, 1u << 22);
+    if (tma && tid == 0) ok = mbar_wait_bounded(bar, 0, g.skip_copy ? 1u : 1u << 22);
     if (__syncthreads_or(!ok)) {
       if (tid == 0) atomicExch(&g_tlgb_status, 1);
       return;
@@ -2482,7 +2494,8 @@ __global__ void __launch_bounds__(256, 3) grad_f2_kernel(const __grid_constant__
               int zz = l2 + kc;
               if (g.pad == TLGB_PAD_CIRCULAR && zz < 0) zz += g.N[2];
               if (yy < 0 || yy >= S || zz < 0 || zz >= S) continue;
-              const float2 v = reg[c * VOL + yy * S + zz];
+              const int ri = c * VOL + yy * S + zz;
+              const float2 v = TLGB_IN_RANGE(ri, 8 * VOL) ? reg[ri] : make_float2(0.f, 0.f);
               const float a1 = pt.dw[1][kb] * pt.w[2][kc], a2 = pt.w[1][kb] * pt.dw[2][kc];
               gy.x = fmaf(a1, v.x, gy.x);
               gy.y = fmaf(a1, v.y, gy.y);
@@ -2511,6 +2524,8 @@ struct PlanLayout {
 constexpr int64_t kFwdChunk = 512;
 constexpr int64_t kAdjChunk = 1024;
 
+std::atomic<int> g_test_skip_copy{0};  // tlgb_test_skip_region_copy
+
 int make_geo(const tlgb_interp_desc* d, Geo& g) {
   if (!d) TLGB_FAIL(TLGB_ERR_INVALID, "null interp descriptor");
   if (d->ndim < 1 || d->ndim > 3) TLGB_FAIL(TLGB_ERR_INVALID, "ndim must be 1, 2 or 3");
@@ -2523,6 +2538,7 @@ int make_geo(const tlgb_interp_desc* d, Geo& g) {
   if (d->nbatch > TLGB_INTERP_MAX_BATCH)
     TLGB_FAIL(TLGB_ERR_UNSUPPORTED, "batch above 524280 entries in one call: split the batch");
   memset(&g, 0, sizeof(g));
+  g.skip_copy = g_test_skip_copy.load();
   g.ndim = d->ndim;
   const int off = 3 - d->ndim;
   int maxnt = 1;
@@ -2657,7 +2673,18 @@ int64_t region_vol(const Geo& g) {
 }
 
 // batch entries staged per forward CTA
+bool fast3(const Geo& g, int cg);
+bool fast2(const Geo& g, int cg);
+
+// A batch of fewer than 8 entries on a geometry of the dedicated 8-entry
+// kernels (3D 8^3 or 2D 16 x 16 tiles, width in (3, 4], norm 1, complex) runs
+// on them as one group: the missing entries are staged as zeros and never
+// written. Those kernels stage each point once for all entries, so even one
+// entry runs faster there than on the generic kernels.
+bool small_batch_on_fast_kernels(const Geo& g) { return g.nbatch < 8 && (fast3(g, 8) || fast2(g, 8)); }
+
 int fwd_cg(const Geo& g) {
+  if (small_batch_on_fast_kernels(g)) return 8;
   int cg = (int)std::min<long long>(std::max<long long>(g.nbatch, 1), CGMAX);
   const int64_t cap = 220 * 1024 - NWF * 32 * (int64_t)pt_bytes(ntb_for(g));
   while (cg > 1 && region_vol(g) * cg * value_size(g) > cap) --cg;
@@ -2668,7 +2695,10 @@ size_t fwd_smem(const Geo& g, int cg) {
   return align_up((size_t)region_vol(g) * cg * value_size(g), 16) + NWF * 32 * pt_bytes(ntb_for(g));
 }
 
-int adj_cg(const Geo& g) { return (int)std::min<long long>(std::max<long long>(g.nbatch, 1), CGMAX); }
+int adj_cg(const Geo& g) {
+  if (small_batch_on_fast_kernels(g)) return 8;
+  return (int)std::min<long long>(std::max<long long>(g.nbatch, 1), CGMAX);
+}
 
 int64_t tile_floats(const Geo& g, int cg) {
   return ((int64_t)g.T[0] * g.T[1] * g.T[2] * cg * (g.cplx ? 2 : 1) + 3) & ~3ll;
@@ -3355,6 +3385,10 @@ extern "C" int tlgb_interp_adjoint_fixed(const tlgb_interp_desc* d, const tlgb_i
   return launch_adj(g, info, (const char*)plan, locs, vals, grid, scratch, (cudaStream_t)stream);
 }
 
+extern "C" int tlgb_test_skip_region_copy(int32_t on) {
+  return tlgb::g_test_skip_copy.exchange(on ? 1 : 0);
+}
+
 extern "C" int tlgb_device_status(int32_t* status, int32_t clear) {
   if (status == nullptr) TLGB_FAIL(TLGB_ERR_INVALID, "status is NULL");
   int v = 0;
@@ -3366,6 +3400,10 @@ extern "C" int tlgb_device_status(int32_t* status, int32_t clear) {
   }
   int vc = 0;
   TLGB_TRY(tlgb::conv_device_status(&vc, clear));
-  *status = v | vc;
+  // debug builds: an index outside its range in a checked access (bit 4)
+  int li = 0, lb = 0;
+  TLGB_TRY(tlgb::checked_status(&li, clear));
+  TLGB_TRY(tlgb::blocks_checked_status(&lb, clear));
+  *status = v | vc | ((li | lb) ? 4 : 0);
   return TLGB_OK;
 }

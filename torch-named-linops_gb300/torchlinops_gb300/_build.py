@@ -25,6 +25,10 @@ INCLUDE = os.path.join(REPO_DIR, "include")
 BUILD_DIR = os.path.join(PROJECT_DIR, "_build")
 LIB_DIR = os.path.join(PKG_DIR, "_lib")
 LIB_PATH = os.path.join(LIB_DIR, "libtlgb.so")
+# debug variant: selected global and shared-memory indices range-checked
+# (-DTLGB_CHECKED); a failed check is reported by tlgb_device_status (bit 4)
+CHECKED_BUILD_DIR = os.path.join(PROJECT_DIR, "_build_checked")
+CHECKED_LIB_PATH = os.path.join(LIB_DIR, "libtlgb_checked.so")
 
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
@@ -62,18 +66,22 @@ def _stale(target: str, deps) -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(verbose: bool = False, jobs: int | None = None) -> str:
-    """Build libtlgb.so if any source or header is newer; return its path."""
-    os.makedirs(BUILD_DIR, exist_ok=True)
+def build(verbose: bool = False, jobs: int | None = None, checked: bool = False) -> str:
+    """Build libtlgb.so (or, with ``checked``, the range-checked debug variant
+    libtlgb_checked.so) if any source or header is newer; return its path."""
+    build_dir = CHECKED_BUILD_DIR if checked else BUILD_DIR
+    lib_path = CHECKED_LIB_PATH if checked else LIB_PATH
+    flags = NVCC_FLAGS + (["-DTLGB_CHECKED"] if checked else [])
+    os.makedirs(build_dir, exist_ok=True)
     os.makedirs(LIB_DIR, exist_ok=True)
     nvcc = _nvcc()
     headers = _headers()
     objs, todo = [], []
     for src in _sources():
-        obj = os.path.join(BUILD_DIR, os.path.basename(src)[:-3] + ".o")
+        obj = os.path.join(build_dir, os.path.basename(src)[:-3] + ".o")
         objs.append(obj)
         if _stale(obj, [src] + headers):
-            cmd = [nvcc, *ARCH_FLAGS, *NVCC_FLAGS, "-I", INCLUDE, "-I", CSRC, "-c", src, "-o", obj]
+            cmd = [nvcc, *ARCH_FLAGS, *flags, "-I", INCLUDE, "-I", CSRC, "-c", src, "-o", obj]
             todo.append(cmd)
 
     def run(cmd):
@@ -89,13 +97,13 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
             for out in ex.map(run, todo):
                 if verbose and out:
                     print(out)
-    if todo or _stale(LIB_PATH, objs):
-        tmp = LIB_PATH + ".tmp"
+    if todo or _stale(lib_path, objs):
+        tmp = lib_path + ".tmp"
         cmd = [nvcc, *ARCH_FLAGS, "-shared", "-o", tmp, *objs]
         run(cmd)
-        os.replace(tmp, LIB_PATH)
-    return LIB_PATH
+        os.replace(tmp, lib_path)
+    return lib_path
 
 
 if __name__ == "__main__":
-    print(build(verbose="-v" in sys.argv))
+    print(build(verbose="-v" in sys.argv, checked="--checked" in sys.argv))

@@ -139,6 +139,7 @@ _SIGNATURES = {
     "tlgb_last_error": ([], ctypes.c_char_p),
     "tlgb_version": ([], ctypes.c_int),
     "tlgb_device_status": ([ctypes.POINTER(ctypes.c_int32), ctypes.c_int32], ctypes.c_int),
+    "tlgb_test_skip_region_copy": ([ctypes.c_int32], ctypes.c_int),
     "tlgb_interp_plan_size": ([_P, _P, _P], ctypes.c_int),
     "tlgb_interp_plan_build": ([_P, _P, _P, ctypes.c_size_t, _P, ctypes.c_size_t, _P, _P], ctypes.c_int),
     "tlgb_interp_adjoint_scratch_size": ([_P, _P, _P], ctypes.c_int),
