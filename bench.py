@@ -202,6 +202,89 @@ class CpuSample:
         }
 
 
+def _median_time(fn, reps: int, warmup: int = 1) -> float:
+    for _ in range(warmup):
+        fn()
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        fn()
+        ts.append(time.perf_counter() - t0)
+    return statistics.median(ts)
+
+
+def cpu_config_baselines():
+    """The other workloads' CPU baselines: the oracle (the reference's torch
+    path restated) on the host cores, each a bounded sample stated beside
+    its figure, scaled to the whole workload where the sample is a fixed
+    fraction of it (about 20 s in all)."""
+    from oracle import blocks as OB
+    from oracle import cg as OCG
+    from oracle import interp as OI
+    from oracle import nufft as ONU
+    from torchlinops_gb300 import mri
+
+    threads = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+    torch.set_num_threads(threads)
+    out = {"cores": threads, "kind": "port"}
+    # plain 2D interpolate, 64^2, 4096 points, W 4, beta for oversampling 1.25 (the whole workload)
+    g = torch.Generator().manual_seed(0)
+    img = torch.complex(torch.randn(64, 64, generator=g), torch.randn(64, 64, generator=g))
+    locs = torch.rand(4096, 2, generator=g) * 64
+    pts = torch.complex(torch.randn(4096, generator=g), torch.randn(4096, generator=g))
+    beta = kb_beta()
+    f = _median_time(lambda: OI.ungrid(img, locs, 4.0, beta=beta), 10, 3)
+    a = _median_time(lambda: OI.grid(pts, locs, (64, 64), 4.0, beta=beta), 10, 3)
+    out["interp2d_64sq_4096pts"] = {"fwd_ms": f * 1e3, "adj_ms": a * 1e3, "sample": "whole workload, median of 10"}
+    # unfold / fold 16 x 160^3 c64, block 8^3, stride 4: one of the 16 batch entries, times 16
+    x = torch.complex(torch.randn(1, 160, 160, 160, generator=g), torch.randn(1, 160, 160, 160, generator=g))
+    u = _median_time(lambda: OB.unfold(x, BLK, BLK_STRIDE), 3)
+    y = OB.unfold(x, BLK, BLK_STRIDE)
+    fo = _median_time(lambda: OB.fold(y, BLK_SHAPE[1:], BLK, BLK_STRIDE), 1, 0)
+    del x, y
+    out["blocks3d_16x160cube"] = {"unfold_ms": 16 * u * 1e3, "fold_ms": 16 * fo * 1e3,
+                                  "sample": "1 of 16 batch entries (unfold median of 3, fold one run), scaled by 16"}
+    # 2D NUFFT forward / adjoint (float32 arithmetic): 1 of 32 slices x 8 coils, times 32
+    SP, RD, N = 402, 512, 256
+    ang = torch.arange(SP, dtype=torch.float64) * math.pi * (math.sqrt(5.0) - 1.0) / 2.0
+    r = (torch.arange(RD, dtype=torch.float64) - RD // 2) * (N / RD)
+    l2 = torch.stack([r[None, :] * torch.cos(ang[:, None]), r[None, :] * torch.sin(ang[:, None])], dim=-1)
+    l2 = (l2 + 0.1 * torch.randn(l2.shape, generator=g, dtype=torch.float64)).to(torch.float32)
+    xi = torch.complex(torch.randn(8, N, N, generator=g), torch.randn(8, N, N, generator=g))
+    ys = torch.complex(torch.randn(8, SP, RD, generator=g), torch.randn(8, SP, RD, generator=g))
+    nf = _median_time(lambda: ONU.nufft(xi, l2, dtype=torch.float32), 3)
+    na = _median_time(lambda: ONU.nufft_adjoint(ys, l2, (N, N), dtype=torch.float32), 3)
+    out["nufft2d_32x8x256sq"] = {"fwd_ms": 32 * nf * 1e3, "adj_ms": 32 * na * 1e3,
+                                 "sample": "1 of 32 slices (8 coils), median of 3, scaled by 32"}
+    # plain CG to 1e-4 on a reduced normal equation of the same kind: 32^3
+    # image, 1 coil, 1024 x 64 Fibonacci-sphere radial points, the data term
+    # scaled to a unit largest eigenvalue (power method) plus lam 1e-3, float64
+    # (the CG workload itself is 128^3 x 8 coils x 2^20 points)
+    n5 = 32
+    l5 = mri.radial_trajectory_3d(1024, 64, n5, "cpu")
+
+    def data(v):
+        return ONU.nufft_adjoint(ONU.nufft(v, l5), l5, (n5,) * 3)
+
+    v = torch.complex(torch.randn(n5, n5, n5, generator=g), torch.randn(n5, n5, n5, generator=g)).to(torch.complex128)
+    for _ in range(15):
+        v = data(v)
+        v = v / torch.linalg.vector_norm(v)
+    scale = 1.0 / float(torch.vdot(v.flatten(), data(v).flatten()).real)
+    xt = torch.complex(torch.randn(n5, n5, n5, generator=g), torch.randn(n5, n5, n5, generator=g)).to(torch.complex128)
+
+    def normal(w):
+        return scale * data(w) + 1e-3 * w
+
+    b = normal(xt)
+    t0 = time.perf_counter()
+    _, iters = OCG.cg(normal, b, rtol=1e-4, max_iters=300)
+    out["cg_sense_reduced"] = {"seconds": time.perf_counter() - t0, "iters": iters,
+                               "sample": "32^3 image, 1 coil, 65,536 radial points, unit-normalised data term + "
+                                         "1e-3 I, float64, plain CG to relative residual 1e-4"}
+    return out
+
+
 def cpu_baseline(sample_pts: int, reps: int = 3):
     cs = CpuSample(sample_pts)
     cs.run()  # warm-up
@@ -212,11 +295,11 @@ def cpu_baseline(sample_pts: int, reps: int = 3):
 def run_reference(args, world, rank):
     if rank != 0:
         return
-    cs = CpuSample(args.ref_sample)
+    cs = CpuSample(args.ref_points)
     per = [cs.run() for _ in range(args.warmup + args.steps)]
     timed = per[args.warmup:]
     t = statistics.median(timed)
-    value = 2 * args.ref_sample * N_COIL / t
+    value = 2 * args.ref_points * N_COIL / t
     desc = cs.describe(t, len(timed))
     line = {
         "impl": "reference",
@@ -233,7 +316,7 @@ def run_reference(args, world, rank):
         "dtype": "c64",
         "data": "synthetic (1/r^2 ball trajectory, N(0,1) complex values), seeded",
         "config": {"workload": f"interp3d_{N_GRID}cube_{N_COIL}coil_{N_PTS}pts", "grid": [N_GRID] * 3, "coils": N_COIL,
-                   "points": N_PTS, "width": WIDTH, "oversamp": OVERSAMP, "sample_points": args.ref_sample,
+                   "points": N_PTS, "width": WIDTH, "oversamp": OVERSAMP, "sample_points": args.ref_points,
                    "step": "ungrid + grid of the sample points on the CPU (reference torch path, restated)",
                    "device": "host CPU"},
         "cpu_baseline": {k: desc[k] for k in ("cores", "kind", "sample")} | {"value": value, "unit": "point-coil samples/s"},
@@ -354,11 +437,14 @@ def run_gpu(args, world, rank, local):
         kernels.update(bench_blocks(dev, peak, args))
     if not args.skip_nufft2d:
         kernels["nufft2d"] = bench_nufft2d(dev, peak)
+    if not args.skip_blocks:
+        kernels["index"] = bench_index(dev, peak)
     line = None
     if rank == 0:
-        cpu = None
+        cpu = cpu_others = None
         if world == 1 and not args.skip_cpu:
             cpu = cpu_baseline(args.ref_sample)
+            cpu_others = cpu_config_baselines()
         cg = None
         if world == 1 and not args.skip_cg:
             cg = bench_cg(dev, args)
@@ -406,6 +492,7 @@ def run_gpu(args, world, rank, local):
                 "algorithmic_bytes_per_launch": ALGO_BYTES,
             },
             "cpu_baseline": cpu,
+            "cpu_baselines_other_workloads": cpu_others,
             "clocks": clocks,
             "gpu_launches": launches_per_step * args.steps,
             "kernels": kernels,
@@ -504,7 +591,18 @@ def bench_nufft2d(dev, peak):
     f_ms, fb_ms, fbl_ms = timed(fwd), timed(fwd_bwd_image), timed(fwd_bwd_both)
     # one ungrid of this workload: grid 256 x 320^2 c64 + locs + 256 x 205,824 c64 values
     ungrid_bytes = S * C * 320 * 320 * 8 + SP * RD * 2 * 4 + S * C * SP * RD * 8
-    del x, a, xg, lg
+    # the trajectory-gradient kernel alone, on the padded grid and the point
+    # cotangents of this workload: reads the 256 x 320^2 grid, the 256 x
+    # 205,824 point values and the locations, writes the gradient
+    from torchlinops_gb300 import interp as I
+
+    kl = linops.prep_locs(locs, (N, N), (320, 320))
+    gk = torch.randn(S * C, 320, 320, dtype=torch.complex64, device=dev, generator=gd)
+    beta = I.kaiser_bessel_beta(4.0, 1.25)
+    grad_ms = timed(lambda: I._grad_locs(gk, a.reshape(S * C, SP, RD), kl, 4.0, "kaiser_bessel", 1, "circular",
+                                         dict(beta=beta)))
+    grad_bytes = S * C * 320 * 320 * 8 + S * C * SP * RD * 8 + 2 * SP * RD * 2 * 4
+    del x, a, xg, lg, gk
     torch.cuda.empty_cache()
     return {
         "workload": "32 slices x 8 coils x 256^2 c64, padded 320^2, golden-angle radial 402 x 512 (+N(0,0.1) jitter)",
@@ -513,6 +611,9 @@ def bench_nufft2d(dev, peak):
         "fwd_bwd_image_and_locs_ms": fbl_ms,
         "ungrid_algorithmic_bytes": ungrid_bytes,
         "samples_per_s_fwd": S * C * SP * RD / (f_ms / 1e3),
+        "grad_locs_kernel": {"ms": grad_ms, "algorithmic_bytes": grad_bytes,
+                             "GBps": grad_bytes / (grad_ms / 1e3) / 1e9,
+                             "frac": grad_bytes / (grad_ms / 1e3) / 1e9 / peak},
     }
 
 
@@ -549,6 +650,7 @@ def bench_cg(dev, args):
                 "true_rel_residual": best.true_rel_residual, "fallback": best.fallback}
 
     normal_ms = timed(lambda: A(b))
+    toeplitz = bench_toeplitz(locs, maps, xt, n, dev)
     plain = solve(None)
     M = precond.CNNPreconditioner(dev, seed=1, init="laplacian", c0=0.02)
     warm = solve(M)
@@ -558,21 +660,143 @@ def bench_cg(dev, args):
                 log_every=max(args.cg_steps // 10, 1))
     learned = solve(M)
     m_ms = timed(lambda: M(b))
+    compare = None
+    if args.precond_compare:
+        # the same network and step count trained on solutions that plain CG
+        # generates (phantoms + noise, CG to 1e-6) instead of (A e, e) pairs
+        t0 = time.perf_counter()
+        pairs = mri.cg_solution_pairs(A, n, args.precond_compare, seed=5000, device=dev)
+        gen_s = time.perf_counter() - t0
+        M2 = precond.CNNPreconditioner(dev, seed=1, init="laplacian", c0=0.02)
+        gen2 = torch.Generator().manual_seed(0)
+
+        def cg_batch(step):
+            idx = torch.randint(0, len(pairs), (batch,), generator=gen2)
+            return [pairs[int(i)] for i in idx]
+
+        log2 = M2.fit(cg_batch, args.cg_steps, lr=1e-3)
+        learned2 = solve(M2)
+        compare = {"cg_solved_phantoms": args.precond_compare, "generation_seconds": gen_s,
+                   "train_seconds": log2.seconds, "learned": learned2,
+                   "speedup_wall": plain["seconds"] / learned2["seconds"],
+                   "speedup_iters": plain["iters"] / learned2["iters"]}
+        del pairs, M2
     return {
         "workload": f"sense3d_{n}cube_{ncoil}coil_{nspokes}x{nread}radial_lam{lam:g}",
         "rtol": 1e-4,
         "normal_op_ms": normal_ms,
+        "toeplitz": toeplitz,
         "preconditioner_ms": m_ms,
         "plain": plain,
         "warm_start": warm,
         "learned": learned,
         "speedup_wall": plain["seconds"] / learned["seconds"],
         "speedup_iters": plain["iters"] / learned["iters"],
+        "trained_on_cg_solutions": compare,
         "train": {"steps": args.cg_steps, "samples": args.cg_steps * batch, "seconds": log.seconds,
                   "loss_first": log.losses[0][1] if log.losses else None,
                   "loss_last": log.losses[-1][1] if log.losses else None},
         "data": "synthetic: ellipsoid phantom, Gaussian coil maps, Fibonacci-sphere radial trajectory, seeded",
     }
+
+
+def bench_toeplitz(locs, maps, xt, n, dev):
+    """The NUFFT normal operator on the 8 coil images S_c x of the CG workload
+    (128^3, 2^20 radial points): its Toeplitz embedding (PSF kernel on the 2x
+    grid, built once; then pad + FFT + multiply + inverse FFT + crop) against
+    the explicit chain (forward NUFFT then adjoint), each the median of 5
+    CUDA-event timings, and the two results' relative difference."""
+    from torchlinops_gb300 import linops
+
+    x8 = (maps * xt[None]).contiguous()
+    s = torch.cuda.current_stream(dev)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    T = linops.NUFFT(locs, (n,) * 3, toeplitz=True).normal()
+    T(x8[:1])
+    torch.cuda.synchronize()
+    build_ms = (time.perf_counter() - t0) * 1e3
+    E = linops.NUFFT(locs, (n,) * 3).normal()
+
+    def med(fn, reps=5):
+        fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(s)
+            fn()
+            e1.record(s)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return statistics.median(ts)
+
+    t_ms = med(lambda: T(x8))
+    e_ms = med(lambda: E(x8))
+    t1_ms = med(lambda: T(x8[:1]))
+    e1_ms = med(lambda: E(x8[:1]))
+    ty, ey = T(x8), E(x8)
+    rel = float(torch.linalg.vector_norm((ty - ey).flatten()) / torch.linalg.vector_norm(ey.flatten()))
+    del x8, ty, ey, T, E
+    torch.cuda.empty_cache()
+    return {"workload": f"NUFFT normal of 8 coil images, {n}^3, {locs.shape[0]} radial points",
+            "toeplitz_ms": t_ms, "explicit_ms": e_ms, "toeplitz_1coil_ms": t1_ms, "explicit_1coil_ms": e1_ms,
+            "kernel_build_ms": build_ms, "rel_diff_vs_explicit": rel}
+
+
+def bench_index(dev, peak):
+    """Sampling at integer locations (the Sampling linop, NUFFT mode
+    "sampling"): the reference's own benchmark shape for index_adjoint
+    (functional/_index/tests/bench_indexing.py: float32 values of shape
+    48 x 500 x 1600, one random index per dim into a 220^3 grid) and a
+    multicoil case (8 coils complex64, 2^20 samples into 160^3). Plans are
+    built once per index set (timed separately); each figure is the median
+    of 10 CUDA-event timings."""
+    import torchlinops_gb300 as T
+
+    s = torch.cuda.current_stream(dev)
+
+    def med(fn, reps=10):
+        fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(s)
+            fn()
+            e1.record(s)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return statistics.median(ts)
+
+    out = {}
+    gd = torch.Generator(device=dev).manual_seed(9)
+    cases = (("float32_48x500x1600_into_220cube", (220, 220, 220), (48, 500, 1600), 1, torch.float32),
+             ("c64_8coil_2^20_into_160cube", (160, 160, 160), (1 << 20,), 8, torch.complex64))
+    for name, grid, shape, coils, dt in cases:
+        idx = tuple(torch.randint(0, n, shape, device=dev, generator=gd) for n in grid)
+        vshape = ((coils,) if coils > 1 else ()) + shape
+        vals = torch.randn(vshape, dtype=dt, device=dev, generator=gd)
+        img = torch.randn(((coils,) if coils > 1 else ()) + grid, dtype=dt, device=dev, generator=gd)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        T.index_adjoint(vals, idx, grid)
+        torch.cuda.synchronize()
+        first_ms = (time.perf_counter() - t0) * 1e3
+        adj_ms = med(lambda: T.index_adjoint(vals, idx, grid))
+        fwd_ms = med(lambda: T.index(img, idx))
+        m = math.prod(shape)
+        es = vals.element_size()
+        # values in and the grid out (adjoint) or the grid in and samples out
+        # (forward), plus the 4-byte cell of each sample the plan holds
+        nbytes = coils * m * es + coils * math.prod(grid) * es + 4 * m
+        out[name] = {"adjoint_ms": adj_ms, "forward_ms": fwd_ms, "first_call_with_plan_ms": first_ms,
+                     "algorithmic_bytes": nbytes, "adjoint_GBps": nbytes / (adj_ms / 1e3) / 1e9,
+                     "adjoint_frac": nbytes / (adj_ms / 1e3) / 1e9 / peak,
+                     "forward_GBps": nbytes / (fwd_ms / 1e3) / 1e9}
+        del idx, vals, img
+        torch.cuda.empty_cache()
+    return out
 
 
 def _resize(grid: int, points: int) -> None:
@@ -587,26 +811,38 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="tlgb", choices=["tlgb", "reference"])
-    ap.add_argument("--ref-sample", type=int, default=1 << 16, help="points in the CPU baseline sample")
+    ap.add_argument("--ref-sample", type=int, default=1 << 19,
+                    help="points in the GPU arm's CPU baseline sample (about 10 s of CPU work)")
+    ap.add_argument("--ref-points", type=int, default=None,
+                    help="points per step of the reference arm (default: all of them, the same workload as the GPU arm)")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-blocks", action="store_true")
     ap.add_argument("--skip-cg", action="store_true", help="skip the learned vs plain CG comparison")
     ap.add_argument("--skip-nufft2d", action="store_true", help="skip the differentiable 2D NUFFT timing")
     ap.add_argument("--cg-steps", type=int, default=500, help="preconditioner training steps (4 samples each)")
+    ap.add_argument("--precond-compare", type=int, default=0,
+                    help="also train on this many phantoms solved by plain CG to 1e-6 and report that network")
     ap.add_argument("--grid", type=int, default=N_GRID, help="grid edge (smaller cases for profiling)")
     ap.add_argument("--points", type=int, default=N_PTS, help="number of points (smaller cases for profiling)")
     ap.add_argument("--blocks-batch", type=int, default=BLK_SHAPE[0],
                     help="array entries of the unfold/fold workload (smaller cases for profiling)")
     ap.add_argument("--nufft2d-only", action="store_true",
                     help="profiling: run only the 2D NUFFT timing and print its figures (not the bench line)")
+    ap.add_argument("--index-only", action="store_true",
+                    help="profiling: run only the sampling-op timing and print its figures (not the bench line)")
     args = ap.parse_args()
     _resize(args.grid, args.points)
+    if args.ref_points is None:
+        args.ref_points = N_PTS
     globals()["BLK_SHAPE"] = (args.blocks_batch,) + BLK_SHAPE[1:]
     args.warmup = max(args.warmup, 3)
-    if args.nufft2d_only:
+    if args.nufft2d_only or args.index_only:
         dev = torch.device("cuda", 0)
         torch.cuda.set_device(dev)
-        print(json.dumps({"nufft2d": bench_nufft2d(dev, measured_peaks()[0])}), flush=True)
+        if args.nufft2d_only:
+            print(json.dumps({"nufft2d": bench_nufft2d(dev, measured_peaks()[0])}), flush=True)
+        else:
+            print(json.dumps({"index": bench_index(dev, measured_peaks()[0])}), flush=True)
         return
     world, rank, local = dist_setup()
     if args.impl == "reference":

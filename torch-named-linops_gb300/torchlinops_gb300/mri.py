@@ -139,6 +139,26 @@ def training_batch(A, n: int, gen: torch.Generator, batch: int = 4, device="cpu"
     return pairs
 
 
+def cg_solution_pairs(A, n: int, count: int, seed: int = 0, rtol: float = 1e-6, max_iters: int = 500,
+                      device="cpu", noise: float = 0.05):
+    """(r, e) training pairs whose e are solutions that plain CG generates:
+    for each of ``count`` seeded 10-ellipsoid phantoms x, the right-hand side
+    r = A x + noise (white, ``noise`` times |A x| / sqrt(size)) and e = the
+    plain-CG solution of A e = r to relative residual ``rtol``."""
+    from . import alg
+
+    pairs = []
+    for i in range(count):
+        g = torch.Generator().manual_seed(seed + i)
+        x = ellipsoid_phantom_3d(n, 10, g, device)
+        r = A(x)
+        w = torch.complex(torch.randn(r.shape, generator=g), torch.randn(r.shape, generator=g)).to(device)
+        r = (r + noise * torch.linalg.vector_norm(r) / math.sqrt(r.numel()) * w).contiguous()
+        e, _ = alg.cg_solve(A, r, rtol=rtol, max_iters=max_iters)
+        pairs.append((r, e))
+    return pairs
+
+
 def power_method(A, v: Tensor, iters: int = 30) -> float:
     """Largest eigenvalue of the self-adjoint PSD operator A (alg/powermethod.py:12-60)."""
     v = v / torch.linalg.vector_norm(v)
