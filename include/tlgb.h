@@ -117,7 +117,16 @@ typedef struct tlgb_interp_plan_info {
   int64_t n_home;         /* points with at least one valid tap (home pairs) */
   int64_t off_records;    /* byte offset of the per-point tap records, 0 = none */
   int64_t kernel_key;     /* kernel, norm and beta the records were built for */
-  int64_t reserved;
+  /* Block lists of the 3D 8-entry gridding (0 when the plan has none): the
+   * (point, block) pairs of 4x4x4-cell output blocks, sorted stably by block,
+   * and their work items (dense blocks are split into parts summed after). */
+  int64_t n_blk_entries;
+  int64_t n_blk_items;
+  int64_t n_blk_partials; /* partial blocks of split (dense) blocks */
+  int64_t n_blk_split;    /* blocks summed from partials */
+  int64_t off_blk_entries;
+  int64_t off_blk_items;
+  int64_t off_blk_split;
 } tlgb_interp_plan_info;
 
 /* Bytes of device memory needed by a plan for this description (worst case)

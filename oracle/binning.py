@@ -18,6 +18,11 @@ restates, independently of the CUDA code, which pairs exist and their order:
   pairs (the GPU treats them as having no taps);
 * pairs are ordered by ``key = 2 * tile + (0 if home else 1)`` and, for equal
   keys, by point index (a stable sort of the pairs in point order).
+
+3D plans of the 8-entry gridding also list (point, block) pairs for output
+blocks of 4 x 4 x 4 cells (``block_pairs``): a point pairs with every block
+that one of its valid taps lands in, keyed ``(b0 * nb1 + b1) * nb2 + b2``,
+in point order within a block.
 """
 
 from __future__ import annotations
@@ -29,7 +34,7 @@ import torch
 
 from .interp import axis_taps
 
-__all__ = ["tile_shape", "plan_pairs"]
+__all__ = ["tile_shape", "plan_pairs", "block_pairs"]
 
 
 def tile_shape(grid_size):
@@ -84,6 +89,48 @@ def plan_pairs(locs: torch.Tensor, grid_size, width, kernel: str = "kaiser_besse
                 lin = (t0 * nt[1] + t1) * nt[2] + t2
                 nonhome = 0 if (i0, i1, i2) == (0, 0, 0) else 1
                 keys.append((2 * lin + nonhome)[m])
+                pts.append(pidx[m])
+    keys = torch.cat(keys).numpy()
+    pts = torch.cat(pts).numpy()
+    order = np.lexsort((pts, keys))
+    return keys[order], pts[order]
+
+
+def block_pairs(locs: torch.Tensor, grid_size, width, kernel: str = "kaiser_bessel", pad_mode: str = "circular"):
+    """(keys, points) of the 3D block lists: every (point, 4^3-cell block)
+    pair, sorted by block key and, within a block, by point index."""
+    assert len(grid_size) == 3
+    N = tuple(int(n) for n in grid_size)
+    nb = tuple(-(-n // 4) for n in N)
+    x = locs.reshape(-1, 3).to(torch.float32)
+    P = x.shape[0]
+    widths = width if isinstance(width, (tuple, list)) else (width,) * 3
+    ok = torch.isfinite(x).all(-1) & (x.abs() < 16777216.0).all(-1)
+    blocks = []  # per dim: [P, 3] distinct blocks, -1 = none
+    for e in range(3):
+        g, _, valid = axis_taps(x[:, e], float(widths[e]), kernel, torch.float32)
+        if pad_mode == "zero":
+            valid = valid & (g >= 0) & (g < N[e])
+        pos = torch.remainder(g, N[e]) if pad_mode == "circular" else g
+        bl = torch.div(pos, 4, rounding_mode="floor")
+        out = torch.full((P, 3), -1, dtype=torch.int64)
+        cnt = torch.zeros(P, dtype=torch.int64)
+        for k in range(g.shape[1]):
+            bk = bl[:, k]
+            seen = (out == bk[:, None]).any(-1)
+            add = valid[:, k] & ~seen & (cnt < 3)
+            idx = torch.nonzero(add).flatten()
+            out[idx, cnt[idx]] = bk[idx]
+            cnt = cnt + add.to(torch.int64)
+        blocks.append(out)
+    keys, pts = [], []
+    pidx = torch.arange(P)
+    for i0 in range(3):
+        for i1 in range(3):
+            for i2 in range(3):
+                b0, b1, b2 = blocks[0][:, i0], blocks[1][:, i1], blocks[2][:, i2]
+                m = ok & (b0 >= 0) & (b1 >= 0) & (b2 >= 0)
+                keys.append(((b0 * nb[1] + b1) * nb[2] + b2)[m])
                 pts.append(pidx[m])
     keys = torch.cat(keys).numpy()
     pts = torch.cat(pts).numpy()

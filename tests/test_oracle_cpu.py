@@ -43,6 +43,21 @@ def test_binning_invariants():
     assert 2.0 < len(keys) / 3000 < 4.0
 
 
+def test_block_list_invariants():
+    gen = torch.Generator().manual_seed(2)
+    locs = torch.rand(3000, 3, generator=gen) * 40 - 4
+    keys, pts = OB.block_pairs(locs, (32, 32, 32), 4.0)
+    assert np.all(np.diff(keys) >= 0)
+    same = np.diff(keys) == 0
+    assert np.all(np.diff(pts)[same] > 0)  # point order inside a block
+    # a window of 4 (5 at exact integers) taps meets at most 2 blocks of 4 per axis
+    assert np.bincount(pts).max() <= 8
+    assert 4.5 < len(keys) / 3000 < 6.0  # 1.75^3 = 5.36 blocks per point on average
+    # every point's blocks contain its taps: one block holds its first tap on each axis
+    kt, pt = OB.plan_pairs(locs, (32, 32, 32), 4.0)
+    assert np.array_equal(np.unique(pts), np.unique(pt))
+
+
 @pytest.mark.parametrize("shape", [(37,), (19, 23), (9, 10, 11)])
 @pytest.mark.parametrize("kernel,norm", [("kaiser_bessel", 1), ("spline", 1), ("kaiser_bessel", 2)])
 @pytest.mark.parametrize("pad", ["circular", "zero"])

@@ -1,6 +1,8 @@
 """The plan's bin permutation, bit-exact against the CPU oracle
 (oracle/binning.py): every (point, tile) pair, ordered by tile, home pairs
-first, then by point index. Sizes large enough for the multi-CTA scans."""
+first, then by point index; and in 3D the (point, 4^3 block) lists of the
+gridding, ordered by block, then by point index. Sizes large enough for the
+multi-CTA scans."""
 
 import numpy as np
 import pytest
@@ -40,3 +42,38 @@ def test_plan_permutation_is_bit_exact(grid_size, npts, pad):
     assert np.array_equal(got, pts)
     # home pairs: one per point with taps
     assert int(plan.info.n_home) == int((keys % 2 == 0).sum())
+
+
+@pytest.mark.parametrize("grid_size,npts,pad", [c for c in CASES if len(c[0]) == 3])
+def test_block_lists_are_bit_exact(grid_size, npts, pad):
+    gen = torch.Generator().manual_seed(npts + 7)
+    n = torch.tensor(grid_size, dtype=torch.float32)
+    locs = torch.rand(npts, 3, generator=gen) * (n + 6) - 3
+    locs[:500] = torch.randint(0, 30, (500, 3), generator=gen).float()  # exact integers: 5 taps
+    locs[500:520, 1] = float("inf")
+    keys, pts = OB.block_pairs(locs, grid_size, 4.0, "kaiser_bessel", pad)
+    plan = interp.get_plan(locs.to(DEV), grid_size, 4.0, "kaiser_bessel", pad, 6.99666)
+    info = plan.info
+    assert int(info.n_blk_entries) == len(pts) and int(info.n_blk_items) > 0
+    off = int(info.off_blk_entries)
+    got = plan.buffer[off:off + 4 * len(pts)].view(torch.int32).cpu().numpy()
+    assert np.array_equal(got, pts)
+    # work items: each block's entries exactly once, split into parts of at most 256
+    items = plan.buffer[int(info.off_blk_items):int(info.off_blk_items) + 16 * int(info.n_blk_items)]
+    items = items.view(torch.int32).reshape(-1, 4).cpu().numpy()
+    full = items[items[:, 1] < items[:, 2]]
+    assert (full[:, 2] - full[:, 1]).max() <= 256
+    cover = np.zeros(len(pts), dtype=np.int64)
+    for b, s0, s1, _ in full:
+        assert np.all(keys[s0:s1] == b)
+        cover[s0:s1] += 1
+    assert np.all(cover == 1)
+    # empty runs and non-empty items together name every block once
+    nb = int(np.prod([-(-s // 4) for s in grid_size]))
+    named = np.zeros(nb, dtype=np.int64)
+    for b, s0, s1, w in items:
+        if s0 == s1:
+            named[b:b - w] += 1
+        elif w < 0 or s0 == keys.searchsorted(b):
+            named[b] += 1
+    assert np.all(named == 1)

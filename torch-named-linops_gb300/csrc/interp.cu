@@ -981,6 +981,69 @@ __global__ void point_records_kernel(Geo g, const float* __restrict__ locs, PRec
   out[p] = R;
 }
 
+// ------------------------------------------------ block lists (3D gridding)
+//
+// The 3D 8-entry gridding works on output blocks of 4 x 4 x 4 cells. A
+// window of 4 taps per dimension meets 1.75 blocks per dimension on average
+// (5.4 blocks of 64 cells per point), and one warp holds a whole block for 8
+// entries in registers (2 cells x 8 entries per lane). The plan lists per
+// block the points whose window meets it, in point order.
+constexpr int kBE = 4;         // block edge in cells, every dimension
+constexpr int kBlkPart = 256;  // entries per work item: denser blocks are split into parts
+constexpr int kZeroRun = 16;   // empty blocks written by one work item
+
+__host__ __device__ __forceinline__ int blocks_along(int n) { return (n + kBE - 1) / kBE; }
+
+// Distinct blocks met along one dim by the cells st .. st+c-1 of a window
+// (st in [0, N); wrapped once in circular mode, where N >= 16 > c).
+__device__ __forceinline__ int axis_blocks(const Geo& g, int e, int st, int c, int* bl) {
+  int cnt = 0;
+  for (int k = 0; k < c; ++k) {
+    int v = st + k;
+    if (v >= g.N[e]) v -= g.N[e];
+    const int b = v / kBE;
+    bool seen = false;
+    for (int i = 0; i < cnt; ++i) seen = seen || bl[i] == b;
+    if (!seen && cnt < 3) bl[cnt++] = b;
+  }
+  return cnt;
+}
+
+__global__ void blk_count_kernel(Geo g, const PRec* __restrict__ precs, uint32_t* __restrict__ cnt) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= g.npts) return;
+  const PRec R = precs[p];
+  uint32_t c = 1;
+  for (int e = 0; e < 3; ++e) {
+    const int ce = (R.cnt >> (4 * e)) & 15;
+    int bl[3];
+    c *= ce ? (uint32_t)axis_blocks(g, e, R.st[e], ce, bl) : 0u;
+  }
+  cnt[p] = c;
+}
+
+__global__ void blk_emit_kernel(Geo g, const PRec* __restrict__ precs, const uint32_t* __restrict__ off,
+                                uint32_t* __restrict__ keys, int32_t* __restrict__ vals) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= g.npts) return;
+  const PRec R = precs[p];
+  int bl[3][3], nc[3];
+  for (int e = 0; e < 3; ++e) {
+    const int ce = (R.cnt >> (4 * e)) & 15;
+    if (!ce) return;
+    nc[e] = axis_blocks(g, e, R.st[e], ce, bl[e]);
+  }
+  const uint32_t nb1 = (uint32_t)blocks_along(g.N[1]), nb2 = (uint32_t)blocks_along(g.N[2]);
+  uint32_t o = off[p];
+  for (int i = 0; i < nc[0]; ++i)
+    for (int j = 0; j < nc[1]; ++j)
+      for (int k = 0; k < nc[2]; ++k) {
+        keys[o] = ((uint32_t)bl[0][i] * nb1 + (uint32_t)bl[1][j]) * nb2 + (uint32_t)bl[2][k];
+        vals[o] = (int32_t)p;
+        ++o;
+      }
+}
+
 // View of one dimension of a record from the tile at o (8 wide, grid N):
 // f = first local position, m = taps inside the tile, k0 = index of the
 // first of them in the record; packed f | m << 3 | k0 << 6. fast is cleared
@@ -1416,6 +1479,288 @@ __global__ void __launch_bounds__(256, 4) adj_f3_kernel(Geo g, const int4* __res
         if (o[2] + z + 1 < g.N[2]) *reinterpret_cast<float2*>(row + 2 * z + 2) = b;
       }
     }
+  }
+}
+
+// ------------------------------------------------- block gridding (3D, 8 entries)
+//
+// One warp per work item: a 4 x 4 x 4-cell output block x 8 complex entries
+// held in registers, lane (x, y, z pair) owning the cells (x, y, 2 zp) and
+// (x, y, 2 zp + 1) for all 8 entries. No two threads own the same value and
+// the warps of a CTA never wait for one another. The warp walks its block's
+// list in chunks of 32 entries: each lane copies one entry's point record
+// and values into the warp's staging slots (cp.async), then turns the record
+// into the block's rows of tap weights; every lane then applies the chunk's
+// entries in list order, 16 packed (re, im) FMAs per entry. Each cell
+// therefore sums its contributions in plan order, starting from zero:
+// bit-identical run to run. Entries whose values are not finite update only
+// the cells of their window (the zero weights elsewhere would spread a NaN
+// or Inf), and exact-integer coordinates (5 taps in a dimension) take their
+// weights from the coordinates instead of the 4-weight record.
+constexpr int kBC = 32;  // entries per chunk (one per lane while staging)
+constexpr int kBS = 44;  // floats per staging slot: rows 0-15 | values 16-31 | z row 32-35 | flags 36;
+                         // 44 keeps the lanes' 16-byte slot stores free of bank conflicts
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+
+// Tap weights of the 4 cells b0 .. b0+3 of one dim, from a record dimension
+// with at most 4 taps (first tap st, count c, weights w4); bit i of valid is
+// set when cell b0 + i is in the window.
+__device__ __forceinline__ float4 block_row(const Geo& g, int e, int b0, int st, int c, const float4& w4,
+                                            unsigned& valid) {
+  const bool circ = g.pad == TLGB_PAD_CIRCULAR;
+  int d = b0 - st;
+  if (circ && d < 0) d += g.N[e];
+  float r[4];
+  valid = 0;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    int t = d + i;
+    if (circ && t >= g.N[e]) t -= g.N[e];
+    const bool ok = b0 + i < g.N[e] && t >= 0 && t < c;
+    r[i] = ok ? pick4(w4, t) : 0.f;
+    valid |= (ok ? 1u : 0u) << i;
+  }
+  return make_float4(r[0], r[1], r[2], r[3]);
+}
+
+// The same from the coordinate (any number of taps; used for 5-tap windows)
+__device__ __forceinline__ float4 block_row_coord(const Geo& g, int e, int b0, float x, unsigned& valid) {
+  const int lower = lower_of(g, e, x);
+  float r[4];
+  valid = 0;
+  for (int i = 0; i < 4; ++i) {
+    const int v = b0 + i;
+    int k = v - lower;
+    if (g.pad == TLGB_PAD_CIRCULAR) k = wrapi(k, g.N[e]);
+    bool ok = v < g.N[e] && k >= 0 && k < g.NT[e];
+    float w = 0.f;
+    if (ok) {
+      const Tap t = tap_eval(g, e, x, lower, k);
+      ok = t.valid;
+      if (ok) w = kern_value_approx(g.kernel, fabsf(t.d), g.beta);
+    }
+    r[i] = w;
+    valid |= (ok ? 1u : 0u) << i;
+  }
+  return make_float4(r[0], r[1], r[2], r[3]);
+}
+
+__device__ __forceinline__ void block_origin(const Geo& g, int key, int& bx, int& by, int& bz) {
+  const int nb1 = blocks_along(g.N[1]), nb2 = blocks_along(g.N[2]);
+  bz = key % nb2;
+  const int t = key / nb2;
+  by = t % nb1;
+  bx = t / nb1;
+}
+
+// Stores the lane's two cells (x, y, z0), (x, y, z0 + 1) of entries 0..ncoil-1.
+__device__ __forceinline__ void block_store(const Geo& g, float* __restrict__ gridv, int c0, int ncoil, int x, int y,
+                                            int z0, const float2 (&a0)[8], const float2 (&a1)[8]) {
+  if (x >= g.N[0] || y >= g.N[1] || z0 >= g.N[2]) return;
+  const long long gvol = (long long)g.N[0] * g.N[1] * g.N[2];
+  const bool two = z0 + 1 < g.N[2];
+  // 16-byte stores need an even Z extent (z0 is even) and an aligned base
+  const bool vec = two && (g.N[2] & 1) == 0 && (reinterpret_cast<uintptr_t>(gridv) & 15) == 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    if (k >= ncoil) break;
+    float* row = gridv + ((long long)(c0 + k) * gvol + ((long long)x * g.N[1] + y) * g.N[2] + z0) * 2;
+    if (vec) {
+      *reinterpret_cast<float4*>(row) = make_float4(a0[k].x, a0[k].y, a1[k].x, a1[k].y);
+    } else {
+      *reinterpret_cast<float2*>(row) = a0[k];
+      if (two) *reinterpret_cast<float2*>(row + 2) = a1[k];
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256, 4) adj_b3_kernel(Geo g, const int4* __restrict__ items, int nitems,
+                                                        const int32_t* __restrict__ bentries,
+                                                        const PRec* __restrict__ precs,
+                                                        const float* __restrict__ locs, const float2* __restrict__ vals,
+                                                        const float4* __restrict__ tv, float* __restrict__ gridv,
+                                                        float* __restrict__ partial) {
+  extern __shared__ __align__(16) float bsm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int item = blockIdx.x * 8 + warp;
+  if (item >= nitems) return;  // no CTA-wide synchronisation below
+  float* S = bsm + warp * (kBC * kBS);
+  const int4 it = items[item];
+  const int cg = blockIdx.y, c0 = cg * 8;
+  const int ncoil = (int)min(8ll, g.nbatch - c0);
+  const int lx = lane >> 3, ly = (lane >> 1) & 3, zp = lane & 1;
+  float2 a0[8], a1[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) a0[k] = a1[k] = make_float2(0.f, 0.f);
+  int bx, by, bz;
+  if (it.y == it.z) {  // a run of -it.w empty blocks
+    for (int b = 0; b < -it.w; ++b) {
+      block_origin(g, it.x + b, bx, by, bz);
+      block_store(g, gridv, c0, ncoil, kBE * bx + lx, kBE * by + ly, kBE * bz + 2 * zp, a0, a1);
+    }
+    return;
+  }
+  block_origin(g, it.x, bx, by, bz);
+  const int B[3] = {kBE * bx, kBE * by, kBE * bz};
+  for (int c = it.y; c < it.z; c += kBC) {
+    const int n = min(kBC, it.z - c);
+    float* sl = S + lane * kBS;
+    int p = 0;
+    if (lane < n) {
+      p = bentries[c + lane];
+      if (!TLGB_IN_RANGE(p, g.npts)) p = 0;
+      const float4* rsrc = reinterpret_cast<const float4*>(precs + p);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) cp_async16(sl + 4 * q, rsrc + q);
+      if (tv) {
+        const float4* vsrc = tv + ((long long)cg * g.npts + p) * 4;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) cp_async16(sl + 16 + 4 * q, vsrc + q);
+      } else {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          if (k < ncoil)
+            cp_async8(sl + 16 + 2 * k, vals + (long long)(c0 + k) * g.npts + p);
+          else
+            *reinterpret_cast<float2*>(sl + 16 + 2 * k) = make_float2(0.f, 0.f);
+        }
+      }
+    }
+    cp_async_wait_all();
+    // the lane's own entry: record -> rows of tap weights over the block
+    unsigned flags = 0;
+    if (lane < n) {
+      const float4* rq = reinterpret_cast<const float4*>(sl);
+      const float4 w0 = rq[0], w1 = rq[1], w2 = rq[2];
+      const int4 t = reinterpret_cast<const int4*>(sl)[3];
+      const int c_x = t.w & 15, c_y = (t.w >> 4) & 15, c_z = (t.w >> 8) & 15;
+      unsigned vx, vy, vz;
+      float4 rx, ry, rz;
+      if (c_x <= 4 && c_y <= 4 && c_z <= 4) {
+        rx = block_row(g, 0, B[0], t.x, c_x, w0, vx);
+        ry = block_row(g, 1, B[1], t.y, c_y, w1, vy);
+        rz = block_row(g, 2, B[2], t.z, c_z, w2, vz);
+      } else {
+        rx = block_row_coord(g, 0, B[0], load_coord(g, locs, p, 0), vx);
+        ry = block_row_coord(g, 1, B[1], load_coord(g, locs, p, 1), vy);
+        rz = block_row_coord(g, 2, B[2], load_coord(g, locs, p, 2), vz);
+      }
+      // a non-finite value turns the zero product into NaN
+      float chk = 0.f;
+      const float4* vq = reinterpret_cast<const float4*>(sl + 16);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const float4 v = vq[q];
+        chk = fmaf(v.x, 0.f, chk);
+        chk = fmaf(v.y, 0.f, chk);
+        chk = fmaf(v.z, 0.f, chk);
+        chk = fmaf(v.w, 0.f, chk);
+      }
+      flags = (chk == 0.f ? 0u : 1u) | (vx << 4) | (vy << 8) | (vz << 12);
+      float4* wq = reinterpret_cast<float4*>(sl);
+      wq[0] = make_float4(rx.x * ry.x, rx.x * ry.y, rx.x * ry.z, rx.x * ry.w);
+      wq[1] = make_float4(rx.y * ry.x, rx.y * ry.y, rx.y * ry.z, rx.y * ry.w);
+      wq[2] = make_float4(rx.z * ry.x, rx.z * ry.y, rx.z * ry.z, rx.z * ry.w);
+      wq[3] = make_float4(rx.w * ry.x, rx.w * ry.y, rx.w * ry.z, rx.w * ry.w);
+      wq[8] = rz;
+      reinterpret_cast<unsigned*>(sl)[36] = flags;
+    }
+    const bool guarded = __ballot_sync(0xffffffffu, flags & 1u) != 0;
+    __syncwarp();
+    // every lane applies the chunk's entries in order
+    auto visit = [&](const float* e, bool ok0, bool ok1) {
+      const float wxy = e[lx * 4 + ly];
+      const float2 wz = *reinterpret_cast<const float2*>(e + 32 + 2 * zp);
+      const float4 v0 = *reinterpret_cast<const float4*>(e + 16), v1 = *reinterpret_cast<const float4*>(e + 20);
+      const float4 v2 = *reinterpret_cast<const float4*>(e + 24), v3 = *reinterpret_cast<const float4*>(e + 28);
+      const float2 v[8] = {make_float2(v0.x, v0.y), make_float2(v0.z, v0.w), make_float2(v1.x, v1.y),
+                           make_float2(v1.z, v1.w), make_float2(v2.x, v2.y), make_float2(v2.z, v2.w),
+                           make_float2(v3.x, v3.y), make_float2(v3.z, v3.w)};
+      const float w0 = wxy * wz.x, w1 = wxy * wz.y;
+      if (ok0) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) a0[k] = __ffma2_rn(make_float2(w0, w0), v[k], a0[k]);
+      }
+      if (ok1) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) a1[k] = __ffma2_rn(make_float2(w1, w1), v[k], a1[k]);
+      }
+    };
+    if (!guarded) {
+#pragma unroll 2
+      for (int j = 0; j < n; ++j) visit(S + j * kBS, true, true);
+    } else {
+      for (int j = 0; j < n; ++j) {
+        const float* e = S + j * kBS;
+        const unsigned f = reinterpret_cast<const unsigned*>(e)[36];
+        bool ok0 = true, ok1 = true;
+        if (f & 1u) {
+          const bool xy = ((f >> (4 + lx)) & (f >> (8 + ly)) & 1u) != 0;
+          ok0 = xy && ((f >> (12 + 2 * zp)) & 1u);
+          ok1 = xy && ((f >> (13 + 2 * zp)) & 1u);
+        }
+        visit(e, ok0, ok1);
+      }
+    }
+    __syncwarp();  // the chunk has been read before the next one is staged
+  }
+  if (it.w >= 0) {  // a part of a split block: its slot of the partial blocks, [cell][entry] complex
+    float4* d = reinterpret_cast<float4*>(partial + (((long long)it.w * gridDim.y + cg) * 64 + lane * 2) * 16);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      d[k] = make_float4(a0[2 * k].x, a0[2 * k].y, a0[2 * k + 1].x, a0[2 * k + 1].y);
+      d[4 + k] = make_float4(a1[2 * k].x, a1[2 * k].y, a1[2 * k + 1].x, a1[2 * k + 1].y);
+    }
+    return;
+  }
+  block_store(g, gridv, c0, ncoil, B[0] + lx, B[1] + ly, B[2] + 2 * zp, a0, a1);
+}
+
+// Sum the partial blocks of one split block in slot order, compensated (as
+// adj_reduce_f3_kernel). CTA = 128 threads: thread (entry half, cell).
+__global__ void __launch_bounds__(128) adj_reduce_b3_kernel(Geo g, const int4* __restrict__ split,
+                                                            const float* __restrict__ partial,
+                                                            float* __restrict__ gridv) {
+  const int4 sp = split[blockIdx.x];
+  const int cg = blockIdx.y, ncg = gridDim.y, c0 = cg * 8;
+  const int ncoil = (int)min(8ll, g.nbatch - c0);
+  const int half = threadIdx.x >> 6, cell = threadIdx.x & 63;
+  int bx, by, bz;
+  block_origin(g, sp.x, bx, by, bz);
+  const long long step = (long long)ncg * 64 * 16 / 4;  // float4s between consecutive partials
+  const float4* src =
+      reinterpret_cast<const float4*>(partial + (((long long)sp.y * ncg + cg) * 64 + cell) * 16 + half * 8);
+  float s[8], cmp[8];
+  {
+    const float4 a = __ldg(src), b = __ldg(src + 1);
+    s[0] = a.x, s[1] = a.y, s[2] = a.z, s[3] = a.w, s[4] = b.x, s[5] = b.y, s[6] = b.z, s[7] = b.w;
+  }
+#pragma unroll
+  for (int i = 0; i < 8; ++i) cmp[i] = 0.f;
+  for (int k = 1; k < sp.z; ++k) {
+    const float4 a = __ldg(src + k * step), b = __ldg(src + k * step + 1);
+    const float v[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+#pragma unroll
+    for (int i = 0; i < 8; ++i) comp_add(s[i], cmp[i], v[i]);
+  }
+  const int x = kBE * bx + (cell >> 4), y = kBE * by + ((cell >> 2) & 3), z = kBE * bz + (cell & 3);
+  if (x >= g.N[0] || y >= g.N[1] || z >= g.N[2]) return;
+  const long long gvol = (long long)g.N[0] * g.N[1] * g.N[2];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int c = half * 4 + k;
+    if (c >= ncoil) break;
+    *reinterpret_cast<float2*>(gridv + ((long long)(c0 + c) * gvol + ((long long)x * g.N[1] + y) * g.N[2] + z) * 2) =
+        make_float2(s[2 * k] + cmp[2 * k], s[2 * k + 1] + cmp[2 * k + 1]);
   }
 }
 
@@ -2517,6 +2862,8 @@ __global__ void __launch_bounds__(256, 3) grad_f2_kernel(const __grid_constant__
 struct PlanLayout {
   int64_t e_max, max_fwd, max_adj, ntiles;
   int64_t off_entries, off_fwd, off_adj, off_split, off_recs, bytes;
+  // block lists of the 3D 8-entry gridding (off_blk_entries == 0: none)
+  int64_t nblocks, eb_max, max_blk_items, off_blk_entries, off_blk_items, off_blk_split;
   // tmp
   int64_t t_cnt, t_keys, t_keys2, t_vals2, t_counts, t_hist, t_total, t_bytes;
 };
@@ -2607,6 +2954,25 @@ bool records_ok(const Geo& g) {
   return g.ndim == 2 && g.T[1] == 16 && g.T[2] == 16 && g.NT[1] == 5 && g.NT[2] == 5;
 }
 
+// 3D geometries whose plans also carry block lists (adj_b3_kernel): the
+// records' geometry, and in circular mode every dim at least 16 cells, so
+// that a wrapped window meets a block at most once.
+bool blocks_ok(const Geo& g) {
+  if (g.ndim != 3 || !records_ok(g)) return false;
+  if (g.pad == TLGB_PAD_CIRCULAR && std::min(g.N[0], std::min(g.N[1], g.N[2])) < 16) return false;
+  const int64_t nb = (int64_t)blocks_along(g.N[0]) * blocks_along(g.N[1]) * blocks_along(g.N[2]);
+  return nb < (1ll << 31);
+}
+
+// Blocks one window can meet along a dim: 2 (at most 5 taps over 4 cells),
+// 3 where a circular window crosses a ragged last block and the wrap.
+int64_t max_blocks_per_dim(const Geo& g, int e) {
+  const int nb = blocks_along(g.N[e]);
+  if (nb == 1) return 1;
+  if (g.pad == TLGB_PAD_CIRCULAR && g.N[e] % kBE != 0) return std::min(3, nb);
+  return 2;
+}
+
 // The kernel, norm and beta a plan's records hold weights for
 int64_t kernel_key(const Geo& g) {
   uint32_t bits;
@@ -2634,20 +3000,34 @@ PlanLayout layout(const Geo& g) {
     L.off_recs = o;
     o = align_up(o + (size_t)g.npts * 64, 256);
   }
+  L.nblocks = L.eb_max = L.max_blk_items = 0;
+  L.off_blk_entries = L.off_blk_items = L.off_blk_split = 0;
+  if (blocks_ok(g) && g.npts > 0) {
+    L.nblocks = (int64_t)blocks_along(g.N[0]) * blocks_along(g.N[1]) * blocks_along(g.N[2]);
+    L.eb_max = g.npts * max_blocks_per_dim(g, 0) * max_blocks_per_dim(g, 1) * max_blocks_per_dim(g, 2);
+    L.max_blk_items = L.nblocks + cdiv(L.eb_max, kBlkPart) + 1;
+    L.off_blk_entries = o;
+    o = align_up(o + (size_t)L.eb_max * 4, 256);
+    L.off_blk_items = o;
+    o = align_up(o + (size_t)L.max_blk_items * 16, 256);
+    L.off_blk_split = o;
+    o = align_up(o + (size_t)(L.nblocks + 1) * 16, 256);
+  }
   L.bytes = o;
+  const int64_t pairs = std::max<int64_t>(std::max(L.e_max, L.eb_max), 1);  // sort buffers serve both lists
   size_t t = 0;
   L.t_cnt = t;
   t = align_up(t + (size_t)(g.npts + 1) * 4, 256);
   L.t_keys = t;
-  t = align_up(t + (size_t)std::max<int64_t>(L.e_max, 1) * 4, 256);
+  t = align_up(t + (size_t)pairs * 4, 256);
   L.t_keys2 = t;
-  t = align_up(t + (size_t)std::max<int64_t>(L.e_max, 1) * 4, 256);
+  t = align_up(t + (size_t)pairs * 4, 256);
   L.t_vals2 = t;
-  t = align_up(t + (size_t)std::max<int64_t>(L.e_max, 1) * 4, 256);
+  t = align_up(t + (size_t)pairs * 4, 256);
   L.t_counts = t;
-  t = align_up(t + (size_t)radix_counts_len(std::max<int64_t>(L.e_max, 1)) * 4, 256);
+  t = align_up(t + (size_t)radix_counts_len(pairs) * 4, 256);
   L.t_hist = t;
-  t = align_up(t + (size_t)(2 * L.ntiles + 1) * 4, 256);
+  t = align_up(t + (size_t)(std::max(2 * L.ntiles, L.nblocks) + 1) * 4, 256);
   L.t_total = t;
   t = align_up(t + 16, 256);
   L.t_bytes = t;
@@ -2775,7 +3155,7 @@ extern "C" int tlgb_interp_plan_size(const tlgb_interp_desc* d, size_t* plan_byt
   Geo g;
   TLGB_TRY(make_geo(d, g));
   const PlanLayout L = layout(g);
-  if (L.e_max >= (1ll << 31)) TLGB_FAIL(TLGB_ERR_UNSUPPORTED, "too many points for one plan");
+  if (std::max(L.e_max, L.eb_max) >= (1ll << 31)) TLGB_FAIL(TLGB_ERR_UNSUPPORTED, "too many points for one plan");
   if (plan_bytes) *plan_bytes = (size_t)L.bytes;
   if (tmp_bytes) *tmp_bytes = (size_t)L.t_bytes;
   return TLGB_OK;
@@ -2787,7 +3167,7 @@ extern "C" int tlgb_interp_plan_build(const tlgb_interp_desc* d, const float* lo
   Geo g;
   TLGB_TRY(make_geo(d, g));
   const PlanLayout L = layout(g);
-  if (L.e_max >= (1ll << 31)) TLGB_FAIL(TLGB_ERR_UNSUPPORTED, "too many points for one plan");
+  if (std::max(L.e_max, L.eb_max) >= (1ll << 31)) TLGB_FAIL(TLGB_ERR_UNSUPPORTED, "too many points for one plan");
   if (!info || !plan || !tmp || (g.npts > 0 && !locs)) TLGB_FAIL(TLGB_ERR_INVALID, "null pointer");
   if (plan_bytes < (size_t)L.bytes || tmp_bytes < (size_t)L.t_bytes) TLGB_FAIL(TLGB_ERR_WORKSPACE, "plan workspace too small");
   cudaStream_t s = (cudaStream_t)stream;
@@ -2863,6 +3243,69 @@ extern "C" int tlgb_interp_plan_build(const tlgb_interp_desc* d, const float* lo
   // host vectors are freed on return: make the copies complete first
   TLGB_CUDA(cudaStreamSynchronize(s));
 
+  // Block lists (3D 8-entry gridding): (point, block) pairs from the tap
+  // records, sorted stably by block; work items of at most kBlkPart entries
+  // (dense blocks split into parts summed in order afterwards) and runs of
+  // up to kZeroRun empty blocks. Items go heaviest first, empty runs last.
+  uint32_t Eb = 0;
+  std::vector<int4> bitems, bsplit;
+  int64_t n_bpartials = 0;
+  if (L.off_blk_entries > 0) {
+    const PRec* recs = (const PRec*)(P + L.off_recs);
+    int32_t* bentries = (int32_t*)(P + L.off_blk_entries);
+    const unsigned nb = (unsigned)cdiv(g.npts, 256);
+    blk_count_kernel<<<nb, 256, 0, s>>>(g, recs, cnt);
+    TLGB_CHECK_LAUNCH();
+    TLGB_TRY(exclusive_scan_u32(cnt, cnt, g.npts, total, counts, s));
+    blk_emit_kernel<<<nb, 256, 0, s>>>(g, recs, cnt, keys, bentries);
+    TLGB_CHECK_LAUNCH();
+    TLGB_CUDA(cudaMemcpyAsync(&Eb, total, 4, cudaMemcpyDeviceToHost, s));
+    TLGB_CUDA(cudaStreamSynchronize(s));
+    int bbits = 1;
+    while ((1ll << bbits) < L.nblocks) ++bbits;
+    TLGB_TRY(radix_sort_pairs(keys, bentries, keys2, vals2, counts, (int64_t)Eb, bbits, s));
+    TLGB_CUDA(cudaMemsetAsync(hist, 0, (size_t)L.nblocks * 4, s));
+    if (Eb > 0) {
+      key_hist_kernel<<<(unsigned)cdiv(Eb, 256), 256, 0, s>>>(keys, Eb, hist);
+      TLGB_CHECK_LAUNCH();
+    }
+    std::vector<uint32_t> hb((size_t)L.nblocks);
+    TLGB_CUDA(cudaMemcpyAsync(hb.data(), hist, hb.size() * 4, cudaMemcpyDeviceToHost, s));
+    TLGB_CUDA(cudaStreamSynchronize(s));
+    int64_t bpos = 0;
+    std::vector<int4> zero_runs;
+    for (int64_t b = 0; b < L.nblocks; ++b) {
+      const int64_t n = hb[(size_t)b];
+      if (n == 0) {
+        int4* last = zero_runs.empty() ? nullptr : &zero_runs.back();
+        if (last && last->x - last->w == b && -last->w < kZeroRun)
+          --last->w;  // extends the run ending at block b - 1
+        else
+          zero_runs.push_back(make_int4((int)b, (int)bpos, (int)bpos, -1));
+        continue;
+      }
+      if (n <= kBlkPart) {
+        bitems.push_back(make_int4((int)b, (int)bpos, (int)(bpos + n), -1));
+      } else {
+        const int64_t nch = cdiv(n, kBlkPart);
+        bsplit.push_back(make_int4((int)b, (int)n_bpartials, (int)nch, 0));
+        for (int64_t k = 0; k < nch; ++k)
+          bitems.push_back(make_int4((int)b, (int)(bpos + k * kBlkPart), (int)std::min(bpos + n, bpos + (k + 1) * kBlkPart),
+                                     (int)(n_bpartials + k)));
+        n_bpartials += nch;
+      }
+      bpos += n;
+    }
+    std::stable_sort(bitems.begin(), bitems.end(), heavier);
+    bitems.insert(bitems.end(), zero_runs.begin(), zero_runs.end());
+    if ((int64_t)bitems.size() > L.max_blk_items) TLGB_FAIL(TLGB_ERR_DEVICE, "block work list larger than its bound");
+    if (!bitems.empty())
+      TLGB_CUDA(cudaMemcpyAsync(P + L.off_blk_items, bitems.data(), bitems.size() * 16, cudaMemcpyHostToDevice, s));
+    if (!bsplit.empty())
+      TLGB_CUDA(cudaMemcpyAsync(P + L.off_blk_split, bsplit.data(), bsplit.size() * 16, cudaMemcpyHostToDevice, s));
+    TLGB_CUDA(cudaStreamSynchronize(s));
+  }
+
   memset(info, 0, sizeof(*info));
   info->n_entries = E;
   info->n_tiles = L.ntiles;
@@ -2883,6 +3326,15 @@ extern "C" int tlgb_interp_plan_build(const tlgb_interp_desc* d, const float* lo
   info->off_records = L.off_recs;
   info->kernel_key = L.off_recs > 0 ? kernel_key(g) : 0;
   info->n_home = n_home;
+  if (L.off_blk_entries > 0) {
+    info->n_blk_entries = Eb;
+    info->n_blk_items = (int64_t)bitems.size();
+    info->n_blk_partials = n_bpartials;
+    info->n_blk_split = (int64_t)bsplit.size();
+    info->off_blk_entries = L.off_blk_entries;
+    info->off_blk_items = L.off_blk_items;
+    info->off_blk_split = L.off_blk_split;
+  }
   return TLGB_OK;
 }
 
@@ -2896,7 +3348,9 @@ bool fast2(const Geo& g, int cg);
 void adj_scratch_parts(const Geo& g, const tlgb_interp_plan_info* info, size_t& partial_bytes, size_t& tv_bytes) {
   const int cg = adj_cg(g);
   const int64_t ncg = cdiv(std::max<long long>(g.nbatch, 1), cg);
-  partial_bytes = align_up((size_t)info->n_partials * ncg * tile_floats(g, cg) * sizeof(float), 256);
+  partial_bytes = fast3(g, cg) && info->n_blk_items > 0
+                      ? align_up((size_t)info->n_blk_partials * ncg * 64 * 16 * sizeof(float), 256)
+                      : align_up((size_t)info->n_partials * ncg * tile_floats(g, cg) * sizeof(float), 256);
   tv_bytes = ((fast3(g, cg) || fast2(g, cg)) && info->off_records > 0) ? (size_t)ncg * g.npts * 8 * 8 : 0;
 }
 }  // namespace
@@ -3054,6 +3508,37 @@ int launch_adj_f3(const Geo& g, const tlgb_interp_plan_info* info, const char* P
   return TLGB_OK;
 }
 
+int launch_adj_b3(const Geo& g, const tlgb_interp_plan_info* info, const char* P, const float* locs,
+                  const void* vals, void* grid, void* scratch, cudaStream_t s) {
+  const int64_t ncg = cdiv(g.nbatch, 8);
+  const size_t sm = 8 * kBC * kBS * sizeof(float);
+  TLGB_TRY(set_smem(adj_b3_kernel, sm));
+  // 16-byte asynchronous copies of the point records and transposed values
+  if (((uintptr_t)(P + info->off_records) & 15) || ((uintptr_t)scratch & 15))
+    TLGB_FAIL(TLGB_ERR_INVALID, "interp adjoint: plan and scratch must be 16-byte aligned");
+  if ((uintptr_t)vals & 7) TLGB_FAIL(TLGB_ERR_INVALID, "interp adjoint: values must be 8-byte aligned");
+  const float4* tv = nullptr;
+  if (g.tv_off >= 0 && g.npts > 0) {
+    float2* t = reinterpret_cast<float2*>(static_cast<char*>(scratch) + g.tv_off);
+    dim3 gt((unsigned)cdiv(g.npts, 32), (unsigned)ncg);
+    transpose_vals_kernel<<<gt, 256, 0, s>>>((const float2*)vals, g.npts, g.nbatch, t);
+    TLGB_CHECK_LAUNCH();
+    tv = reinterpret_cast<const float4*>(t);
+  }
+  dim3 grd((unsigned)cdiv(info->n_blk_items, 8), (unsigned)ncg);
+  adj_b3_kernel<<<grd, 256, sm, s>>>(g, (const int4*)(P + info->off_blk_items), (int)info->n_blk_items,
+                                    (const int32_t*)(P + info->off_blk_entries), (const PRec*)(P + info->off_records),
+                                    locs, (const float2*)vals, tv, (float*)grid, (float*)scratch);
+  TLGB_CHECK_LAUNCH();
+  if (info->n_blk_split > 0) {
+    dim3 g2((unsigned)info->n_blk_split, (unsigned)ncg);
+    adj_reduce_b3_kernel<<<g2, 128, 0, s>>>(g, (const int4*)(P + info->off_blk_split), (const float*)scratch,
+                                            (float*)grid);
+    TLGB_CHECK_LAUNCH();
+  }
+  return TLGB_OK;
+}
+
 int launch_adj_f2(const Geo& g, const tlgb_interp_plan_info* info, const char* P, const float* locs,
                   const void* vals, void* grid, void* scratch, cudaStream_t s) {
   const int64_t ncg = cdiv(g.nbatch, 8);
@@ -3098,6 +3583,8 @@ template <int N, int NDIM, int NTB>
 int launch_adj_t(const Geo& g, int cg, const tlgb_interp_plan_info* info, const char* P, const float* locs,
                  const void* vals, void* grid, void* scratch, cudaStream_t s) {
   if constexpr (N == 4 && NDIM == 3 && NTB == 5)
+    if (fast3(g, cg) && info->off_records > 0 && info->n_blk_items > 0)
+      return launch_adj_b3(g, info, P, locs, vals, grid, scratch, s);
     if (fast3(g, cg) && info->off_records > 0) return launch_adj_f3(g, info, P, locs, vals, grid, scratch, s);
   if constexpr (NDIM == 2 && NTB == 5)
     if (fast2(g, cg) && info->off_records > 0) return launch_adj_f2(g, info, P, locs, vals, grid, scratch, s);

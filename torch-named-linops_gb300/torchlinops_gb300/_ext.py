@@ -63,7 +63,13 @@ class PlanInfo(ctypes.Structure):
         ("n_home", ctypes.c_int64),
         ("off_records", ctypes.c_int64),
         ("kernel_key", ctypes.c_int64),
-        ("reserved", ctypes.c_int64),
+        ("n_blk_entries", ctypes.c_int64),
+        ("n_blk_items", ctypes.c_int64),
+        ("n_blk_partials", ctypes.c_int64),
+        ("n_blk_split", ctypes.c_int64),
+        ("off_blk_entries", ctypes.c_int64),
+        ("off_blk_items", ctypes.c_int64),
+        ("off_blk_split", ctypes.c_int64),
     ]
 
 
