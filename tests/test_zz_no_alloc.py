@@ -50,7 +50,7 @@ def test_fixed_scratch_gridding_matches_caller_scratch_gridding():
     beta = T.kaiser_bessel_beta(4.0, 1.25)
     ref = T.grid(vals, locs, (n, n, n), 4.0, kernel_params=dict(beta=beta))
     plan = interp.get_plan(locs, (n, n, n), 4.0, "kaiser_bessel", "circular", beta)
-    assert plan.info.n_partials > 0, "the case must exercise the partial-tile scratch"
+    assert plan.info.n_blk_partials > 0, "the case must exercise the partial-block scratch"
     desc = interp._desc(3, (n, n, n), (4.0,) * 3, "kaiser_bessel", 1, "circular", beta, True, vals.shape[0],
                         vals.shape[1])
     for _ in range(2):  # the second call sees the first call's buffer contents
@@ -68,7 +68,8 @@ def test_fixed_scratch_rejects_plans_beyond_its_buffer():
                         vals.shape[1])
     big = _ext.PlanInfo()
     ctypes.memmove(ctypes.byref(big), ctypes.byref(plan.info), ctypes.sizeof(big))
-    big.n_partials = 1 << 20  # far more partial tiles than the fixed buffer holds
+    big.n_partials = 1 << 20  # far more partial tiles (and blocks) than the fixed buffer holds
+    big.n_blk_partials = 1 << 20
     out = torch.zeros((vals.shape[0], n, n, n), dtype=torch.complex64, device=DEV)
 
     class _P:

@@ -1726,42 +1726,46 @@ __global__ void __launch_bounds__(256, 4) adj_b3_kernel(Geo g, const int4* __res
 }
 
 // Sum the partial blocks of one split block in slot order, compensated (as
-// adj_reduce_f3_kernel). CTA = 128 threads: thread (entry half, cell).
-__global__ void __launch_bounds__(128) adj_reduce_b3_kernel(Geo g, const int4* __restrict__ split,
+// adj_reduce_f3_kernel). CTA = 256 threads: thread (cell, entry pair), one
+// float4 of each partial, four partials in flight.
+__global__ void __launch_bounds__(256) adj_reduce_b3_kernel(Geo g, const int4* __restrict__ split,
                                                             const float* __restrict__ partial,
                                                             float* __restrict__ gridv) {
   const int4 sp = split[blockIdx.x];
   const int cg = blockIdx.y, ncg = gridDim.y, c0 = cg * 8;
   const int ncoil = (int)min(8ll, g.nbatch - c0);
-  const int half = threadIdx.x >> 6, cell = threadIdx.x & 63;
+  const int cell = threadIdx.x >> 2, q = threadIdx.x & 3;  // entries 2q, 2q + 1
   int bx, by, bz;
   block_origin(g, sp.x, bx, by, bz);
-  const long long step = (long long)ncg * 64 * 16 / 4;  // float4s between consecutive partials
-  const float4* src =
-      reinterpret_cast<const float4*>(partial + (((long long)sp.y * ncg + cg) * 64 + cell) * 16 + half * 8);
-  float s[8], cmp[8];
-  {
-    const float4 a = __ldg(src), b = __ldg(src + 1);
-    s[0] = a.x, s[1] = a.y, s[2] = a.z, s[3] = a.w, s[4] = b.x, s[5] = b.y, s[6] = b.z, s[7] = b.w;
+  const long long step = (long long)ncg * 64 * 4;  // float4s between consecutive partials
+  const float4* src = reinterpret_cast<const float4*>(partial + ((long long)sp.y * ncg + cg) * 64 * 16) + threadIdx.x;
+  float4 sum = __ldg(src), comp = make_float4(0.f, 0.f, 0.f, 0.f);
+  int k = 1;
+  for (; k + 4 <= sp.z; k += 4) {
+    float4 v[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) v[i] = __ldg(src + (k + i) * step);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      comp_add(sum.x, comp.x, v[i].x);
+      comp_add(sum.y, comp.y, v[i].y);
+      comp_add(sum.z, comp.z, v[i].z);
+      comp_add(sum.w, comp.w, v[i].w);
+    }
   }
-#pragma unroll
-  for (int i = 0; i < 8; ++i) cmp[i] = 0.f;
-  for (int k = 1; k < sp.z; ++k) {
-    const float4 a = __ldg(src + k * step), b = __ldg(src + k * step + 1);
-    const float v[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
-#pragma unroll
-    for (int i = 0; i < 8; ++i) comp_add(s[i], cmp[i], v[i]);
+  for (; k < sp.z; ++k) {
+    const float4 v = __ldg(src + k * step);
+    comp_add(sum.x, comp.x, v.x);
+    comp_add(sum.y, comp.y, v.y);
+    comp_add(sum.z, comp.z, v.z);
+    comp_add(sum.w, comp.w, v.w);
   }
   const int x = kBE * bx + (cell >> 4), y = kBE * by + ((cell >> 2) & 3), z = kBE * bz + (cell & 3);
   if (x >= g.N[0] || y >= g.N[1] || z >= g.N[2]) return;
   const long long gvol = (long long)g.N[0] * g.N[1] * g.N[2];
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const int c = half * 4 + k;
-    if (c >= ncoil) break;
-    *reinterpret_cast<float2*>(gridv + ((long long)(c0 + c) * gvol + ((long long)x * g.N[1] + y) * g.N[2] + z) * 2) =
-        make_float2(s[2 * k] + cmp[2 * k], s[2 * k + 1] + cmp[2 * k + 1]);
-  }
+  float* dst = gridv + ((long long)(c0 + 2 * q) * gvol + ((long long)x * g.N[1] + y) * g.N[2] + z) * 2;
+  if (2 * q < ncoil) *reinterpret_cast<float2*>(dst) = make_float2(sum.x + comp.x, sum.y + comp.y);
+  if (2 * q + 1 < ncoil) *reinterpret_cast<float2*>(dst + gvol * 2) = make_float2(sum.z + comp.z, sum.w + comp.w);
 }
 
 // 2D gridding. The view of one dimension of a record from a 16-wide tile at o
@@ -3246,7 +3250,10 @@ extern "C" int tlgb_interp_plan_build(const tlgb_interp_desc* d, const float* lo
   // Block lists (3D 8-entry gridding): (point, block) pairs from the tap
   // records, sorted stably by block; work items of at most kBlkPart entries
   // (dense blocks split into parts summed in order afterwards) and runs of
-  // up to kZeroRun empty blocks. Items go heaviest first, empty runs last.
+  // up to kZeroRun empty blocks, in block order. A point's blocks are
+  // neighbours, so in block order its record and values are read again
+  // while they are still in L2 (in heaviest-first order nearly every read of
+  // them went to DRAM).
   uint32_t Eb = 0;
   std::vector<int4> bitems, bsplit;
   int64_t n_bpartials = 0;
@@ -3273,15 +3280,14 @@ extern "C" int tlgb_interp_plan_build(const tlgb_interp_desc* d, const float* lo
     TLGB_CUDA(cudaMemcpyAsync(hb.data(), hist, hb.size() * 4, cudaMemcpyDeviceToHost, s));
     TLGB_CUDA(cudaStreamSynchronize(s));
     int64_t bpos = 0;
-    std::vector<int4> zero_runs;
     for (int64_t b = 0; b < L.nblocks; ++b) {
       const int64_t n = hb[(size_t)b];
       if (n == 0) {
-        int4* last = zero_runs.empty() ? nullptr : &zero_runs.back();
-        if (last && last->x - last->w == b && -last->w < kZeroRun)
-          --last->w;  // extends the run ending at block b - 1
+        int4* last = bitems.empty() ? nullptr : &bitems.back();
+        if (last && last->y == last->z && last->x - last->w == b && -last->w < kZeroRun)
+          --last->w;  // extends the run of empty blocks ending at block b - 1
         else
-          zero_runs.push_back(make_int4((int)b, (int)bpos, (int)bpos, -1));
+          bitems.push_back(make_int4((int)b, (int)bpos, (int)bpos, -1));
         continue;
       }
       if (n <= kBlkPart) {
@@ -3296,8 +3302,6 @@ extern "C" int tlgb_interp_plan_build(const tlgb_interp_desc* d, const float* lo
       }
       bpos += n;
     }
-    std::stable_sort(bitems.begin(), bitems.end(), heavier);
-    bitems.insert(bitems.end(), zero_runs.begin(), zero_runs.end());
     if ((int64_t)bitems.size() > L.max_blk_items) TLGB_FAIL(TLGB_ERR_DEVICE, "block work list larger than its bound");
     if (!bitems.empty())
       TLGB_CUDA(cudaMemcpyAsync(P + L.off_blk_items, bitems.data(), bitems.size() * 16, cudaMemcpyHostToDevice, s));
@@ -3532,7 +3536,7 @@ int launch_adj_b3(const Geo& g, const tlgb_interp_plan_info* info, const char* P
   TLGB_CHECK_LAUNCH();
   if (info->n_blk_split > 0) {
     dim3 g2((unsigned)info->n_blk_split, (unsigned)ncg);
-    adj_reduce_b3_kernel<<<g2, 128, 0, s>>>(g, (const int4*)(P + info->off_blk_split), (const float*)scratch,
+    adj_reduce_b3_kernel<<<g2, 256, 0, s>>>(g, (const int4*)(P + info->off_blk_split), (const float*)scratch,
                                             (float*)grid);
     TLGB_CHECK_LAUNCH();
   }
