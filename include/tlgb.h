@@ -127,6 +127,7 @@ typedef struct tlgb_interp_plan_info {
   int64_t off_blk_entries;
   int64_t off_blk_items;
   int64_t off_blk_split;
+  int64_t off_blk_rows;   /* per point, the tap weights over each block it meets */
 } tlgb_interp_plan_info;
 
 /* Bytes of device memory needed by a plan for this description (worst case)

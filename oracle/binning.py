@@ -22,7 +22,9 @@ restates, independently of the CUDA code, which pairs exist and their order:
 3D plans of the 8-entry gridding also list (point, block) pairs for output
 blocks of 4 x 4 x 4 cells (``block_pairs``): a point pairs with every block
 that one of its valid taps lands in, keyed ``(b0 * nb1 + b1) * nb2 + b2``,
-in point order within a block.
+in point order within a block. Each pair is stored as
+``point | (i0 | i1 << 1 | i2 << 2) << 29``, i_e the index of the block among
+the point's blocks along dim e in window order.
 """
 
 from __future__ import annotations
@@ -97,8 +99,9 @@ def plan_pairs(locs: torch.Tensor, grid_size, width, kernel: str = "kaiser_besse
 
 
 def block_pairs(locs: torch.Tensor, grid_size, width, kernel: str = "kaiser_bessel", pad_mode: str = "circular"):
-    """(keys, points) of the 3D block lists: every (point, 4^3-cell block)
-    pair, sorted by block key and, within a block, by point index."""
+    """(keys, entries) of the 3D block lists: every (point, 4^3-cell block)
+    pair, sorted by block key and, within a block, by point index; entries
+    as stored by the plan (point index and the block's index per dim)."""
     assert len(grid_size) == 3
     N = tuple(int(n) for n in grid_size)
     nb = tuple(-(-n // 4) for n in N)
@@ -123,7 +126,7 @@ def block_pairs(locs: torch.Tensor, grid_size, width, kernel: str = "kaiser_bess
             out[idx, cnt[idx]] = bk[idx]
             cnt = cnt + add.to(torch.int64)
         blocks.append(out)
-    keys, pts = [], []
+    keys, pts, sels = [], [], []
     pidx = torch.arange(P)
     for i0 in range(3):
         for i1 in range(3):
@@ -132,7 +135,9 @@ def block_pairs(locs: torch.Tensor, grid_size, width, kernel: str = "kaiser_bess
                 m = ok & (b0 >= 0) & (b1 >= 0) & (b2 >= 0)
                 keys.append(((b0 * nb[1] + b1) * nb[2] + b2)[m])
                 pts.append(pidx[m])
+                sels.append(torch.full((int(m.sum()),), i0 | i1 << 1 | i2 << 2, dtype=torch.int64))
     keys = torch.cat(keys).numpy()
     pts = torch.cat(pts).numpy()
-    order = np.lexsort((pts, keys))
-    return keys[order], pts[order]
+    sels = torch.cat(sels).numpy()
+    order = np.lexsort((pts, keys))  # by block, then by point
+    return keys[order], pts[order] | (sels[order] << 29)

@@ -46,12 +46,13 @@ def test_binning_invariants():
 def test_block_list_invariants():
     gen = torch.Generator().manual_seed(2)
     locs = torch.rand(3000, 3, generator=gen) * 40 - 4
-    keys, pts = OB.block_pairs(locs, (32, 32, 32), 4.0)
+    keys, ent = OB.block_pairs(locs, (32, 32, 32), 4.0)
+    pts = ent & ((1 << 29) - 1)
     assert np.all(np.diff(keys) >= 0)
     same = np.diff(keys) == 0
     assert np.all(np.diff(pts)[same] > 0)  # point order inside a block
     # a window of 4 (5 at exact integers) taps meets at most 2 blocks of 4 per axis
-    assert np.bincount(pts).max() <= 8
+    assert np.bincount(pts).max() <= 8 and (ent >> 29).max() <= 7
     assert 4.5 < len(keys) / 3000 < 6.0  # 1.75^3 = 5.36 blocks per point on average
     # every point's blocks contain its taps: one block holds its first tap on each axis
     kt, pt = OB.plan_pairs(locs, (32, 32, 32), 4.0)

@@ -56,8 +56,8 @@ def test_block_lists_are_bit_exact(grid_size, npts, pad):
     info = plan.info
     assert int(info.n_blk_entries) == len(pts) and int(info.n_blk_items) > 0
     off = int(info.off_blk_entries)
-    got = plan.buffer[off:off + 4 * len(pts)].view(torch.int32).cpu().numpy()
-    assert np.array_equal(got, pts)
+    got = plan.buffer[off:off + 4 * len(pts)].view(torch.int32).cpu().numpy().astype(np.int64) & 0xFFFFFFFF
+    assert np.array_equal(got, pts)  # point index and block index per dim
     # work items: each block's entries exactly once, split into parts of at most 256
     items = plan.buffer[int(info.off_blk_items):int(info.off_blk_items) + 16 * int(info.n_blk_items)]
     items = items.view(torch.int32).reshape(-1, 4).cpu().numpy()

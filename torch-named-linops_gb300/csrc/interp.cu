@@ -991,11 +991,13 @@ __global__ void point_records_kernel(Geo g, const float* __restrict__ locs, PRec
 constexpr int kBE = 4;         // block edge in cells, every dimension
 constexpr int kBlkPart = 256;  // entries per work item: denser blocks are split into parts
 constexpr int kZeroRun = 16;   // empty blocks written by one work item
+constexpr int kSelShift = 29;  // entry = point | (its block's index per dim, 3 bits) << 29
 
 __host__ __device__ __forceinline__ int blocks_along(int n) { return (n + kBE - 1) / kBE; }
 
 // Distinct blocks met along one dim by the cells st .. st+c-1 of a window
-// (st in [0, N); wrapped once in circular mode, where N >= 16 > c).
+// (st in [0, N); wrapped once in circular mode, where N >= 16 > c). At most
+// 2: 5 taps over blocks of 4 cells (circular grids are multiples of 4).
 __device__ __forceinline__ int axis_blocks(const Geo& g, int e, int st, int c, int* bl) {
   int cnt = 0;
   for (int k = 0; k < c; ++k) {
@@ -1039,9 +1041,43 @@ __global__ void blk_emit_kernel(Geo g, const PRec* __restrict__ precs, const uin
     for (int j = 0; j < nc[1]; ++j)
       for (int k = 0; k < nc[2]; ++k) {
         keys[o] = ((uint32_t)bl[0][i] * nb1 + (uint32_t)bl[1][j]) * nb2 + (uint32_t)bl[2][k];
-        vals[o] = (int32_t)p;
+        vals[o] = (int32_t)((uint32_t)p | (uint32_t)(i | j << 1 | k << 2) << kSelShift);
         ++o;
       }
+}
+
+// The tap weights of a point over each block it meets: per dim the rows of
+// its first and second block (in axis_blocks order), 4 cells each, from the
+// coordinate as the tap records; a cell outside the window holds -0.0 (valid
+// weights are >= +0), so the sign bit tells the gridding which cells the
+// window covers.
+__global__ void blk_rows_kernel(Geo g, const float* __restrict__ locs, const PRec* __restrict__ precs,
+                                float4* __restrict__ rows) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= g.npts) return;
+  const PRec R = precs[p];
+  for (int e = 0; e < 3; ++e) {
+    const int ce = (R.cnt >> (4 * e)) & 15;
+    int bl[3] = {0, 0, 0};
+    const int nb = ce ? axis_blocks(g, e, R.st[e], ce, bl) : 0;
+    const float x = load_coord(g, locs, p, e);
+    const int lower = coord_ok(x) ? lower_of(g, e, x) : 0;
+    for (int i = 0; i < 2; ++i) {
+      float r[4];
+      for (int q = 0; q < 4; ++q) {
+        const int v = kBE * bl[i] + q;
+        int k = v - lower;
+        if (g.pad == TLGB_PAD_CIRCULAR) k = wrapi(k, g.N[e]);
+        float w = -0.0f;
+        if (i < nb && v < g.N[e] && k >= 0 && k < g.NT[e]) {
+          const Tap t = tap_eval(g, e, x, lower, k);
+          if (t.valid) w = kern_value_approx(g.kernel, fabsf(t.d), g.beta);
+        }
+        r[q] = w;
+      }
+      rows[p * 6 + 2 * e + i] = make_float4(r[0], r[1], r[2], r[3]);
+    }
+  }
 }
 
 // View of one dimension of a record from the tile at o (8 wide, grid N):
@@ -1488,18 +1524,18 @@ __global__ void __launch_bounds__(256, 4) adj_f3_kernel(Geo g, const int4* __res
 // held in registers, lane (x, y, z pair) owning the cells (x, y, 2 zp) and
 // (x, y, 2 zp + 1) for all 8 entries. No two threads own the same value and
 // the warps of a CTA never wait for one another. The warp walks its block's
-// list in chunks of 32 entries: each lane copies one entry's point record
-// and values into the warp's staging slots (cp.async), then turns the record
-// into the block's rows of tap weights; every lane then applies the chunk's
-// entries in list order, 16 packed (re, im) FMAs per entry. Each cell
-// therefore sums its contributions in plan order, starting from zero:
-// bit-identical run to run. Entries whose values are not finite update only
-// the cells of their window (the zero weights elsewhere would spread a NaN
-// or Inf), and exact-integer coordinates (5 taps in a dimension) take their
-// weights from the coordinates instead of the 4-weight record.
+// list in chunks of 32 entries: each lane copies one entry's values and the
+// point's three rows of tap weights over this block (from the plan) into
+// the warp's staging slots (cp.async) and multiplies the x and y rows out;
+// every lane then applies the chunk's entries in list order, 16 packed
+// (re, im) FMAs per entry. Each cell therefore sums its contributions in
+// plan order, starting from zero: bit-identical run to run. Entries whose
+// values are not finite update only the cells of their window (the zero
+// weights elsewhere would spread a NaN or Inf); the rows mark the cells
+// outside the window with -0.0.
 constexpr int kBC = 32;  // entries per chunk (one per lane while staging)
-constexpr int kBS = 44;  // floats per staging slot: rows 0-15 | values 16-31 | z row 32-35 | flags 36;
-                         // 44 keeps the lanes' 16-byte slot stores free of bank conflicts
+constexpr int kBS = 44;  // floats per staging slot: x*y weights 0-15 | values 16-31 | z, x, y rows 32-43
+                         // (44 keeps the lanes' 16-byte slot stores free of bank conflicts)
 
 __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
@@ -1509,49 +1545,6 @@ __device__ __forceinline__ void cp_async8(void* dst, const void* src) {
 }
 __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
-}
-
-// Tap weights of the 4 cells b0 .. b0+3 of one dim, from a record dimension
-// with at most 4 taps (first tap st, count c, weights w4); bit i of valid is
-// set when cell b0 + i is in the window.
-__device__ __forceinline__ float4 block_row(const Geo& g, int e, int b0, int st, int c, const float4& w4,
-                                            unsigned& valid) {
-  const bool circ = g.pad == TLGB_PAD_CIRCULAR;
-  int d = b0 - st;
-  if (circ && d < 0) d += g.N[e];
-  float r[4];
-  valid = 0;
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    int t = d + i;
-    if (circ && t >= g.N[e]) t -= g.N[e];
-    const bool ok = b0 + i < g.N[e] && t >= 0 && t < c;
-    r[i] = ok ? pick4(w4, t) : 0.f;
-    valid |= (ok ? 1u : 0u) << i;
-  }
-  return make_float4(r[0], r[1], r[2], r[3]);
-}
-
-// The same from the coordinate (any number of taps; used for 5-tap windows)
-__device__ __forceinline__ float4 block_row_coord(const Geo& g, int e, int b0, float x, unsigned& valid) {
-  const int lower = lower_of(g, e, x);
-  float r[4];
-  valid = 0;
-  for (int i = 0; i < 4; ++i) {
-    const int v = b0 + i;
-    int k = v - lower;
-    if (g.pad == TLGB_PAD_CIRCULAR) k = wrapi(k, g.N[e]);
-    bool ok = v < g.N[e] && k >= 0 && k < g.NT[e];
-    float w = 0.f;
-    if (ok) {
-      const Tap t = tap_eval(g, e, x, lower, k);
-      ok = t.valid;
-      if (ok) w = kern_value_approx(g.kernel, fabsf(t.d), g.beta);
-    }
-    r[i] = w;
-    valid |= (ok ? 1u : 0u) << i;
-  }
-  return make_float4(r[0], r[1], r[2], r[3]);
 }
 
 __device__ __forceinline__ void block_origin(const Geo& g, int key, int& bx, int& by, int& bz) {
@@ -1583,10 +1576,10 @@ __device__ __forceinline__ void block_store(const Geo& g, float* __restrict__ gr
   }
 }
 
-__global__ void __launch_bounds__(256, 4) adj_b3_kernel(Geo g, const int4* __restrict__ items, int nitems,
-                                                        const int32_t* __restrict__ bentries,
-                                                        const PRec* __restrict__ precs,
-                                                        const float* __restrict__ locs, const float2* __restrict__ vals,
+__global__ void __launch_bounds__(256, 3) adj_b3_kernel(Geo g, const int4* __restrict__ items, int nitems,
+                                                        const uint32_t* __restrict__ bentries,
+                                                        const float4* __restrict__ rows,
+                                                        const float2* __restrict__ vals,
                                                         const float4* __restrict__ tv, float* __restrict__ gridv,
                                                         float* __restrict__ partial) {
   extern __shared__ __align__(16) float bsm[];
@@ -1614,13 +1607,14 @@ __global__ void __launch_bounds__(256, 4) adj_b3_kernel(Geo g, const int4* __res
   for (int c = it.y; c < it.z; c += kBC) {
     const int n = min(kBC, it.z - c);
     float* sl = S + lane * kBS;
-    int p = 0;
     if (lane < n) {
-      p = bentries[c + lane];
+      const uint32_t en = bentries[c + lane];
+      long long p = en & ((1u << kSelShift) - 1u);
       if (!TLGB_IN_RANGE(p, g.npts)) p = 0;
-      const float4* rsrc = reinterpret_cast<const float4*>(precs + p);
-#pragma unroll
-      for (int q = 0; q < 4; ++q) cp_async16(sl + 4 * q, rsrc + q);
+      const float4* rsrc = rows + p * 6;
+      cp_async16(sl + 32, rsrc + 4 + ((en >> (kSelShift + 2)) & 1));  // z row
+      cp_async16(sl + 36, rsrc + 0 + ((en >> kSelShift) & 1));        // x row
+      cp_async16(sl + 40, rsrc + 2 + ((en >> (kSelShift + 1)) & 1));  // y row
       if (tv) {
         const float4* vsrc = tv + ((long long)cg * g.npts + p) * 4;
 #pragma unroll
@@ -1636,26 +1630,11 @@ __global__ void __launch_bounds__(256, 4) adj_b3_kernel(Geo g, const int4* __res
       }
     }
     cp_async_wait_all();
-    // the lane's own entry: record -> rows of tap weights over the block
-    unsigned flags = 0;
+    // the lane's own entry: x and y rows -> their products; finite values?
+    bool nonfinite = false;
     if (lane < n) {
-      const float4* rq = reinterpret_cast<const float4*>(sl);
-      const float4 w0 = rq[0], w1 = rq[1], w2 = rq[2];
-      const int4 t = reinterpret_cast<const int4*>(sl)[3];
-      const int c_x = t.w & 15, c_y = (t.w >> 4) & 15, c_z = (t.w >> 8) & 15;
-      unsigned vx, vy, vz;
-      float4 rx, ry, rz;
-      if (c_x <= 4 && c_y <= 4 && c_z <= 4) {
-        rx = block_row(g, 0, B[0], t.x, c_x, w0, vx);
-        ry = block_row(g, 1, B[1], t.y, c_y, w1, vy);
-        rz = block_row(g, 2, B[2], t.z, c_z, w2, vz);
-      } else {
-        rx = block_row_coord(g, 0, B[0], load_coord(g, locs, p, 0), vx);
-        ry = block_row_coord(g, 1, B[1], load_coord(g, locs, p, 1), vy);
-        rz = block_row_coord(g, 2, B[2], load_coord(g, locs, p, 2), vz);
-      }
-      // a non-finite value turns the zero product into NaN
-      float chk = 0.f;
+      const float4 rx = *reinterpret_cast<const float4*>(sl + 36), ry = *reinterpret_cast<const float4*>(sl + 40);
+      float chk = 0.f;  // a non-finite value turns the zero product into NaN
       const float4* vq = reinterpret_cast<const float4*>(sl + 16);
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
@@ -1665,16 +1644,14 @@ __global__ void __launch_bounds__(256, 4) adj_b3_kernel(Geo g, const int4* __res
         chk = fmaf(v.z, 0.f, chk);
         chk = fmaf(v.w, 0.f, chk);
       }
-      flags = (chk == 0.f ? 0u : 1u) | (vx << 4) | (vy << 8) | (vz << 12);
+      nonfinite = !(chk == 0.f);
       float4* wq = reinterpret_cast<float4*>(sl);
       wq[0] = make_float4(rx.x * ry.x, rx.x * ry.y, rx.x * ry.z, rx.x * ry.w);
       wq[1] = make_float4(rx.y * ry.x, rx.y * ry.y, rx.y * ry.z, rx.y * ry.w);
       wq[2] = make_float4(rx.z * ry.x, rx.z * ry.y, rx.z * ry.z, rx.z * ry.w);
       wq[3] = make_float4(rx.w * ry.x, rx.w * ry.y, rx.w * ry.z, rx.w * ry.w);
-      wq[8] = rz;
-      reinterpret_cast<unsigned*>(sl)[36] = flags;
     }
-    const bool guarded = __ballot_sync(0xffffffffu, flags & 1u) != 0;
+    const unsigned guarded = __ballot_sync(0xffffffffu, nonfinite);
     __syncwarp();
     // every lane applies the chunk's entries in order
     auto visit = [&](const float* e, bool ok0, bool ok1) {
@@ -1701,12 +1678,11 @@ __global__ void __launch_bounds__(256, 4) adj_b3_kernel(Geo g, const int4* __res
     } else {
       for (int j = 0; j < n; ++j) {
         const float* e = S + j * kBS;
-        const unsigned f = reinterpret_cast<const unsigned*>(e)[36];
         bool ok0 = true, ok1 = true;
-        if (f & 1u) {
-          const bool xy = ((f >> (4 + lx)) & (f >> (8 + ly)) & 1u) != 0;
-          ok0 = xy && ((f >> (12 + 2 * zp)) & 1u);
-          ok1 = xy && ((f >> (13 + 2 * zp)) & 1u);
+        if ((guarded >> j) & 1u) {  // only the cells of the window: weights with a clear sign bit
+          const bool xy = !signbit(e[36 + lx]) && !signbit(e[40 + ly]);
+          ok0 = xy && !signbit(e[32 + 2 * zp]);
+          ok1 = xy && !signbit(e[33 + 2 * zp]);
         }
         visit(e, ok0, ok1);
       }
@@ -2867,7 +2843,7 @@ struct PlanLayout {
   int64_t e_max, max_fwd, max_adj, ntiles;
   int64_t off_entries, off_fwd, off_adj, off_split, off_recs, bytes;
   // block lists of the 3D 8-entry gridding (off_blk_entries == 0: none)
-  int64_t nblocks, eb_max, max_blk_items, off_blk_entries, off_blk_items, off_blk_split;
+  int64_t nblocks, eb_max, max_blk_items, off_blk_entries, off_blk_items, off_blk_split, off_blk_rows;
   // tmp
   int64_t t_cnt, t_keys, t_keys2, t_vals2, t_counts, t_hist, t_total, t_bytes;
 };
@@ -2959,23 +2935,20 @@ bool records_ok(const Geo& g) {
 }
 
 // 3D geometries whose plans also carry block lists (adj_b3_kernel): the
-// records' geometry, and in circular mode every dim at least 16 cells, so
-// that a wrapped window meets a block at most once.
+// records' geometry, and in circular mode every dim a multiple of 4 cells
+// and at least 16, so that a wrapped window meets at most 2 blocks per dim
+// and each of them once.
 bool blocks_ok(const Geo& g) {
-  if (g.ndim != 3 || !records_ok(g)) return false;
-  if (g.pad == TLGB_PAD_CIRCULAR && std::min(g.N[0], std::min(g.N[1], g.N[2])) < 16) return false;
+  if (g.ndim != 3 || !records_ok(g) || g.npts >= (1ll << kSelShift)) return false;
+  if (g.pad == TLGB_PAD_CIRCULAR)
+    for (int e = 0; e < 3; ++e)
+      if (g.N[e] < 16 || g.N[e] % kBE != 0) return false;
   const int64_t nb = (int64_t)blocks_along(g.N[0]) * blocks_along(g.N[1]) * blocks_along(g.N[2]);
   return nb < (1ll << 31);
 }
 
-// Blocks one window can meet along a dim: 2 (at most 5 taps over 4 cells),
-// 3 where a circular window crosses a ragged last block and the wrap.
-int64_t max_blocks_per_dim(const Geo& g, int e) {
-  const int nb = blocks_along(g.N[e]);
-  if (nb == 1) return 1;
-  if (g.pad == TLGB_PAD_CIRCULAR && g.N[e] % kBE != 0) return std::min(3, nb);
-  return 2;
-}
+// Blocks one window can meet along a dim: 2 (at most 5 taps over 4 cells)
+int64_t max_blocks_per_dim(const Geo& g, int e) { return blocks_along(g.N[e]) == 1 ? 1 : 2; }
 
 // The kernel, norm and beta a plan's records hold weights for
 int64_t kernel_key(const Geo& g) {
@@ -3005,7 +2978,7 @@ PlanLayout layout(const Geo& g) {
     o = align_up(o + (size_t)g.npts * 64, 256);
   }
   L.nblocks = L.eb_max = L.max_blk_items = 0;
-  L.off_blk_entries = L.off_blk_items = L.off_blk_split = 0;
+  L.off_blk_entries = L.off_blk_items = L.off_blk_split = L.off_blk_rows = 0;
   if (blocks_ok(g) && g.npts > 0) {
     L.nblocks = (int64_t)blocks_along(g.N[0]) * blocks_along(g.N[1]) * blocks_along(g.N[2]);
     L.eb_max = g.npts * max_blocks_per_dim(g, 0) * max_blocks_per_dim(g, 1) * max_blocks_per_dim(g, 2);
@@ -3016,6 +2989,8 @@ PlanLayout layout(const Geo& g) {
     o = align_up(o + (size_t)L.max_blk_items * 16, 256);
     L.off_blk_split = o;
     o = align_up(o + (size_t)(L.nblocks + 1) * 16, 256);
+    L.off_blk_rows = o;
+    o = align_up(o + (size_t)g.npts * 96, 256);
   }
   L.bytes = o;
   const int64_t pairs = std::max<int64_t>(std::max(L.e_max, L.eb_max), 1);  // sort buffers serve both lists
@@ -3266,6 +3241,8 @@ extern "C" int tlgb_interp_plan_build(const tlgb_interp_desc* d, const float* lo
     TLGB_TRY(exclusive_scan_u32(cnt, cnt, g.npts, total, counts, s));
     blk_emit_kernel<<<nb, 256, 0, s>>>(g, recs, cnt, keys, bentries);
     TLGB_CHECK_LAUNCH();
+    blk_rows_kernel<<<nb, 256, 0, s>>>(g, locs, recs, (float4*)(P + L.off_blk_rows));
+    TLGB_CHECK_LAUNCH();
     TLGB_CUDA(cudaMemcpyAsync(&Eb, total, 4, cudaMemcpyDeviceToHost, s));
     TLGB_CUDA(cudaStreamSynchronize(s));
     int bbits = 1;
@@ -3338,6 +3315,7 @@ extern "C" int tlgb_interp_plan_build(const tlgb_interp_desc* d, const float* lo
     info->off_blk_entries = L.off_blk_entries;
     info->off_blk_items = L.off_blk_items;
     info->off_blk_split = L.off_blk_split;
+    info->off_blk_rows = L.off_blk_rows;
   }
   return TLGB_OK;
 }
@@ -3517,8 +3495,8 @@ int launch_adj_b3(const Geo& g, const tlgb_interp_plan_info* info, const char* P
   const int64_t ncg = cdiv(g.nbatch, 8);
   const size_t sm = 8 * kBC * kBS * sizeof(float);
   TLGB_TRY(set_smem(adj_b3_kernel, sm));
-  // 16-byte asynchronous copies of the point records and transposed values
-  if (((uintptr_t)(P + info->off_records) & 15) || ((uintptr_t)scratch & 15))
+  // 16-byte asynchronous copies of the weight rows and transposed values
+  if (((uintptr_t)P & 15) || ((uintptr_t)scratch & 15))
     TLGB_FAIL(TLGB_ERR_INVALID, "interp adjoint: plan and scratch must be 16-byte aligned");
   if ((uintptr_t)vals & 7) TLGB_FAIL(TLGB_ERR_INVALID, "interp adjoint: values must be 8-byte aligned");
   const float4* tv = nullptr;
@@ -3531,8 +3509,8 @@ int launch_adj_b3(const Geo& g, const tlgb_interp_plan_info* info, const char* P
   }
   dim3 grd((unsigned)cdiv(info->n_blk_items, 8), (unsigned)ncg);
   adj_b3_kernel<<<grd, 256, sm, s>>>(g, (const int4*)(P + info->off_blk_items), (int)info->n_blk_items,
-                                    (const int32_t*)(P + info->off_blk_entries), (const PRec*)(P + info->off_records),
-                                    locs, (const float2*)vals, tv, (float*)grid, (float*)scratch);
+                                    (const uint32_t*)(P + info->off_blk_entries), (const float4*)(P + info->off_blk_rows),
+                                    (const float2*)vals, tv, (float*)grid, (float*)scratch);
   TLGB_CHECK_LAUNCH();
   if (info->n_blk_split > 0) {
     dim3 g2((unsigned)info->n_blk_split, (unsigned)ncg);

@@ -70,6 +70,7 @@ class PlanInfo(ctypes.Structure):
         ("off_blk_entries", ctypes.c_int64),
         ("off_blk_items", ctypes.c_int64),
         ("off_blk_split", ctypes.c_int64),
+        ("off_blk_rows", ctypes.c_int64),
     ]
 
 
