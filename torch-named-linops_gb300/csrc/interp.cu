@@ -1520,22 +1520,30 @@ __global__ void __launch_bounds__(256, 4) adj_f3_kernel(Geo g, const int4* __res
 
 // ------------------------------------------------- block gridding (3D, 8 entries)
 //
-// One warp per work item: a 4 x 4 x 4-cell output block x 8 complex entries
-// held in registers, lane (x, y, z pair) owning the cells (x, y, 2 zp) and
-// (x, y, 2 zp + 1) for all 8 entries. No two threads own the same value and
-// the warps of a CTA never wait for one another. The warp walks its block's
+// A CTA takes 64 consecutive work items (blocks, parts of dense blocks, runs
+// of empty blocks); its warps take them one at a time from a shared counter,
+// so a dense block costs one warp, not the CTA, and which warp takes an item
+// does not change its result. A warp holds its item's 4 x 4 x 4-cell output
+// block x 8 complex entries as the accumulators of warp-level tensor-core
+// products (mma.sync m16n8k8, tf32 inputs, fp32 accumulation): the block's
+// 64 cells are the 4 row tiles (one per x, rows (y, z)), the 8 entries'
+// real and imaginary parts the 2 column tiles. The warp walks the block's
 // list in chunks of 32 entries: each lane copies one entry's values and the
-// point's three rows of tap weights over this block (from the plan) into
-// the warp's staging slots (cp.async) and multiplies the x and y rows out;
-// every lane then applies the chunk's entries in list order, 16 packed
-// (re, im) FMAs per entry. Each cell therefore sums its contributions in
-// plan order, starting from zero: bit-identical run to run. Entries whose
-// values are not finite update only the cells of their window (the zero
-// weights elsewhere would spread a NaN or Inf); the rows mark the cells
-// outside the window with -0.0.
-constexpr int kBC = 32;  // entries per chunk (one per lane while staging)
-constexpr int kBS = 44;  // floats per staging slot: x*y weights 0-15 | values 16-31 | z, x, y rows 32-43
-                         // (44 keeps the lanes' 16-byte slot stores free of bank conflicts)
+// point's three rows of tap weights over this block (from the plan) into the
+// warp's staging slots (cp.async). Then each group of 8 entries is one rank-8
+// update of the block: weights (x row * y row * z row, built in registers)
+// times values. fp32 accuracy from tf32 inputs: each operand is split into a
+// high and a low tf32 part and the update is hi*hi + hi*lo + lo*hi (the
+// lo*lo term is below 2^-22 of the product). The result depends only on the
+// plan's order: bit-identical run to run. A chunk with a non-finite value is
+// applied entry by entry on the CUDA cores instead, each such entry to the
+// cells of its window only (a zero weight would carry its NaN or Inf to the
+// whole block); the rows mark the cells outside the window with -0.0.
+constexpr int kBC = 32;       // entries per chunk (one per lane while staging)
+constexpr int kB3Items = 64;  // work items per CTA, taken by its warps one at a time
+constexpr int kBS = 40;       // floats per staged entry: x row 0-3 | y row 4-7 | z row 8-11 | values 16-31
+                              // (40: the tensor-core operand loads of a group of 8 entries are free of
+                              // bank conflicts)
 
 __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
@@ -1547,6 +1555,21 @@ __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
 }
 
+// x = hi + lo with hi, lo tf32 (round to nearest); x - hi is exact in fp32
+__device__ __forceinline__ void split_tf32(float x, unsigned& hi, unsigned& lo) {
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(hi) : "f"(x));
+  const float r = x - __uint_as_float(hi);
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(lo) : "f"(r));
+}
+
+// d += a * b, m16n8k8, tf32 inputs, fp32 accumulators
+__device__ __forceinline__ void mma_tf32(float (&d)[4], const unsigned (&a)[4], unsigned b0, unsigned b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
 __device__ __forceinline__ void block_origin(const Geo& g, int key, int& bx, int& by, int& bz) {
   const int nb1 = blocks_along(g.N[1]), nb2 = blocks_along(g.N[2]);
   bz = key % nb2;
@@ -1555,23 +1578,30 @@ __device__ __forceinline__ void block_origin(const Geo& g, int key, int& bx, int
   bx = t / nb1;
 }
 
-// Stores the lane's two cells (x, y, z0), (x, y, z0 + 1) of entries 0..ncoil-1.
-__device__ __forceinline__ void block_store(const Geo& g, float* __restrict__ gridv, int c0, int ncoil, int x, int y,
-                                            int z0, const float2 (&a0)[8], const float2 (&a1)[8]) {
-  if (x >= g.N[0] || y >= g.N[1] || z0 >= g.N[2]) return;
+// The accumulator fragment of lane (g8, t4): D[m][nt][2h + c] is cell
+// (x m, y (g8 >> 2) + 2h, z g8 & 3) of the block, entry 4 nt + t4, real (c = 0)
+// or imaginary part. Stores the lane's cells of entries below ncoil.
+__device__ __forceinline__ void frag_store(const Geo& g, float* __restrict__ gridv, int c0, int ncoil, int B0, int B1,
+                                           int B2, int g8, int t4, const float (&D)[4][2][4]) {
   const long long gvol = (long long)g.N[0] * g.N[1] * g.N[2];
-  const bool two = z0 + 1 < g.N[2];
-  // 16-byte stores need an even Z extent (z0 is even) and an aligned base
-  const bool vec = two && (g.N[2] & 1) == 0 && (reinterpret_cast<uintptr_t>(gridv) & 15) == 0;
+  const int z = B2 + (g8 & 3);
+  if (z >= g.N[2]) return;
 #pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    if (k >= ncoil) break;
-    float* row = gridv + ((long long)(c0 + k) * gvol + ((long long)x * g.N[1] + y) * g.N[2] + z0) * 2;
-    if (vec) {
-      *reinterpret_cast<float4*>(row) = make_float4(a0[k].x, a0[k].y, a1[k].x, a1[k].y);
-    } else {
-      *reinterpret_cast<float2*>(row) = a0[k];
-      if (two) *reinterpret_cast<float2*>(row + 2) = a1[k];
+  for (int m = 0; m < 4; ++m) {
+    const int x = B0 + m;
+    if (x >= g.N[0]) break;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int y = B1 + (g8 >> 2) + 2 * h;
+      if (y >= g.N[1]) continue;
+      const long long cell = ((long long)x * g.N[1] + y) * g.N[2] + z;
+#pragma unroll
+      for (int nt = 0; nt < 2; ++nt) {
+        const int e = 4 * nt + t4;
+        if (e < ncoil)
+          *reinterpret_cast<float2*>(gridv + ((long long)(c0 + e) * gvol + cell) * 2) =
+              make_float2(D[m][nt][2 * h], D[m][nt][2 * h + 1]);
+      }
     }
   }
 }
@@ -1583,122 +1613,159 @@ __global__ void __launch_bounds__(256, 3) adj_b3_kernel(Geo g, const int4* __res
                                                         const float4* __restrict__ tv, float* __restrict__ gridv,
                                                         float* __restrict__ partial) {
   extern __shared__ __align__(16) float bsm[];
+  __shared__ int next_item;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int item = blockIdx.x * 8 + warp;
-  if (item >= nitems) return;  // no CTA-wide synchronisation below
+  if (threadIdx.x == 0) next_item = 0;
+  __syncthreads();  // the only CTA-wide synchronisation: the warps then take items on their own
   float* S = bsm + warp * (kBC * kBS);
-  const int4 it = items[item];
   const int cg = blockIdx.y, c0 = cg * 8;
   const int ncoil = (int)min(8ll, g.nbatch - c0);
-  const int lx = lane >> 3, ly = (lane >> 1) & 3, zp = lane & 1;
-  float2 a0[8], a1[8];
+  const int g8 = lane >> 2, t4 = lane & 3;
+  const int first = blockIdx.x * kB3Items, last = min(nitems, first + kB3Items);
+  for (;;) {
+    int item = 0;
+    if (lane == 0) item = first + atomicAdd(&next_item, 1);
+    item = __shfl_sync(0xffffffffu, item, 0);
+    if (item >= last) return;
+    const int4 it = items[item];
+    float D[4][2][4];
 #pragma unroll
-  for (int k = 0; k < 8; ++k) a0[k] = a1[k] = make_float2(0.f, 0.f);
-  int bx, by, bz;
-  if (it.y == it.z) {  // a run of -it.w empty blocks
-    for (int b = 0; b < -it.w; ++b) {
-      block_origin(g, it.x + b, bx, by, bz);
-      block_store(g, gridv, c0, ncoil, kBE * bx + lx, kBE * by + ly, kBE * bz + 2 * zp, a0, a1);
+    for (int m = 0; m < 4; ++m)
+#pragma unroll
+      for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) D[m][nt][i] = 0.f;
+    int bx, by, bz;
+    if (it.y == it.z) {  // a run of -it.w empty blocks
+      for (int b = 0; b < -it.w; ++b) {
+        block_origin(g, it.x + b, bx, by, bz);
+        frag_store(g, gridv, c0, ncoil, kBE * bx, kBE * by, kBE * bz, g8, t4, D);
+      }
+      continue;
     }
-    return;
-  }
-  block_origin(g, it.x, bx, by, bz);
-  const int B[3] = {kBE * bx, kBE * by, kBE * bz};
-  for (int c = it.y; c < it.z; c += kBC) {
-    const int n = min(kBC, it.z - c);
-    float* sl = S + lane * kBS;
-    if (lane < n) {
-      const uint32_t en = bentries[c + lane];
-      long long p = en & ((1u << kSelShift) - 1u);
-      if (!TLGB_IN_RANGE(p, g.npts)) p = 0;
-      const float4* rsrc = rows + p * 6;
-      cp_async16(sl + 32, rsrc + 4 + ((en >> (kSelShift + 2)) & 1));  // z row
-      cp_async16(sl + 36, rsrc + 0 + ((en >> kSelShift) & 1));        // x row
-      cp_async16(sl + 40, rsrc + 2 + ((en >> (kSelShift + 1)) & 1));  // y row
-      if (tv) {
-        const float4* vsrc = tv + ((long long)cg * g.npts + p) * 4;
+    block_origin(g, it.x, bx, by, bz);
+    for (int c = it.y; c < it.z; c += kBC) {
+      const int n = min(kBC, it.z - c);
+      const int n8 = (n + 7) & ~7;  // the tensor-core steps read whole groups of 8 entries
+      float* sl = S + lane * kBS;
+      if (lane < n) {
+        const uint32_t en = bentries[c + lane];
+        long long p = en & ((1u << kSelShift) - 1u);
+        if (!TLGB_IN_RANGE(p, g.npts)) p = 0;
+        const float4* rsrc = rows + p * 6;
+        cp_async16(sl + 0, rsrc + 0 + ((en >> kSelShift) & 1));        // x row
+        cp_async16(sl + 4, rsrc + 2 + ((en >> (kSelShift + 1)) & 1));  // y row
+        cp_async16(sl + 8, rsrc + 4 + ((en >> (kSelShift + 2)) & 1));  // z row
+        if (tv) {
+          const float4* vsrc = tv + ((long long)cg * g.npts + p) * 4;
 #pragma unroll
-        for (int q = 0; q < 4; ++q) cp_async16(sl + 16 + 4 * q, vsrc + q);
+          for (int q = 0; q < 4; ++q) cp_async16(sl + 16 + 4 * q, vsrc + q);
+        } else {
+#pragma unroll
+          for (int k = 0; k < 8; ++k) {
+            if (k < ncoil)
+              cp_async8(sl + 16 + 2 * k, vals + (long long)(c0 + k) * g.npts + p);
+            else
+              *reinterpret_cast<float2*>(sl + 16 + 2 * k) = make_float2(0.f, 0.f);
+          }
+        }
+      } else if (lane < n8) {  // padding entries of the last group: zero weights and values
+        const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        float4* q4 = reinterpret_cast<float4*>(sl);
+        q4[0] = q4[1] = q4[2] = z4;
+        q4[4] = q4[5] = q4[6] = q4[7] = z4;
+      }
+      cp_async_wait_all();
+      bool nonfinite = false;
+      if (lane < n) {  // a non-finite value turns the zero product into NaN
+        float chk = 0.f;
+        const float4* vq = reinterpret_cast<const float4*>(sl + 16);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const float4 v = vq[q];
+          chk = fmaf(v.x, 0.f, chk);
+          chk = fmaf(v.y, 0.f, chk);
+          chk = fmaf(v.z, 0.f, chk);
+          chk = fmaf(v.w, 0.f, chk);
+        }
+        nonfinite = !(chk == 0.f);
+      }
+      const unsigned guarded = __ballot_sync(0xffffffffu, nonfinite);
+      __syncwarp();
+      if (!guarded) {
+        for (int kk = 0; kk < n8; kk += 8) {  // entries kk + t4 and kk + t4 + 4 of this lane's fragments
+          const float* e0 = S + (kk + t4) * kBS;
+          const float* e1 = e0 + 4 * kBS;
+          unsigned bh[2][2], bl[2][2];
+#pragma unroll
+          for (int nt = 0; nt < 2; ++nt) {
+            split_tf32(e0[16 + 8 * nt + g8], bh[nt][0], bl[nt][0]);
+            split_tf32(e1[16 + 8 * nt + g8], bh[nt][1], bl[nt][1]);
+          }
+          const float4 x0 = *reinterpret_cast<const float4*>(e0), x1 = *reinterpret_cast<const float4*>(e1);
+          const float z0 = e0[8 + (g8 & 3)], z1 = e1[8 + (g8 & 3)];
+          const float yz0a = e0[4 + (g8 >> 2)] * z0, yz0b = e0[6 + (g8 >> 2)] * z0;
+          const float yz1a = e1[4 + (g8 >> 2)] * z1, yz1b = e1[6 + (g8 >> 2)] * z1;
+          const float xs0[4] = {x0.x, x0.y, x0.z, x0.w}, xs1[4] = {x1.x, x1.y, x1.z, x1.w};
+#pragma unroll
+          for (int m = 0; m < 4; ++m) {
+            unsigned ah[4], al[4];
+            split_tf32(xs0[m] * yz0a, ah[0], al[0]);
+            split_tf32(xs0[m] * yz0b, ah[1], al[1]);
+            split_tf32(xs1[m] * yz1a, ah[2], al[2]);
+            split_tf32(xs1[m] * yz1b, ah[3], al[3]);
+#pragma unroll
+            for (int nt = 0; nt < 2; ++nt) {
+              mma_tf32(D[m][nt], ah, bh[nt][0], bh[nt][1]);
+              mma_tf32(D[m][nt], ah, bl[nt][0], bl[nt][1]);
+              mma_tf32(D[m][nt], al, bh[nt][0], bh[nt][1]);
+            }
+          }
+        }
       } else {
+        // entry by entry on the CUDA cores, in order; a non-finite entry only
+        // reaches the cells of its window (weights with a clear sign bit)
+        for (int j = 0; j < n; ++j) {
+          const float* e = S + j * kBS;
+          const bool nf = (guarded >> j) & 1u;
+          const float z = e[8 + (g8 & 3)];
 #pragma unroll
-        for (int k = 0; k < 8; ++k) {
-          if (k < ncoil)
-            cp_async8(sl + 16 + 2 * k, vals + (long long)(c0 + k) * g.npts + p);
-          else
-            *reinterpret_cast<float2*>(sl + 16 + 2 * k) = make_float2(0.f, 0.f);
+          for (int m = 0; m < 4; ++m) {
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+              const float y = e[4 + (g8 >> 2) + 2 * h];
+              const float w = e[m] * (y * z);
+              const bool ok = !nf || (!signbit(e[m]) && !signbit(y) && !signbit(z));
+#pragma unroll
+              for (int nt = 0; nt < 2; ++nt) {
+                const float2 v = *reinterpret_cast<const float2*>(e + 16 + 2 * (4 * nt + t4));
+                if (ok) {
+                  D[m][nt][2 * h] = fmaf(w, v.x, D[m][nt][2 * h]);
+                  D[m][nt][2 * h + 1] = fmaf(w, v.y, D[m][nt][2 * h + 1]);
+                }
+              }
+            }
+          }
         }
       }
+      __syncwarp();  // the chunk has been read before the next one is staged
     }
-    cp_async_wait_all();
-    // the lane's own entry: x and y rows -> their products; finite values?
-    bool nonfinite = false;
-    if (lane < n) {
-      const float4 rx = *reinterpret_cast<const float4*>(sl + 36), ry = *reinterpret_cast<const float4*>(sl + 40);
-      float chk = 0.f;  // a non-finite value turns the zero product into NaN
-      const float4* vq = reinterpret_cast<const float4*>(sl + 16);
+    if (it.w >= 0) {  // a part of a split block: its slot of the partial blocks, [cell][entry] complex
+      float* dst = partial + ((long long)it.w * gridDim.y + cg) * 64 * 16;
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const float4 v = vq[q];
-        chk = fmaf(v.x, 0.f, chk);
-        chk = fmaf(v.y, 0.f, chk);
-        chk = fmaf(v.z, 0.f, chk);
-        chk = fmaf(v.w, 0.f, chk);
-      }
-      nonfinite = !(chk == 0.f);
-      float4* wq = reinterpret_cast<float4*>(sl);
-      wq[0] = make_float4(rx.x * ry.x, rx.x * ry.y, rx.x * ry.z, rx.x * ry.w);
-      wq[1] = make_float4(rx.y * ry.x, rx.y * ry.y, rx.y * ry.z, rx.y * ry.w);
-      wq[2] = make_float4(rx.z * ry.x, rx.z * ry.y, rx.z * ry.z, rx.z * ry.w);
-      wq[3] = make_float4(rx.w * ry.x, rx.w * ry.y, rx.w * ry.z, rx.w * ry.w);
-    }
-    const unsigned guarded = __ballot_sync(0xffffffffu, nonfinite);
-    __syncwarp();
-    // every lane applies the chunk's entries in order
-    auto visit = [&](const float* e, bool ok0, bool ok1) {
-      const float wxy = e[lx * 4 + ly];
-      const float2 wz = *reinterpret_cast<const float2*>(e + 32 + 2 * zp);
-      const float4 v0 = *reinterpret_cast<const float4*>(e + 16), v1 = *reinterpret_cast<const float4*>(e + 20);
-      const float4 v2 = *reinterpret_cast<const float4*>(e + 24), v3 = *reinterpret_cast<const float4*>(e + 28);
-      const float2 v[8] = {make_float2(v0.x, v0.y), make_float2(v0.z, v0.w), make_float2(v1.x, v1.y),
-                           make_float2(v1.z, v1.w), make_float2(v2.x, v2.y), make_float2(v2.z, v2.w),
-                           make_float2(v3.x, v3.y), make_float2(v3.z, v3.w)};
-      const float w0 = wxy * wz.x, w1 = wxy * wz.y;
-      if (ok0) {
+      for (int m = 0; m < 4; ++m)
 #pragma unroll
-        for (int k = 0; k < 8; ++k) a0[k] = __ffma2_rn(make_float2(w0, w0), v[k], a0[k]);
-      }
-      if (ok1) {
+        for (int h = 0; h < 2; ++h) {
+          const int cell = m * 16 + ((g8 >> 2) + 2 * h) * 4 + (g8 & 3);
 #pragma unroll
-        for (int k = 0; k < 8; ++k) a1[k] = __ffma2_rn(make_float2(w1, w1), v[k], a1[k]);
-      }
-    };
-    if (!guarded) {
-#pragma unroll 2
-      for (int j = 0; j < n; ++j) visit(S + j * kBS, true, true);
+          for (int nt = 0; nt < 2; ++nt)
+            *reinterpret_cast<float2*>(dst + cell * 16 + 2 * (4 * nt + t4)) =
+                make_float2(D[m][nt][2 * h], D[m][nt][2 * h + 1]);
+        }
     } else {
-      for (int j = 0; j < n; ++j) {
-        const float* e = S + j * kBS;
-        bool ok0 = true, ok1 = true;
-        if ((guarded >> j) & 1u) {  // only the cells of the window: weights with a clear sign bit
-          const bool xy = !signbit(e[36 + lx]) && !signbit(e[40 + ly]);
-          ok0 = xy && !signbit(e[32 + 2 * zp]);
-          ok1 = xy && !signbit(e[33 + 2 * zp]);
-        }
-        visit(e, ok0, ok1);
-      }
+      frag_store(g, gridv, c0, ncoil, kBE * bx, kBE * by, kBE * bz, g8, t4, D);
     }
-    __syncwarp();  // the chunk has been read before the next one is staged
   }
-  if (it.w >= 0) {  // a part of a split block: its slot of the partial blocks, [cell][entry] complex
-    float4* d = reinterpret_cast<float4*>(partial + (((long long)it.w * gridDim.y + cg) * 64 + lane * 2) * 16);
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      d[k] = make_float4(a0[2 * k].x, a0[2 * k].y, a0[2 * k + 1].x, a0[2 * k + 1].y);
-      d[4 + k] = make_float4(a1[2 * k].x, a1[2 * k].y, a1[2 * k + 1].x, a1[2 * k + 1].y);
-    }
-    return;
-  }
-  block_store(g, gridv, c0, ncoil, B[0] + lx, B[1] + ly, B[2] + 2 * zp, a0, a1);
 }
 
 // Sum the partial blocks of one split block in slot order, compensated (as
@@ -3507,7 +3574,7 @@ int launch_adj_b3(const Geo& g, const tlgb_interp_plan_info* info, const char* P
     TLGB_CHECK_LAUNCH();
     tv = reinterpret_cast<const float4*>(t);
   }
-  dim3 grd((unsigned)cdiv(info->n_blk_items, 8), (unsigned)ncg);
+  dim3 grd((unsigned)cdiv(info->n_blk_items, kB3Items), (unsigned)ncg);
   adj_b3_kernel<<<grd, 256, sm, s>>>(g, (const int4*)(P + info->off_blk_items), (int)info->n_blk_items,
                                     (const uint32_t*)(P + info->off_blk_entries), (const float4*)(P + info->off_blk_rows),
                                     (const float2*)vals, tv, (float*)grid, (float*)scratch);
