@@ -350,7 +350,9 @@ def run_gpu(args, world, rank, local):
     plan_ms = (time.perf_counter() - t0) * 1e3
     # per step: the gather, the point-major value transpose, the gridding and
     # (when dense tiles are split) the ordered sum of their parts
-    launches_per_step = 3 + (1 if plan.info.n_split_tiles > 0 else 0)
+    blocks = plan.info.n_blk_items > 0  # 3D gridding on block lists
+    n_split = plan.info.n_blk_split if blocks else plan.info.n_split_tiles
+    launches_per_step = 3 + (1 if n_split > 0 else 0)
 
     stream = torch.cuda.current_stream(dev)
     for _ in range(args.warmup):
@@ -427,7 +429,10 @@ def run_gpu(args, world, rank, local):
                    "frac": ALGO_BYTES / (fwd_ms / 1e3) / 1e9 / peak},
         "grid": {"ms": adj_ms, "GBps": ALGO_BYTES / (adj_ms / 1e3) / 1e9,
                  "frac": ALGO_BYTES / (adj_ms / 1e3) / 1e9 / peak,
-                 "partial_tiles": int(plan.info.n_partials)},
+                 "split": ({"blocks": int(plan.info.n_blk_split), "partial_blocks": int(plan.info.n_blk_partials),
+                            "block_entries": int(plan.info.n_blk_entries), "items": int(plan.info.n_blk_items)}
+                           if blocks else {"tiles": int(plan.info.n_split_tiles),
+                                           "partial_tiles": int(plan.info.n_partials)})},
         "plan_build_ms": plan_ms,
         "plan_entries": int(plan.info.n_entries),
     }

@@ -991,6 +991,7 @@ __global__ void point_records_kernel(Geo g, const float* __restrict__ locs, PRec
 constexpr int kBE = 4;         // block edge in cells, every dimension
 constexpr int kBlkPart = 256;  // entries per work item: denser blocks are split into parts
 constexpr int kZeroRun = 16;   // empty blocks written by one work item
+constexpr int kCube = 4;       // blocks per edge of the cubes the gridding items visit in turn
 constexpr int kSelShift = 29;  // entry = point | (its block's index per dim, 3 bits) << 29
 
 __host__ __device__ __forceinline__ int blocks_along(int n) { return (n + kBE - 1) / kBE; }
@@ -1769,47 +1770,68 @@ __global__ void __launch_bounds__(256, 3) adj_b3_kernel(Geo g, const int4* __res
 }
 
 // Sum the partial blocks of one split block in slot order, compensated (as
-// adj_reduce_f3_kernel). CTA = 256 threads: thread (cell, entry pair), one
-// float4 of each partial, four partials in flight.
-__global__ void __launch_bounds__(256) adj_reduce_b3_kernel(Geo g, const int4* __restrict__ split,
-                                                            const float* __restrict__ partial,
-                                                            float* __restrict__ gridv) {
+// adj_reduce_f3_kernel). CTA = 1024 threads: thread (quarter q, cell, entry
+// pair) sums the q-th quarter of the parts in slot order, one float4 of each,
+// eight in flight (the block at the centre of a dense trajectory has a few
+// hundred parts); then the quarters are added in order.
+__global__ void __launch_bounds__(1024) adj_reduce_b3_kernel(Geo g, const int4* __restrict__ split,
+                                                             const float* __restrict__ partial,
+                                                             float* __restrict__ gridv) {
+  __shared__ float4 qs[3][256], qc[3][256];
   const int4 sp = split[blockIdx.x];
   const int cg = blockIdx.y, ncg = gridDim.y, c0 = cg * 8;
   const int ncoil = (int)min(8ll, g.nbatch - c0);
-  const int cell = threadIdx.x >> 2, q = threadIdx.x & 3;  // entries 2q, 2q + 1
-  int bx, by, bz;
-  block_origin(g, sp.x, bx, by, bz);
+  const int q = threadIdx.x >> 8, r = threadIdx.x & 255;
+  const int cell = r >> 2, ep = r & 3;  // entries 2 ep, 2 ep + 1
   const long long step = (long long)ncg * 64 * 4;  // float4s between consecutive partials
-  const float4* src = reinterpret_cast<const float4*>(partial + ((long long)sp.y * ncg + cg) * 64 * 16) + threadIdx.x;
-  float4 sum = __ldg(src), comp = make_float4(0.f, 0.f, 0.f, 0.f);
-  int k = 1;
-  for (; k + 4 <= sp.z; k += 4) {
-    float4 v[4];
+  const float4* src = reinterpret_cast<const float4*>(partial + ((long long)sp.y * ncg + cg) * 64 * 16) + r;
+  const int k0 = (int)((long long)sp.z * q / 4), k1 = (int)((long long)sp.z * (q + 1) / 4);
+  float4 sum = make_float4(0.f, 0.f, 0.f, 0.f), comp = sum;
+  int k = k0;
+  for (; k + 8 <= k1; k += 8) {
+    float4 v[8];
 #pragma unroll
-    for (int i = 0; i < 4; ++i) v[i] = __ldg(src + (k + i) * step);
+    for (int i = 0; i < 8; ++i) v[i] = __ldg(src + (k + i) * step);
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
+    for (int i = 0; i < 8; ++i) {
       comp_add(sum.x, comp.x, v[i].x);
       comp_add(sum.y, comp.y, v[i].y);
       comp_add(sum.z, comp.z, v[i].z);
       comp_add(sum.w, comp.w, v[i].w);
     }
   }
-  for (; k < sp.z; ++k) {
+  for (; k < k1; ++k) {
     const float4 v = __ldg(src + k * step);
     comp_add(sum.x, comp.x, v.x);
     comp_add(sum.y, comp.y, v.y);
     comp_add(sum.z, comp.z, v.z);
     comp_add(sum.w, comp.w, v.w);
   }
+  if (q > 0) {
+    qs[q - 1][r] = sum;
+    qc[q - 1][r] = comp;
+  }
+  __syncthreads();
+  if (q > 0) return;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {  // the later quarters in order, their compensations with them
+    const float4 s2 = qs[i][r], c2 = qc[i][r];
+    comp_add(sum.x, comp.x, s2.x);
+    comp_add(sum.y, comp.y, s2.y);
+    comp_add(sum.z, comp.z, s2.z);
+    comp_add(sum.w, comp.w, s2.w);
+    comp.x += c2.x, comp.y += c2.y, comp.z += c2.z, comp.w += c2.w;
+  }
+  int bx, by, bz;
+  block_origin(g, sp.x, bx, by, bz);
   const int x = kBE * bx + (cell >> 4), y = kBE * by + ((cell >> 2) & 3), z = kBE * bz + (cell & 3);
   if (x >= g.N[0] || y >= g.N[1] || z >= g.N[2]) return;
   const long long gvol = (long long)g.N[0] * g.N[1] * g.N[2];
-  float* dst = gridv + ((long long)(c0 + 2 * q) * gvol + ((long long)x * g.N[1] + y) * g.N[2] + z) * 2;
-  if (2 * q < ncoil) *reinterpret_cast<float2*>(dst) = make_float2(sum.x + comp.x, sum.y + comp.y);
-  if (2 * q + 1 < ncoil) *reinterpret_cast<float2*>(dst + gvol * 2) = make_float2(sum.z + comp.z, sum.w + comp.w);
+  float* dst = gridv + ((long long)(c0 + 2 * ep) * gvol + ((long long)x * g.N[1] + y) * g.N[2] + z) * 2;
+  if (2 * ep < ncoil) *reinterpret_cast<float2*>(dst) = make_float2(sum.x + comp.x, sum.y + comp.y);
+  if (2 * ep + 1 < ncoil) *reinterpret_cast<float2*>(dst + gvol * 2) = make_float2(sum.z + comp.z, sum.w + comp.w);
 }
+
 
 // 2D gridding. The view of one dimension of a record from a 16-wide tile at o
 // (grid N): f | m << 4 | k0 << 7, as tile_view (f first local position, m
@@ -3292,10 +3314,9 @@ extern "C" int tlgb_interp_plan_build(const tlgb_interp_desc* d, const float* lo
   // Block lists (3D 8-entry gridding): (point, block) pairs from the tap
   // records, sorted stably by block; work items of at most kBlkPart entries
   // (dense blocks split into parts summed in order afterwards) and runs of
-  // up to kZeroRun empty blocks, in block order. A point's blocks are
-  // neighbours, so in block order its record and values are read again
-  // while they are still in L2 (in heaviest-first order nearly every read of
-  // them went to DRAM).
+  // up to kZeroRun empty blocks. A point's blocks are neighbours, so items
+  // in spatial order read its rows and values again while they are still in
+  // L2 (in heaviest-first order nearly every read of them went to DRAM).
   uint32_t Eb = 0;
   std::vector<int4> bitems, bsplit;
   int64_t n_bpartials = 0;
@@ -3323,29 +3344,39 @@ extern "C" int tlgb_interp_plan_build(const tlgb_interp_desc* d, const float* lo
     std::vector<uint32_t> hb((size_t)L.nblocks);
     TLGB_CUDA(cudaMemcpyAsync(hb.data(), hist, hb.size() * 4, cudaMemcpyDeviceToHost, s));
     TLGB_CUDA(cudaStreamSynchronize(s));
-    int64_t bpos = 0;
-    for (int64_t b = 0; b < L.nblocks; ++b) {
-      const int64_t n = hb[(size_t)b];
+    // items in cube order: cubes of kCube^3 blocks, blocks in key order
+    // inside a cube, so that the blocks a point meets are worked on close
+    // together in time and find its rows and values in L2
+    std::vector<int64_t> bstart((size_t)L.nblocks + 1, 0);
+    for (int64_t b = 0; b < L.nblocks; ++b) bstart[(size_t)b + 1] = bstart[(size_t)b] + hb[(size_t)b];
+    const int64_t nbx = blocks_along(g.N[0]), nby = blocks_along(g.N[1]), nbz = blocks_along(g.N[2]);
+    auto add_block = [&](int64_t b) {
+      const int64_t n = hb[(size_t)b], bpos = bstart[(size_t)b];
       if (n == 0) {
         int4* last = bitems.empty() ? nullptr : &bitems.back();
         if (last && last->y == last->z && last->x - last->w == b && -last->w < kZeroRun)
           --last->w;  // extends the run of empty blocks ending at block b - 1
         else
           bitems.push_back(make_int4((int)b, (int)bpos, (int)bpos, -1));
-        continue;
+        return;
       }
       if (n <= kBlkPart) {
         bitems.push_back(make_int4((int)b, (int)bpos, (int)(bpos + n), -1));
-      } else {
-        const int64_t nch = cdiv(n, kBlkPart);
-        bsplit.push_back(make_int4((int)b, (int)n_bpartials, (int)nch, 0));
-        for (int64_t k = 0; k < nch; ++k)
-          bitems.push_back(make_int4((int)b, (int)(bpos + k * kBlkPart), (int)std::min(bpos + n, bpos + (k + 1) * kBlkPart),
-                                     (int)(n_bpartials + k)));
-        n_bpartials += nch;
+        return;
       }
-      bpos += n;
-    }
+      const int64_t nch = cdiv(n, kBlkPart);
+      bsplit.push_back(make_int4((int)b, (int)n_bpartials, (int)nch, 0));
+      for (int64_t k = 0; k < nch; ++k)
+        bitems.push_back(make_int4((int)b, (int)(bpos + k * kBlkPart), (int)std::min(bpos + n, bpos + (k + 1) * kBlkPart),
+                                   (int)(n_bpartials + k)));
+      n_bpartials += nch;
+    };
+    for (int64_t cx = 0; cx < nbx; cx += kCube)
+      for (int64_t cy = 0; cy < nby; cy += kCube)
+        for (int64_t cz = 0; cz < nbz; cz += kCube)
+          for (int64_t bx = cx; bx < std::min(nbx, cx + kCube); ++bx)
+            for (int64_t by = cy; by < std::min(nby, cy + kCube); ++by)
+              for (int64_t bz = cz; bz < std::min(nbz, cz + kCube); ++bz) add_block((bx * nby + by) * nbz + bz);
     if ((int64_t)bitems.size() > L.max_blk_items) TLGB_FAIL(TLGB_ERR_DEVICE, "block work list larger than its bound");
     if (!bitems.empty())
       TLGB_CUDA(cudaMemcpyAsync(P + L.off_blk_items, bitems.data(), bitems.size() * 16, cudaMemcpyHostToDevice, s));
@@ -3581,7 +3612,7 @@ int launch_adj_b3(const Geo& g, const tlgb_interp_plan_info* info, const char* P
   TLGB_CHECK_LAUNCH();
   if (info->n_blk_split > 0) {
     dim3 g2((unsigned)info->n_blk_split, (unsigned)ncg);
-    adj_reduce_b3_kernel<<<g2, 256, 0, s>>>(g, (const int4*)(P + info->off_blk_split), (const float*)scratch,
+    adj_reduce_b3_kernel<<<g2, 1024, 0, s>>>(g, (const int4*)(P + info->off_blk_split), (const float*)scratch,
                                             (float*)grid);
     TLGB_CHECK_LAUNCH();
   }
