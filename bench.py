@@ -442,6 +442,8 @@ def run_gpu(args, world, rank, local):
         kernels.update(bench_blocks(dev, peak, args))
     if not args.skip_nufft2d:
         kernels["nufft2d"] = bench_nufft2d(dev, peak)
+    if not args.skip_nufft3d:
+        kernels["nufft3d"] = bench_nufft3d(locs_h, dev)
     if not args.skip_blocks:
         kernels["index"] = bench_index(dev, peak)
     line = None
@@ -709,6 +711,43 @@ def bench_cg(dev, args):
     }
 
 
+def bench_nufft3d(locs_h, dev):
+    """The same trajectory at the NUFFT level: 8 coil images of 205^3
+    (padded 1.25x to 256^3), the ball's points centred and scaled by 205/256.
+    Forward (apodize, pad, centred FFT, ungrid, scale), adjoint and the
+    explicit normal operator (forward then adjoint), each the median of 3
+    CUDA-event timings; the plan is built before the timings."""
+    from torchlinops_gb300 import linops
+
+    n = 205
+    locs = ((locs_h - N_GRID / 2) * (n / N_GRID)).to(dev)
+    gen = torch.Generator(device=dev).manual_seed(7)
+    x = torch.randn(N_COIL, n, n, n, dtype=torch.complex64, device=dev, generator=gen)
+    A = linops.NUFFT(locs, (n,) * 3)
+    s = torch.cuda.current_stream(dev)
+    y = A(x)
+    AH, AN = A.H, A.normal()
+    AH(y)
+    torch.cuda.synchronize()
+
+    def med(fn, reps=3):
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(s)
+            fn()
+            e1.record(s)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return statistics.median(ts)
+
+    out = {"workload": f"3D NUFFT, {N_COIL} coils x {n}^3 c64, padded to {int(n * 1.25)}^3, {locs.shape[0]} points",
+           "forward_ms": med(lambda: A(x)), "adjoint_ms": med(lambda: AH(y)), "normal_ms": med(lambda: AN(x))}
+    del x, y, A, AH, AN
+    torch.cuda.empty_cache()
+    return out
+
+
 def bench_toeplitz(locs, maps, xt, n, dev):
     """The NUFFT normal operator on the 8 coil images S_c x of the CG workload
     (128^3, 2^20 radial points): its Toeplitz embedding (PSF kernel on the 2x
@@ -828,6 +867,7 @@ def main():
     ap.add_argument("--skip-blocks", action="store_true")
     ap.add_argument("--skip-cg", action="store_true", help="skip the learned vs plain CG comparison")
     ap.add_argument("--skip-nufft2d", action="store_true", help="skip the differentiable 2D NUFFT timing")
+    ap.add_argument("--skip-nufft3d", action="store_true", help="skip the 3D NUFFT-level timing (205^3 x 8 coils)")
     ap.add_argument("--cg-steps", type=int, default=500, help="preconditioner training steps (4 samples each)")
     ap.add_argument("--precond-phantoms", type=int, default=64,
                     help="phantoms solved by plain CG to 1e-6 for the preconditioner's training data")
