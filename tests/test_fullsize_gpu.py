@@ -94,8 +94,8 @@ def test_fullsize_grid_dense_centre_vs_fp64(interp_case):
     """The hottest voxels (tens of thousands of points pile onto each cell of
     the centre tile): the GPU's error against the FP64 oracle stays at the
     level of one float32 rounding per cell, and no worse than the float32
-    oracle's own sequential sum (chunked accumulation in shared memory, then
-    a compensated sum of the chunk partials)."""
+    oracle's own sequential sum (parts of at most 256 points per block
+    accumulated in fp32, then a compensated sum of the parts)."""
     locs_h, locs, img, vals, beta = interp_case
     g = T.grid(vals, locs, (N, N, N), 4.0, kernel_params=dict(beta=beta))
     c = torch.tensor((128.0, 128.0, 128.0))
