@@ -1623,12 +1623,28 @@ __global__ void __launch_bounds__(256, 3) adj_b3_kernel(Geo g, const int4* __res
   const int ncoil = (int)min(8ll, g.nbatch - c0);
   const int g8 = lane >> 2, t4 = lane & 3;
   const int first = blockIdx.x * kB3Items, last = min(nitems, first + kB3Items);
+  auto grab = [&]() {
+    int i = 0;
+    if (lane == 0) i = first + atomicAdd(&next_item, 1);
+    return __shfl_sync(0xffffffffu, i, 0);
+  };
+  // one item and the next chunk's point indices ahead: a chunk's copies wait
+  // only for their own data, not for the descriptor and index loads before it
+  int item = grab();
+  if (item >= last) return;
+  int4 itn = items[item];
+  int inext = grab();
+  int4 itnn = inext < last ? items[inext] : make_int4(0, 0, 0, 0);
+  uint32_t enext = lane < min(kBC, itn.z - itn.y) ? bentries[itn.y + lane] : 0u;
   for (;;) {
-    int item = 0;
-    if (lane == 0) item = first + atomicAdd(&next_item, 1);
-    item = __shfl_sync(0xffffffffu, item, 0);
     if (item >= last) return;
-    const int4 it = items[item];
+    const int4 it = itn;
+    itn = itnn;
+    item = inext;
+    if (item < last) {
+      inext = grab();
+      itnn = inext < last ? items[inext] : make_int4(0, 0, 0, 0);
+    }
     float D[4][2][4];
 #pragma unroll
     for (int m = 0; m < 4; ++m)
@@ -1642,6 +1658,7 @@ __global__ void __launch_bounds__(256, 3) adj_b3_kernel(Geo g, const int4* __res
         block_origin(g, it.x + b, bx, by, bz);
         frag_store(g, gridv, c0, ncoil, kBE * bx, kBE * by, kBE * bz, g8, t4, D);
       }
+      if (item < last) enext = lane < min(kBC, itn.z - itn.y) ? bentries[itn.y + lane] : 0u;
       continue;
     }
     block_origin(g, it.x, bx, by, bz);
@@ -1649,8 +1666,13 @@ __global__ void __launch_bounds__(256, 3) adj_b3_kernel(Geo g, const int4* __res
       const int n = min(kBC, it.z - c);
       const int n8 = (n + 7) & ~7;  // the tensor-core steps read whole groups of 8 entries
       float* sl = S + lane * kBS;
+      const uint32_t en = enext;
+      // the point indices of the next chunk: this item's, or the next item's first
+      if (c + kBC < it.z)
+        enext = lane < min(kBC, it.z - c - kBC) ? bentries[c + kBC + lane] : 0u;
+      else if (item < last)
+        enext = lane < min(kBC, itn.z - itn.y) ? bentries[itn.y + lane] : 0u;
       if (lane < n) {
-        const uint32_t en = bentries[c + lane];
         long long p = en & ((1u << kSelShift) - 1u);
         if (!TLGB_IN_RANGE(p, g.npts)) p = 0;
         const float4* rsrc = rows + p * 6;
