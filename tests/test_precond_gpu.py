@@ -60,3 +60,33 @@ def test_plain_cg_is_the_fallback(problem, bad):
         M = lambda r: r * sign  # noqa: E731
     _, info = alg.cg_solve(A, b, rtol=1e-4, max_iters=600, M=M)
     assert info.fallback and info.converged and info.true_rel_residual < 2e-4
+
+
+def test_training_resumes_from_its_checkpoint(problem, tmp_path):
+    """A training interrupted after a checkpoint and started again with the
+    same data ends where the uninterrupted training ends."""
+    n, A, b = problem
+
+    def sample(step):  # the same batch for the same step
+        return mri.training_batch(A, n, torch.Generator().manual_seed(100 + step), 2, DEV)
+
+    manifest = {"sample": "mri.training_batch, seed 100 + step, 2 pairs", "n": n, "lr": 1e-3}
+    full = precond.CNNPreconditioner(DEV, seed=2)
+    full.fit(sample, 6, lr=1e-3)
+
+    def interrupted(step):
+        if step == 4:
+            raise RuntimeError("interrupted")
+        return sample(step)
+
+    path = str(tmp_path / "precond.ckpt")
+    first = precond.CNNPreconditioner(DEV, seed=2)
+    with pytest.raises(RuntimeError, match="interrupted"):
+        first.fit(interrupted, 6, lr=1e-3, checkpoint=path, checkpoint_every=3, manifest=manifest)
+    again = precond.CNNPreconditioner(DEV, seed=7)  # other initial weights: the checkpoint replaces them
+    log = again.fit(sample, 6, lr=1e-3, checkpoint=path, checkpoint_every=3, manifest=manifest)
+    assert log.resumed_from == 3
+    for p, q in zip(full.parameters(), again.parameters()):
+        assert torch.allclose(p.detach(), q.detach(), rtol=1e-6, atol=1e-7)
+    with pytest.raises(ValueError, match="another training run"):
+        precond.CNNPreconditioner(DEV).fit(sample, 6, checkpoint=path, manifest={"other": 1})

@@ -28,6 +28,7 @@ from __future__ import annotations
 
 import ctypes
 import math
+import os
 from dataclasses import dataclass, field
 from typing import Callable, Optional
 
@@ -47,6 +48,8 @@ __all__ = [
     "laplacian_params",
     "CNNPreconditioner",
     "TrainLog",
+    "save_train_checkpoint",
+    "load_train_checkpoint",
 ]
 
 C = 16  # channels of every activation (narrower layers are zero-padded)
@@ -143,6 +146,43 @@ def unpack(y: Tensor, z: Optional[Tensor] = None, scale: Optional[Tensor] = None
 class TrainLog:
     losses: list = field(default_factory=list)
     seconds: float = 0.0
+    resumed_from: int = 0  # the step a resumed training continued from (0: a fresh start)
+
+
+CHECKPOINT_VERSION = 1
+
+
+def save_train_checkpoint(path: str, model: "CNNPreconditioner", opt, sched, step: int, losses: list,
+                          manifest: Optional[dict]) -> None:
+    """Write a training checkpoint: the weights, the optimiser and schedule
+    state, the next step, the loss log and the manifest of the training data
+    (whatever identifies it: phantom seeds, solver tolerance, batch size,
+    learning rate). The file is replaced atomically, so an interrupted save
+    leaves the previous checkpoint intact."""
+    ck = {"version": CHECKPOINT_VERSION, "step": int(step), "model": model.state_dict(),
+          "optim": opt.state_dict(), "sched": sched.state_dict() if sched is not None else None,
+          "losses": list(losses), "manifest": manifest}
+    tmp = f"{path}.tmp"
+    torch.save(ck, tmp)
+    os.replace(tmp, path)
+
+
+def load_train_checkpoint(path: str, model: "CNNPreconditioner", opt, sched, manifest: Optional[dict]) -> tuple:
+    """Restore a checkpoint written by ``save_train_checkpoint`` into the
+    model, optimiser and schedule; returns (next step, loss log). A checkpoint
+    of another training run (its manifest differs from ``manifest``) raises
+    ValueError instead of mixing two runs' data."""
+    ck = torch.load(path, map_location="cpu", weights_only=False)
+    if ck.get("version") != CHECKPOINT_VERSION:
+        raise ValueError(f"{path}: checkpoint version {ck.get('version')!r}, expected {CHECKPOINT_VERSION}")
+    if manifest is not None and ck.get("manifest") != manifest:
+        raise ValueError(f"{path}: checkpoint of another training run (manifest {ck.get('manifest')!r}, "
+                         f"this run {manifest!r})")
+    model.load_state_dict(ck["model"])
+    opt.load_state_dict(ck["optim"])
+    if sched is not None and ck.get("sched") is not None:
+        sched.load_state_dict(ck["sched"])
+    return int(ck["step"]), list(ck["losses"])
 
 
 FEAT = 8  # features per real component (channels 0-7: real part, 8-15: imaginary part)
@@ -306,16 +346,28 @@ class CNNPreconditioner:
         return loss, [dv1, dv2, gskip]
 
     def fit(self, sample: Callable[[int], object], steps: int, lr: float = 1e-3, log_every: int = 0,
-            loss: str = "scale_invariant") -> TrainLog:
-        """Adam over ``steps`` batches ``sample(step)`` (lists of (r, e) pairs)."""
+            loss: str = "scale_invariant", checkpoint: Optional[str] = None, checkpoint_every: int = 0,
+            manifest: Optional[dict] = None) -> TrainLog:
+        """Adam over ``steps`` batches ``sample(step)`` (lists of (r, e) pairs).
+
+        With ``checkpoint`` (a file path), the training state is saved there
+        every ``checkpoint_every`` steps and after the last one, and a
+        training that finds the file resumes after its last saved step. So
+        ``sample`` must give the same batch for the same step (seeded by the
+        step), and ``manifest`` names the training data: a checkpoint with
+        another manifest is refused rather than resumed."""
         import time
 
         params = self.parameters()
         opt = torch.optim.Adam(params, lr=lr)
         sched = torch.optim.lr_scheduler.CosineAnnealingLR(opt, T_max=max(steps, 1), eta_min=lr * 0.05)
         log = TrainLog()
+        start = 0
+        if checkpoint and os.path.exists(checkpoint):
+            start, log.losses = load_train_checkpoint(checkpoint, self, opt, sched, manifest)
+            log.resumed_from = start
         t0 = time.perf_counter()
-        for step in range(steps):
+        for step in range(start, steps):
             lval, grads = self.loss_and_grads(sample(step), loss)
             for p, g in zip(params, grads):
                 p.grad = g
@@ -326,6 +378,8 @@ class CNNPreconditioner:
             self._cache = None
             if log_every and (step % log_every == 0 or step == steps - 1):
                 log.losses.append((step, float(lval)))
+            if checkpoint and ((checkpoint_every and (step + 1) % checkpoint_every == 0) or step == steps - 1):
+                save_train_checkpoint(checkpoint, self, opt, sched, step + 1, log.losses, manifest)
         torch.cuda.synchronize()
         log.seconds = time.perf_counter() - t0
         return log
