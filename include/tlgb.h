@@ -370,6 +370,18 @@ int tlgb_cg_set_pap(const float* p, const float* ap, int64_t n, int is_complex, 
 int tlgb_cg_step(float* x, float* r, float* p, const float* ap, int64_t n, int is_complex, double* state,
                  void* scratch, size_t scratch_bytes, tlgb_stream_t stream);
 
+/* Flexible preconditioned CG (state[TLGB_CG_RS] holds <r, z>):
+ * x += a p, r -= a Ap with a = state[RS] / state[PAP] (float64, applied
+ * rounded to float32). After z = M(r): state[RS] = Re <r, z>, the flexible
+ * Polak-Ribiere beta = -a Re <Ap, z> / <r_old, z_old> clamped at 0, and
+ * p = z + beta p, all on the device (no host synchronisation). The reference's
+ * CG has no preconditioner; these extend its step and direction updates
+ * (alg/pcg.py:73-87) to the flexible PCG of the learned preconditioner. */
+int tlgb_pcg_update(float* x, float* r, const float* p, const float* ap, int64_t n, int is_complex,
+                    const double* state, tlgb_stream_t stream);
+int tlgb_pcg_direction(const float* r, const float* z, const float* ap, float* p, int64_t n, int is_complex,
+                       double* state, void* scratch, size_t scratch_bytes, tlgb_stream_t stream);
+
 /* ------------------------------------------------------------------------ */
 /* Centred-FFT shifts folded into the NUFFT's pad and crop (complex64).      */
 /* The reference's cfftn = fftshift . fftn . ifftshift (utils/_fft.py:7-60)  */

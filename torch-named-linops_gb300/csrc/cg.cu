@@ -136,6 +136,62 @@ __global__ void __launch_bounds__(kDotThreads) cg_dir_kernel(float* __restrict__
     p[i] = fmaf(beta, p[i], r[i]);
 }
 
+// Flexible preconditioned CG (st[RS] holds <r, z>): x += a p ; r -= a Ap
+// with a = st[RS] / st[PAP], rounded once to float32 as in cg_step_kernel.
+__global__ void __launch_bounds__(kDotThreads) pcg_update_kernel(float* __restrict__ x, float* __restrict__ r,
+                                                                 const float* __restrict__ p,
+                                                                 const float* __restrict__ ap, int64_t nf,
+                                                                 const double* __restrict__ st) {
+  const double rz = st[TLGB_CG_RS], pap = st[TLGB_CG_PAP];
+  const float a = (float)(pap != 0.0 ? rz / pap : 0.0);
+  for (int64_t i = (int64_t)blockIdx.x * kDotThreads + threadIdx.x; i < nf; i += (int64_t)gridDim.x * kDotThreads) {
+    x[i] = fmaf(a, p[i], x[i]);
+    r[i] = fmaf(-a, ap[i], r[i]);
+  }
+}
+
+// partial[b] = (Re <r, z>, Re <Ap, z>) over this block's slice (complex
+// values as interleaved floats: the real part of the Hermitian product is
+// the plain sum over both components)
+__global__ void __launch_bounds__(kDotThreads) pcg_dots_kernel(const float* __restrict__ r,
+                                                               const float* __restrict__ z,
+                                                               const float* __restrict__ ap, int64_t nf,
+                                                               double2* __restrict__ partial) {
+  double2 acc = make_double2(0.0, 0.0);
+  const int64_t per = (nf + gridDim.x - 1) / gridDim.x;
+  const int64_t b = (int64_t)blockIdx.x * per;
+  const int64_t e = b + per < nf ? b + per : nf;
+  for (int64_t i = b + threadIdx.x; i < e; i += kDotThreads) {
+    const double zi = z[i];
+    acc.x += (double)r[i] * zi;
+    acc.y += (double)ap[i] * zi;
+  }
+  acc = block_sum2(acc);
+  if (threadIdx.x == 0) partial[blockIdx.x] = acc;
+}
+
+// <r, z> and the flexible (Polak-Ribiere) beta = <r_new - r_old, z> / <r_old, z_old>,
+// with r_new - r_old = -a Ap (the form that does not subtract two nearly equal
+// residuals), clamped at 0; rolls the state
+__global__ void pcg_scalars_kernel(const double2* __restrict__ partial, int np, double* __restrict__ st) {
+  double2 acc = make_double2(0.0, 0.0);
+  for (int i = threadIdx.x; i < np; i += kDotThreads) {
+    acc.x += partial[i].x;
+    acc.y += partial[i].y;
+  }
+  acc = block_sum2(acc);
+  if (threadIdx.x == 0) {
+    const double rz_old = st[TLGB_CG_RS], pap = st[TLGB_CG_PAP];
+    const double a = pap != 0.0 ? rz_old / pap : 0.0;
+    const double beta = rz_old != 0.0 ? -a * acc.y / rz_old : 0.0;
+    st[TLGB_CG_ALPHA] = a;
+    st[TLGB_CG_RS_OLD] = rz_old;
+    st[TLGB_CG_RS] = acc.x;
+    st[TLGB_CG_BETA] = beta > 0.0 ? beta : 0.0;
+    st[TLGB_CG_ITERS] += 1.0;
+  }
+}
+
 __global__ void copy_pap_kernel(const double* __restrict__ dot, double* __restrict__ st) {
   st[TLGB_CG_PAP] = dot[0];
 }
@@ -185,6 +241,36 @@ extern "C" int tlgb_cg_step(float* x, float* r, float* p, const float* ap, int64
   TLGB_CHECK_LAUNCH();
   const int nd = (int)std::min<int64_t>(4 * 152, std::max<int64_t>(1, cdiv(nf, kDotThreads)));
   cg_dir_kernel<<<nd, kDotThreads, 0, s>>>(p, r, nf, state);
+  TLGB_CHECK_LAUNCH();
+  return TLGB_OK;
+}
+
+extern "C" int tlgb_pcg_update(float* x, float* r, const float* p, const float* ap, int64_t n, int is_complex,
+                               const double* state, tlgb_stream_t stream) {
+  if (n < 0 || !state || (n > 0 && (!x || !r || !p || !ap))) TLGB_FAIL(TLGB_ERR_INVALID, "bad pcg arguments");
+  const int64_t nf = is_complex ? 2 * n : n;
+  if (nf == 0) return TLGB_OK;
+  const int nd = (int)std::min<int64_t>(4 * 152, std::max<int64_t>(1, cdiv(nf, kDotThreads)));
+  pcg_update_kernel<<<nd, kDotThreads, 0, (cudaStream_t)stream>>>(x, r, p, ap, nf, state);
+  TLGB_CHECK_LAUNCH();
+  return TLGB_OK;
+}
+
+extern "C" int tlgb_pcg_direction(const float* r, const float* z, const float* ap, float* p, int64_t n,
+                                  int is_complex, double* state, void* scratch, size_t scratch_bytes,
+                                  tlgb_stream_t stream) {
+  if (n < 0 || !state || (n > 0 && (!r || !z || !ap || !p))) TLGB_FAIL(TLGB_ERR_INVALID, "bad pcg arguments");
+  if (scratch_bytes < tlgb_cg_scratch_bytes() || !scratch) TLGB_FAIL(TLGB_ERR_WORKSPACE, "cg scratch too small");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int64_t nf = is_complex ? 2 * n : n;
+  const int nb = nblocks_for(nf);
+  double2* part = (double2*)scratch;
+  pcg_dots_kernel<<<nb, kDotThreads, 0, s>>>(r, z, ap, nf, part);
+  TLGB_CHECK_LAUNCH();
+  pcg_scalars_kernel<<<1, kDotThreads, 0, s>>>(part, nb, state);
+  TLGB_CHECK_LAUNCH();
+  const int nd = (int)std::min<int64_t>(4 * 152, std::max<int64_t>(1, cdiv(nf, kDotThreads)));
+  cg_dir_kernel<<<nd, kDotThreads, 0, s>>>(p, z, nf, state);
   TLGB_CHECK_LAUNCH();
   return TLGB_OK;
 }

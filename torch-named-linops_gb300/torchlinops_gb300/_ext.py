@@ -167,6 +167,8 @@ _SIGNATURES = {
     "tlgb_dot_f64": ([_P, _P, ctypes.c_int64, ctypes.c_int, _P, _P, ctypes.c_size_t, _P], ctypes.c_int),
     "tlgb_cg_set_pap": ([_P, _P, ctypes.c_int64, ctypes.c_int, _P, _P, ctypes.c_size_t, _P], ctypes.c_int),
     "tlgb_cg_step": ([_P, _P, _P, _P, ctypes.c_int64, ctypes.c_int, _P, _P, ctypes.c_size_t, _P], ctypes.c_int),
+    "tlgb_pcg_update": ([_P, _P, _P, _P, ctypes.c_int64, ctypes.c_int, _P, _P], ctypes.c_int),
+    "tlgb_pcg_direction": ([_P, _P, _P, _P, ctypes.c_int64, ctypes.c_int, _P, _P, ctypes.c_size_t, _P], ctypes.c_int),
     "tlgb_pad_shift_c64": ([_P, ctypes.c_int64, ctypes.c_int32, _P, _P, _P, _P, ctypes.c_int32, _P, _P,
                             ctypes.c_int32, _P, _P], ctypes.c_int),
     "tlgb_crop_shift_c64": ([_P, ctypes.c_int64, ctypes.c_int32, _P, _P, _P, _P, ctypes.c_int32, _P, _P,

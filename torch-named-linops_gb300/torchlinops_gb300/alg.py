@@ -208,22 +208,30 @@ def cg_solve(
                     info.converged = True
                     break
     else:
+        # flexible PCG, fused on the device like plain CG: float64 <r, z>,
+        # <p, Ap>, <Ap, z>, alpha and the Polak-Ribiere beta stay in the state
+        # vector; no host synchronisation between checks
         z = M(r).contiguous()
         p = z.clone()
-        rz = _cdot(r, z).real
+        state = torch.zeros(_ext.CG_STATE_LEN, dtype=torch.float64, device=dev)
+        state[_ext.CG_RS] = dot64(r, z)[0]
+        sc = _scratch(dev)
+        L = _ext.lib()
+        n = b.numel()
+        cplx = 1 if b.is_complex() else 0
         for k in range(1, max_iters + 1):
             Ap = A(p).contiguous()
-            pAp = _cdot(p, Ap).real
-            alpha = (rz / pAp).to(torch.float32)
-            x = x + alpha * p
-            r_new = (r - alpha * Ap).contiguous()
-            z_new = M(r_new).contiguous()
-            rz_new = _cdot(r_new, z_new).real
-            # flexible (Polak-Ribiere) beta = <r_new - r, z_new> / <r, z>
-            beta = (rz_new - _cdot(r, z_new).real) / rz
-            beta = torch.clamp(beta, min=0.0).to(torch.float32)
-            p = (z_new + beta * p).contiguous()
-            r, rz = r_new, rz_new
+            with torch.cuda.device(dev):
+                st = _ext.stream_ptr(dev)
+                _ext.check(L.tlgb_cg_set_pap(_ext.ptr(p), _ext.ptr(Ap), n, cplx, _ext.ptr(state), _ext.ptr(sc),
+                                             sc.numel(), st), "pcg")
+                _ext.check(L.tlgb_pcg_update(_ext.ptr(x), _ext.ptr(r), _ext.ptr(p), _ext.ptr(Ap), n, cplx,
+                                             _ext.ptr(state), st), "pcg")
+            z = M(r).contiguous()
+            with torch.cuda.device(dev):
+                _ext.check(L.tlgb_pcg_direction(_ext.ptr(r), _ext.ptr(z), _ext.ptr(Ap), _ext.ptr(p), n, cplx,
+                                                _ext.ptr(state), _ext.ptr(sc), sc.numel(), _ext.stream_ptr(dev)),
+                           "pcg")
             info.iters = k
             if k % check_every == 0 or k == max_iters:
                 rel = float(norm64(r)) / bnorm
