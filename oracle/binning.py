@@ -19,9 +19,10 @@ restates, independently of the CUDA code, which pairs exist and their order:
 * pairs are ordered by ``key = 2 * tile + (0 if home else 1)`` and, for equal
   keys, by point index (a stable sort of the pairs in point order).
 
-3D plans of the 8-entry gridding also list (point, block) pairs for output
-blocks of 4 x 4 x 4 cells (``block_pairs``): a point pairs with every block
-that one of its valid taps lands in, keyed ``(b0 * nb1 + b1) * nb2 + b2``,
+Plans of the 8-entry gridding also list (point, block) pairs for output
+blocks of 4 x 4 x 4 cells (3D) or 8 x 8 cells (2D) (``block_pairs``): a point
+pairs with every block that one of its valid taps lands in, keyed
+``(b0 * nb1 + b1) * nb2 + b2``,
 in point order within a block. Each pair is stored as
 ``point | (i0 | i1 << 1 | i2 << 2) << 29``, i_e the index of the block among
 the point's blocks along dim e in window order.
@@ -99,23 +100,33 @@ def plan_pairs(locs: torch.Tensor, grid_size, width, kernel: str = "kaiser_besse
 
 
 def block_pairs(locs: torch.Tensor, grid_size, width, kernel: str = "kaiser_bessel", pad_mode: str = "circular"):
-    """(keys, entries) of the 3D block lists: every (point, 4^3-cell block)
-    pair, sorted by block key and, within a block, by point index; entries
-    as stored by the plan (point index and the block's index per dim)."""
-    assert len(grid_size) == 3
-    N = tuple(int(n) for n in grid_size)
-    nb = tuple(-(-n // 4) for n in N)
-    x = locs.reshape(-1, 3).to(torch.float32)
+    """(keys, entries) of the block lists: every (point, block) pair for
+    blocks of 4 x 4 x 4 cells (3D) or 8 x 8 cells (2D), sorted by block key
+    and, within a block, by point index; entries as stored by the plan (point
+    index and the block's index per internal dim; a 2D grid's leading
+    internal dim has one block)."""
+    nd = len(grid_size)
+    assert nd in (2, 3)
+    N = (1,) * (3 - nd) + tuple(int(n) for n in grid_size)
+    edge = (4, 4, 4) if nd == 3 else (1, 8, 8)
+    nb = tuple(-(-n // b) for n, b in zip(N, edge))
+    x = locs.reshape(-1, nd).to(torch.float32)
     P = x.shape[0]
-    widths = width if isinstance(width, (tuple, list)) else (width,) * 3
+    widths = width if isinstance(width, (tuple, list)) else (width,) * nd
     ok = torch.isfinite(x).all(-1) & (x.abs() < 16777216.0).all(-1)
-    blocks = []  # per dim: [P, 3] distinct blocks, -1 = none
+    blocks = []  # per internal dim: [P, 3] distinct blocks, -1 = none
     for e in range(3):
-        g, _, valid = axis_taps(x[:, e], float(widths[e]), kernel, torch.float32)
+        if e < 3 - nd:
+            t = torch.full((P, 3), -1, dtype=torch.int64)
+            t[:, 0] = 0
+            blocks.append(t)
+            continue
+        a = e - (3 - nd)
+        g, _, valid = axis_taps(x[:, a], float(widths[a]), kernel, torch.float32)
         if pad_mode == "zero":
             valid = valid & (g >= 0) & (g < N[e])
         pos = torch.remainder(g, N[e]) if pad_mode == "circular" else g
-        bl = torch.div(pos, 4, rounding_mode="floor")
+        bl = torch.div(pos, edge[e], rounding_mode="floor")
         out = torch.full((P, 3), -1, dtype=torch.int64)
         cnt = torch.zeros(P, dtype=torch.int64)
         for k in range(g.shape[1]):

@@ -44,12 +44,16 @@ def test_plan_permutation_is_bit_exact(grid_size, npts, pad):
     assert int(plan.info.n_home) == int((keys % 2 == 0).sum())
 
 
-@pytest.mark.parametrize("grid_size,npts,pad", [c for c in CASES if len(c[0]) == 3])
+BLOCK_CASES = [c for c in CASES if len(c[0]) == 3] + [((200, 144), 50000, "circular"), ((190, 150), 40000, "zero")]
+
+
+@pytest.mark.parametrize("grid_size,npts,pad", BLOCK_CASES)
 def test_block_lists_are_bit_exact(grid_size, npts, pad):
     gen = torch.Generator().manual_seed(npts + 7)
+    nd = len(grid_size)
     n = torch.tensor(grid_size, dtype=torch.float32)
-    locs = torch.rand(npts, 3, generator=gen) * (n + 6) - 3
-    locs[:500] = torch.randint(0, 30, (500, 3), generator=gen).float()  # exact integers: 5 taps
+    locs = torch.rand(npts, nd, generator=gen) * (n + 6) - 3
+    locs[:500] = torch.randint(0, 30, (500, nd), generator=gen).float()  # exact integers: 5 taps
     locs[500:520, 1] = float("inf")
     keys, pts = OB.block_pairs(locs, grid_size, 4.0, "kaiser_bessel", pad)
     plan = interp.get_plan(locs.to(DEV), grid_size, 4.0, "kaiser_bessel", pad, 6.99666)
@@ -69,7 +73,7 @@ def test_block_lists_are_bit_exact(grid_size, npts, pad):
         cover[s0:s1] += 1
     assert np.all(cover == 1)
     # empty runs and non-empty items together name every block once
-    nb = int(np.prod([-(-s // 4) for s in grid_size]))
+    nb = int(np.prod([-(-s // (4 if nd == 3 else 8)) for s in grid_size]))
     named = np.zeros(nb, dtype=np.int64)
     for b, s0, s1, w in items:
         if s0 == s1:

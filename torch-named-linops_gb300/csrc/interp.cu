@@ -983,28 +983,37 @@ __global__ void point_records_kernel(Geo g, const float* __restrict__ locs, PRec
 
 // ------------------------------------------------ block lists (3D gridding)
 //
-// The 3D 8-entry gridding works on output blocks of 4 x 4 x 4 cells. A
-// window of 4 taps per dimension meets 1.75 blocks per dimension on average
-// (5.4 blocks of 64 cells per point), and one warp holds a whole block for 8
-// entries in registers (2 cells x 8 entries per lane). The plan lists per
-// block the points whose window meets it, in point order.
-constexpr int kBE = 4;         // block edge in cells, every dimension
+// The 8-entry gridding works on output blocks of 4 x 4 x 4 cells in 3D and
+// 8 x 8 cells in 2D (64 cells either way). A window of 4 taps per dimension
+// meets 1.75 blocks of 4 (1.375 of 8) per dimension on average, and one warp
+// holds a whole block for 8 entries. The plan lists per block the points
+// whose window meets it, in point order.
 constexpr int kBlkPart = 256;  // entries per work item: denser blocks are split into parts
 constexpr int kZeroRun = 16;   // empty blocks written by one work item
 constexpr int kCube = 4;       // blocks per edge of the cubes the gridding items visit in turn
 constexpr int kSelShift = 29;  // entry = point | (its block's index per dim, 3 bits) << 29
 
-__host__ __device__ __forceinline__ int blocks_along(int n) { return (n + kBE - 1) / kBE; }
+// block edge along internal dim e: 4 in 3D; 8 along the two dims of a 2D
+// grid (1 along its inactive leading dim)
+__host__ __device__ __forceinline__ int block_edge(int ndim, int e) { return ndim == 3 ? 4 : (e == 0 ? 1 : 8); }
+__host__ __device__ __forceinline__ int blocks_along(int n, int edge) { return (n + edge - 1) / edge; }
+__host__ __device__ __forceinline__ int blocks_along(const Geo& g, int e) {
+  return blocks_along(g.N[e], block_edge(g.ndim, e));
+}
+// floats of tap rows per point: 2 rows per active dim, one weight per cell
+__host__ __device__ __forceinline__ int row_floats(int ndim) { return ndim == 3 ? 24 : 32; }
 
 // Distinct blocks met along one dim by the cells st .. st+c-1 of a window
 // (st in [0, N); wrapped once in circular mode, where N >= 16 > c). At most
-// 2: 5 taps over blocks of 4 cells (circular grids are multiples of 4).
+// 2: 5 taps over blocks of 4 or 8 cells (circular grids are multiples of the
+// block edge).
 __device__ __forceinline__ int axis_blocks(const Geo& g, int e, int st, int c, int* bl) {
+  const int edge = block_edge(g.ndim, e);
   int cnt = 0;
   for (int k = 0; k < c; ++k) {
     int v = st + k;
     if (v >= g.N[e]) v -= g.N[e];
-    const int b = v / kBE;
+    const int b = v / edge;
     bool seen = false;
     for (int i = 0; i < cnt; ++i) seen = seen || bl[i] == b;
     if (!seen && cnt < 3) bl[cnt++] = b;
@@ -1036,7 +1045,7 @@ __global__ void blk_emit_kernel(Geo g, const PRec* __restrict__ precs, const uin
     if (!ce) return;
     nc[e] = axis_blocks(g, e, R.st[e], ce, bl[e]);
   }
-  const uint32_t nb1 = (uint32_t)blocks_along(g.N[1]), nb2 = (uint32_t)blocks_along(g.N[2]);
+  const uint32_t nb1 = (uint32_t)blocks_along(g, 1), nb2 = (uint32_t)blocks_along(g, 2);
   uint32_t o = off[p];
   for (int i = 0; i < nc[0]; ++i)
     for (int j = 0; j < nc[1]; ++j)
@@ -1047,26 +1056,27 @@ __global__ void blk_emit_kernel(Geo g, const PRec* __restrict__ precs, const uin
       }
 }
 
-// The tap weights of a point over each block it meets: per dim the rows of
-// its first and second block (in axis_blocks order), 4 cells each, from the
-// coordinate as the tap records; a cell outside the window holds -0.0 (valid
-// weights are >= +0), so the sign bit tells the gridding which cells the
-// window covers.
+// The tap weights of a point over each block it meets: per active dim the
+// rows of its first and second block (in axis_blocks order), one weight per
+// cell of the block (4 in 3D, 8 in 2D), from the coordinate as the tap
+// records; a cell outside the window holds -0.0 (valid weights are >= +0), so
+// the sign bit tells the gridding which cells the window covers.
 __global__ void blk_rows_kernel(Geo g, const float* __restrict__ locs, const PRec* __restrict__ precs,
-                                float4* __restrict__ rows) {
+                                float* __restrict__ rows) {
   const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= g.npts) return;
   const PRec R = precs[p];
-  for (int e = 0; e < 3; ++e) {
+  float* out = rows + p * row_floats(g.ndim);
+  for (int e = 3 - g.ndim; e < 3; ++e) {
+    const int edge = block_edge(g.ndim, e);
     const int ce = (R.cnt >> (4 * e)) & 15;
     int bl[3] = {0, 0, 0};
     const int nb = ce ? axis_blocks(g, e, R.st[e], ce, bl) : 0;
     const float x = load_coord(g, locs, p, e);
     const int lower = coord_ok(x) ? lower_of(g, e, x) : 0;
     for (int i = 0; i < 2; ++i) {
-      float r[4];
-      for (int q = 0; q < 4; ++q) {
-        const int v = kBE * bl[i] + q;
+      for (int q = 0; q < edge; ++q) {
+        const int v = edge * bl[i] + q;
         int k = v - lower;
         if (g.pad == TLGB_PAD_CIRCULAR) k = wrapi(k, g.N[e]);
         float w = -0.0f;
@@ -1074,9 +1084,8 @@ __global__ void blk_rows_kernel(Geo g, const float* __restrict__ locs, const PRe
           const Tap t = tap_eval(g, e, x, lower, k);
           if (t.valid) w = kern_value_approx(g.kernel, fabsf(t.d), g.beta);
         }
-        r[q] = w;
+        *out++ = w;
       }
-      rows[p * 6 + 2 * e + i] = make_float4(r[0], r[1], r[2], r[3]);
     }
   }
 }
@@ -1572,29 +1581,46 @@ __device__ __forceinline__ void mma_tf32(float (&d)[4], const unsigned (&a)[4], 
 }
 
 __device__ __forceinline__ void block_origin(const Geo& g, int key, int& bx, int& by, int& bz) {
-  const int nb1 = blocks_along(g.N[1]), nb2 = blocks_along(g.N[2]);
+  const int nb1 = blocks_along(g, 1), nb2 = blocks_along(g, 2);
   bz = key % nb2;
   const int t = key / nb2;
   by = t % nb1;
   bx = t / nb1;
 }
 
-// The accumulator fragment of lane (g8, t4): D[m][nt][2h + c] is cell
-// (x m, y (g8 >> 2) + 2h, z g8 & 3) of the block, entry 4 nt + t4, real (c = 0)
-// or imaginary part. Stores the lane's cells of entries below ncoil.
-__device__ __forceinline__ void frag_store(const Geo& g, float* __restrict__ gridv, int c0, int ncoil, int B0, int B1,
-                                           int B2, int g8, int t4, const float (&D)[4][2][4]) {
+// The accumulator fragment of lane (g8, t4): D[m][nt][2h + c] holds entry
+// 4 nt + t4 (real part c = 0, imaginary c = 1) of the block cell
+// 3D: (x m, y (g8 >> 2) + 2h, z g8 & 3); 2D: (y 2m + h, z g8).
+template <int NDIM>
+__device__ __forceinline__ void frag_cell(int m, int h, int g8, int& x, int& y, int& z) {
+  if constexpr (NDIM == 3) {
+    x = m, y = (g8 >> 2) + 2 * h, z = g8 & 3;
+  } else {
+    x = 0, y = 2 * m + h, z = g8;
+  }
+}
+// index of a block cell in [x][y][z] order (64 cells)
+template <int NDIM>
+__device__ __forceinline__ int cell_index(int x, int y, int z) {
+  return NDIM == 3 ? (x * 4 + y) * 4 + z : y * 8 + z;
+}
+
+// Stores the lane's cells of block key `blk` for entries below ncoil.
+template <int NDIM>
+__device__ __forceinline__ void frag_store(const Geo& g, float* __restrict__ gridv, int c0, int ncoil, int blk, int g8,
+                                           int t4, const float (&D)[4][2][4]) {
+  int bx, by, bz;
+  block_origin(g, blk, bx, by, bz);
+  const int B0 = bx * block_edge(NDIM, 0), B1 = by * block_edge(NDIM, 1), B2 = bz * block_edge(NDIM, 2);
   const long long gvol = (long long)g.N[0] * g.N[1] * g.N[2];
-  const int z = B2 + (g8 & 3);
-  if (z >= g.N[2]) return;
 #pragma unroll
   for (int m = 0; m < 4; ++m) {
-    const int x = B0 + m;
-    if (x >= g.N[0]) break;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
-      const int y = B1 + (g8 >> 2) + 2 * h;
-      if (y >= g.N[1]) continue;
+      int lx, ly, lz;
+      frag_cell<NDIM>(m, h, g8, lx, ly, lz);
+      const int x = B0 + lx, y = B1 + ly, z = B2 + lz;
+      if (x >= g.N[0] || y >= g.N[1] || z >= g.N[2]) continue;
       const long long cell = ((long long)x * g.N[1] + y) * g.N[2] + z;
 #pragma unroll
       for (int nt = 0; nt < 2; ++nt) {
@@ -1607,9 +1633,10 @@ __device__ __forceinline__ void frag_store(const Geo& g, float* __restrict__ gri
   }
 }
 
+template <int NDIM>
 __global__ void __launch_bounds__(256, 3) adj_b3_kernel(Geo g, const int4* __restrict__ items, int nitems,
                                                         const uint32_t* __restrict__ bentries,
-                                                        const float4* __restrict__ rows,
+                                                        const float* __restrict__ rows,
                                                         const float2* __restrict__ vals,
                                                         const float4* __restrict__ tv, float* __restrict__ gridv,
                                                         float* __restrict__ partial) {
@@ -1652,16 +1679,11 @@ __global__ void __launch_bounds__(256, 3) adj_b3_kernel(Geo g, const int4* __res
       for (int nt = 0; nt < 2; ++nt)
 #pragma unroll
         for (int i = 0; i < 4; ++i) D[m][nt][i] = 0.f;
-    int bx, by, bz;
     if (it.y == it.z) {  // a run of -it.w empty blocks
-      for (int b = 0; b < -it.w; ++b) {
-        block_origin(g, it.x + b, bx, by, bz);
-        frag_store(g, gridv, c0, ncoil, kBE * bx, kBE * by, kBE * bz, g8, t4, D);
-      }
+      for (int b = 0; b < -it.w; ++b) frag_store<NDIM>(g, gridv, c0, ncoil, it.x + b, g8, t4, D);
       if (item < last) enext = lane < min(kBC, itn.z - itn.y) ? bentries[itn.y + lane] : 0u;
       continue;
     }
-    block_origin(g, it.x, bx, by, bz);
     for (int c = it.y; c < it.z; c += kBC) {
       const int n = min(kBC, it.z - c);
       const int n8 = (n + 7) & ~7;  // the tensor-core steps read whole groups of 8 entries
@@ -1675,10 +1697,19 @@ __global__ void __launch_bounds__(256, 3) adj_b3_kernel(Geo g, const int4* __res
       if (lane < n) {
         long long p = en & ((1u << kSelShift) - 1u);
         if (!TLGB_IN_RANGE(p, g.npts)) p = 0;
-        const float4* rsrc = rows + p * 6;
-        cp_async16(sl + 0, rsrc + 0 + ((en >> kSelShift) & 1));        // x row
-        cp_async16(sl + 4, rsrc + 2 + ((en >> (kSelShift + 1)) & 1));  // y row
-        cp_async16(sl + 8, rsrc + 4 + ((en >> (kSelShift + 2)) & 1));  // z row
+        const float* rsrc = rows + p * row_floats(NDIM);
+        if constexpr (NDIM == 3) {  // rows of 4 cells: x 0-3, y 4-7, z 8-11
+          cp_async16(sl + 0, rsrc + 4 * (0 + ((en >> kSelShift) & 1)));
+          cp_async16(sl + 4, rsrc + 4 * (2 + ((en >> (kSelShift + 1)) & 1)));
+          cp_async16(sl + 8, rsrc + 4 * (4 + ((en >> (kSelShift + 2)) & 1)));
+        } else {  // rows of 8 cells: y 0-7, z 8-15
+          const float* ry = rsrc + 8 * (0 + ((en >> (kSelShift + 1)) & 1));
+          const float* rz = rsrc + 8 * (2 + ((en >> (kSelShift + 2)) & 1));
+          cp_async16(sl + 0, ry);
+          cp_async16(sl + 4, ry + 4);
+          cp_async16(sl + 8, rz);
+          cp_async16(sl + 12, rz + 4);
+        }
         if (tv) {
           const float4* vsrc = tv + ((long long)cg * g.npts + p) * 4;
 #pragma unroll
@@ -1695,7 +1726,7 @@ __global__ void __launch_bounds__(256, 3) adj_b3_kernel(Geo g, const int4* __res
       } else if (lane < n8) {  // padding entries of the last group: zero weights and values
         const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
         float4* q4 = reinterpret_cast<float4*>(sl);
-        q4[0] = q4[1] = q4[2] = z4;
+        q4[0] = q4[1] = q4[2] = q4[3] = z4;
         q4[4] = q4[5] = q4[6] = q4[7] = z4;
       }
       cp_async_wait_all();
@@ -1725,18 +1756,32 @@ __global__ void __launch_bounds__(256, 3) adj_b3_kernel(Geo g, const int4* __res
             split_tf32(e0[16 + 8 * nt + g8], bh[nt][0], bl[nt][0]);
             split_tf32(e1[16 + 8 * nt + g8], bh[nt][1], bl[nt][1]);
           }
-          const float4 x0 = *reinterpret_cast<const float4*>(e0), x1 = *reinterpret_cast<const float4*>(e1);
-          const float z0 = e0[8 + (g8 & 3)], z1 = e1[8 + (g8 & 3)];
-          const float yz0a = e0[4 + (g8 >> 2)] * z0, yz0b = e0[6 + (g8 >> 2)] * z0;
-          const float yz1a = e1[4 + (g8 >> 2)] * z1, yz1b = e1[6 + (g8 >> 2)] * z1;
-          const float xs0[4] = {x0.x, x0.y, x0.z, x0.w}, xs1[4] = {x1.x, x1.y, x1.z, x1.w};
+          // weights of rows g8 and g8 + 8 of row tile m, for entries e0 and e1
+          float wa[4][2], wb[4][2];
+          if constexpr (NDIM == 3) {  // x m * (y (g8 >> 2) + 2h * z g8 & 3)
+            const float z0 = e0[8 + (g8 & 3)], z1 = e1[8 + (g8 & 3)];
+            const float yz0a = e0[4 + (g8 >> 2)] * z0, yz0b = e0[6 + (g8 >> 2)] * z0;
+            const float yz1a = e1[4 + (g8 >> 2)] * z1, yz1b = e1[6 + (g8 >> 2)] * z1;
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+              wa[m][0] = e0[m] * yz0a, wa[m][1] = e0[m] * yz0b;
+              wb[m][0] = e1[m] * yz1a, wb[m][1] = e1[m] * yz1b;
+            }
+          } else {  // y 2m + h * z g8
+            const float z0 = e0[8 + g8], z1 = e1[8 + g8];
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+              wa[m][0] = e0[2 * m] * z0, wa[m][1] = e0[2 * m + 1] * z0;
+              wb[m][0] = e1[2 * m] * z1, wb[m][1] = e1[2 * m + 1] * z1;
+            }
+          }
 #pragma unroll
           for (int m = 0; m < 4; ++m) {
             unsigned ah[4], al[4];
-            split_tf32(xs0[m] * yz0a, ah[0], al[0]);
-            split_tf32(xs0[m] * yz0b, ah[1], al[1]);
-            split_tf32(xs1[m] * yz1a, ah[2], al[2]);
-            split_tf32(xs1[m] * yz1b, ah[3], al[3]);
+            split_tf32(wa[m][0], ah[0], al[0]);
+            split_tf32(wa[m][1], ah[1], al[1]);
+            split_tf32(wb[m][0], ah[2], al[2]);
+            split_tf32(wb[m][1], ah[3], al[3]);
 #pragma unroll
             for (int nt = 0; nt < 2; ++nt) {
               mma_tf32(D[m][nt], ah, bh[nt][0], bh[nt][1]);
@@ -1751,14 +1796,17 @@ __global__ void __launch_bounds__(256, 3) adj_b3_kernel(Geo g, const int4* __res
         for (int j = 0; j < n; ++j) {
           const float* e = S + j * kBS;
           const bool nf = (guarded >> j) & 1u;
-          const float z = e[8 + (g8 & 3)];
 #pragma unroll
           for (int m = 0; m < 4; ++m) {
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
-              const float y = e[4 + (g8 >> 2) + 2 * h];
-              const float w = e[m] * (y * z);
-              const bool ok = !nf || (!signbit(e[m]) && !signbit(y) && !signbit(z));
+              int lx, ly, lz;
+              frag_cell<NDIM>(m, h, g8, lx, ly, lz);
+              // weights of the cell along each dim: 3D rows x 0-3, y 4-7, z 8-11; 2D y 0-7, z 8-15
+              const float wx = NDIM == 3 ? e[lx] : 1.f;
+              const float y = NDIM == 3 ? e[4 + ly] : e[ly], z = e[8 + lz];
+              const float w = wx * (y * z);
+              const bool ok = !nf || (!signbit(wx) && !signbit(y) && !signbit(z));
 #pragma unroll
               for (int nt = 0; nt < 2; ++nt) {
                 const float2 v = *reinterpret_cast<const float2*>(e + 16 + 2 * (4 * nt + t4));
@@ -1779,14 +1827,16 @@ __global__ void __launch_bounds__(256, 3) adj_b3_kernel(Geo g, const int4* __res
       for (int m = 0; m < 4; ++m)
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
-          const int cell = m * 16 + ((g8 >> 2) + 2 * h) * 4 + (g8 & 3);
+          int lx, ly, lz;
+          frag_cell<NDIM>(m, h, g8, lx, ly, lz);
+          const int cell = cell_index<NDIM>(lx, ly, lz);
 #pragma unroll
           for (int nt = 0; nt < 2; ++nt)
             *reinterpret_cast<float2*>(dst + cell * 16 + 2 * (4 * nt + t4)) =
                 make_float2(D[m][nt][2 * h], D[m][nt][2 * h + 1]);
         }
     } else {
-      frag_store(g, gridv, c0, ncoil, kBE * bx, kBE * by, kBE * bz, g8, t4, D);
+      frag_store<NDIM>(g, gridv, c0, ncoil, it.x, g8, t4, D);
     }
   }
 }
@@ -1796,6 +1846,7 @@ __global__ void __launch_bounds__(256, 3) adj_b3_kernel(Geo g, const int4* __res
 // pair) sums the q-th quarter of the parts in slot order, one float4 of each,
 // eight in flight (the block at the centre of a dense trajectory has a few
 // hundred parts); then the quarters are added in order.
+template <int NDIM>
 __global__ void __launch_bounds__(1024) adj_reduce_b3_kernel(Geo g, const int4* __restrict__ split,
                                                              const float* __restrict__ partial,
                                                              float* __restrict__ gridv) {
@@ -1846,7 +1897,9 @@ __global__ void __launch_bounds__(1024) adj_reduce_b3_kernel(Geo g, const int4* 
   }
   int bx, by, bz;
   block_origin(g, sp.x, bx, by, bz);
-  const int x = kBE * bx + (cell >> 4), y = kBE * by + ((cell >> 2) & 3), z = kBE * bz + (cell & 3);
+  const int x = bx * block_edge(NDIM, 0) + (NDIM == 3 ? cell >> 4 : 0);
+  const int y = by * block_edge(NDIM, 1) + (NDIM == 3 ? (cell >> 2) & 3 : cell >> 3);
+  const int z = bz * block_edge(NDIM, 2) + (NDIM == 3 ? cell & 3 : cell & 7);
   if (x >= g.N[0] || y >= g.N[1] || z >= g.N[2]) return;
   const long long gvol = (long long)g.N[0] * g.N[1] * g.N[2];
   float* dst = gridv + ((long long)(c0 + 2 * ep) * gvol + ((long long)x * g.N[1] + y) * g.N[2] + z) * 2;
@@ -3045,21 +3098,22 @@ bool records_ok(const Geo& g) {
   return g.ndim == 2 && g.T[1] == 16 && g.T[2] == 16 && g.NT[1] == 5 && g.NT[2] == 5;
 }
 
-// 3D geometries whose plans also carry block lists (adj_b3_kernel): the
-// records' geometry, and in circular mode every dim a multiple of 4 cells
-// and at least 16, so that a wrapped window meets at most 2 blocks per dim
-// and each of them once.
+// Geometries whose plans also carry block lists (adj_b3_kernel): those of
+// the tap records (3D 8^3 or 2D 16 x 16 tiles, at most 5 taps per dim), and
+// in circular mode every active dim a multiple of the block edge and at
+// least 16 cells, so that a wrapped window meets at most 2 blocks per dim and
+// each of them once.
 bool blocks_ok(const Geo& g) {
-  if (g.ndim != 3 || !records_ok(g) || g.npts >= (1ll << kSelShift)) return false;
+  if (g.ndim < 2 || !records_ok(g) || g.npts >= (1ll << kSelShift)) return false;
   if (g.pad == TLGB_PAD_CIRCULAR)
-    for (int e = 0; e < 3; ++e)
-      if (g.N[e] < 16 || g.N[e] % kBE != 0) return false;
-  const int64_t nb = (int64_t)blocks_along(g.N[0]) * blocks_along(g.N[1]) * blocks_along(g.N[2]);
+    for (int e = 3 - g.ndim; e < 3; ++e)
+      if (g.N[e] < 16 || g.N[e] % block_edge(g.ndim, e) != 0) return false;
+  const int64_t nb = (int64_t)blocks_along(g, 0) * blocks_along(g, 1) * blocks_along(g, 2);
   return nb < (1ll << 31);
 }
 
 // Blocks one window can meet along a dim: 2 (at most 5 taps over 4 cells)
-int64_t max_blocks_per_dim(const Geo& g, int e) { return blocks_along(g.N[e]) == 1 ? 1 : 2; }
+int64_t max_blocks_per_dim(const Geo& g, int e) { return blocks_along(g, e) == 1 ? 1 : 2; }
 
 // The kernel, norm and beta a plan's records hold weights for
 int64_t kernel_key(const Geo& g) {
@@ -3091,7 +3145,7 @@ PlanLayout layout(const Geo& g) {
   L.nblocks = L.eb_max = L.max_blk_items = 0;
   L.off_blk_entries = L.off_blk_items = L.off_blk_split = L.off_blk_rows = 0;
   if (blocks_ok(g) && g.npts > 0) {
-    L.nblocks = (int64_t)blocks_along(g.N[0]) * blocks_along(g.N[1]) * blocks_along(g.N[2]);
+    L.nblocks = (int64_t)blocks_along(g, 0) * blocks_along(g, 1) * blocks_along(g, 2);
     L.eb_max = g.npts * max_blocks_per_dim(g, 0) * max_blocks_per_dim(g, 1) * max_blocks_per_dim(g, 2);
     L.max_blk_items = L.nblocks + cdiv(L.eb_max, kBlkPart) + 1;
     L.off_blk_entries = o;
@@ -3101,7 +3155,7 @@ PlanLayout layout(const Geo& g) {
     L.off_blk_split = o;
     o = align_up(o + (size_t)(L.nblocks + 1) * 16, 256);
     L.off_blk_rows = o;
-    o = align_up(o + (size_t)g.npts * 96, 256);
+    o = align_up(o + (size_t)g.npts * row_floats(g.ndim) * 4, 256);
   }
   L.bytes = o;
   const int64_t pairs = std::max<int64_t>(std::max(L.e_max, L.eb_max), 1);  // sort buffers serve both lists
@@ -3351,7 +3405,7 @@ extern "C" int tlgb_interp_plan_build(const tlgb_interp_desc* d, const float* lo
     TLGB_TRY(exclusive_scan_u32(cnt, cnt, g.npts, total, counts, s));
     blk_emit_kernel<<<nb, 256, 0, s>>>(g, recs, cnt, keys, bentries);
     TLGB_CHECK_LAUNCH();
-    blk_rows_kernel<<<nb, 256, 0, s>>>(g, locs, recs, (float4*)(P + L.off_blk_rows));
+    blk_rows_kernel<<<nb, 256, 0, s>>>(g, locs, recs, (float*)(P + L.off_blk_rows));
     TLGB_CHECK_LAUNCH();
     TLGB_CUDA(cudaMemcpyAsync(&Eb, total, 4, cudaMemcpyDeviceToHost, s));
     TLGB_CUDA(cudaStreamSynchronize(s));
@@ -3371,7 +3425,7 @@ extern "C" int tlgb_interp_plan_build(const tlgb_interp_desc* d, const float* lo
     // together in time and find its rows and values in L2
     std::vector<int64_t> bstart((size_t)L.nblocks + 1, 0);
     for (int64_t b = 0; b < L.nblocks; ++b) bstart[(size_t)b + 1] = bstart[(size_t)b] + hb[(size_t)b];
-    const int64_t nbx = blocks_along(g.N[0]), nby = blocks_along(g.N[1]), nbz = blocks_along(g.N[2]);
+    const int64_t nbx = blocks_along(g, 0), nby = blocks_along(g, 1), nbz = blocks_along(g, 2);
     auto add_block = [&](int64_t b) {
       const int64_t n = hb[(size_t)b], bpos = bstart[(size_t)b];
       if (n == 0) {
@@ -3450,7 +3504,7 @@ bool fast2(const Geo& g, int cg);
 void adj_scratch_parts(const Geo& g, const tlgb_interp_plan_info* info, size_t& partial_bytes, size_t& tv_bytes) {
   const int cg = adj_cg(g);
   const int64_t ncg = cdiv(std::max<long long>(g.nbatch, 1), cg);
-  partial_bytes = fast3(g, cg) && info->n_blk_items > 0
+  partial_bytes = (fast3(g, cg) || fast2(g, cg)) && info->n_blk_items > 0
                       ? align_up((size_t)info->n_blk_partials * ncg * 64 * 16 * sizeof(float), 256)
                       : align_up((size_t)info->n_partials * ncg * tile_floats(g, cg) * sizeof(float), 256);
   tv_bytes = ((fast3(g, cg) || fast2(g, cg)) && info->off_records > 0) ? (size_t)ncg * g.npts * 8 * 8 : 0;
@@ -3610,11 +3664,12 @@ int launch_adj_f3(const Geo& g, const tlgb_interp_plan_info* info, const char* P
   return TLGB_OK;
 }
 
+template <int NDIM>
 int launch_adj_b3(const Geo& g, const tlgb_interp_plan_info* info, const char* P, const float* locs,
                   const void* vals, void* grid, void* scratch, cudaStream_t s) {
   const int64_t ncg = cdiv(g.nbatch, 8);
   const size_t sm = 8 * kBC * kBS * sizeof(float);
-  TLGB_TRY(set_smem(adj_b3_kernel, sm));
+  TLGB_TRY(set_smem(adj_b3_kernel<NDIM>, sm));
   // 16-byte asynchronous copies of the weight rows and transposed values
   if (((uintptr_t)P & 15) || ((uintptr_t)scratch & 15))
     TLGB_FAIL(TLGB_ERR_INVALID, "interp adjoint: plan and scratch must be 16-byte aligned");
@@ -3628,14 +3683,15 @@ int launch_adj_b3(const Geo& g, const tlgb_interp_plan_info* info, const char* P
     tv = reinterpret_cast<const float4*>(t);
   }
   dim3 grd((unsigned)cdiv(info->n_blk_items, kB3Items), (unsigned)ncg);
-  adj_b3_kernel<<<grd, 256, sm, s>>>(g, (const int4*)(P + info->off_blk_items), (int)info->n_blk_items,
-                                    (const uint32_t*)(P + info->off_blk_entries), (const float4*)(P + info->off_blk_rows),
-                                    (const float2*)vals, tv, (float*)grid, (float*)scratch);
+  adj_b3_kernel<NDIM><<<grd, 256, sm, s>>>(g, (const int4*)(P + info->off_blk_items), (int)info->n_blk_items,
+                                          (const uint32_t*)(P + info->off_blk_entries),
+                                          (const float*)(P + info->off_blk_rows), (const float2*)vals, tv,
+                                          (float*)grid, (float*)scratch);
   TLGB_CHECK_LAUNCH();
   if (info->n_blk_split > 0) {
     dim3 g2((unsigned)info->n_blk_split, (unsigned)ncg);
-    adj_reduce_b3_kernel<<<g2, 1024, 0, s>>>(g, (const int4*)(P + info->off_blk_split), (const float*)scratch,
-                                            (float*)grid);
+    adj_reduce_b3_kernel<NDIM><<<g2, 1024, 0, s>>>(g, (const int4*)(P + info->off_blk_split),
+                                                  (const float*)scratch, (float*)grid);
     TLGB_CHECK_LAUNCH();
   }
   return TLGB_OK;
@@ -3686,9 +3742,11 @@ int launch_adj_t(const Geo& g, int cg, const tlgb_interp_plan_info* info, const 
                  const void* vals, void* grid, void* scratch, cudaStream_t s) {
   if constexpr (N == 4 && NDIM == 3 && NTB == 5)
     if (fast3(g, cg) && info->off_records > 0 && info->n_blk_items > 0)
-      return launch_adj_b3(g, info, P, locs, vals, grid, scratch, s);
+      return launch_adj_b3<3>(g, info, P, locs, vals, grid, scratch, s);
     if (fast3(g, cg) && info->off_records > 0) return launch_adj_f3(g, info, P, locs, vals, grid, scratch, s);
   if constexpr (NDIM == 2 && NTB == 5)
+    if (fast2(g, cg) && info->off_records > 0 && info->n_blk_items > 0)
+      return launch_adj_b3<2>(g, info, P, locs, vals, grid, scratch, s);
     if (fast2(g, cg) && info->off_records > 0) return launch_adj_f2(g, info, P, locs, vals, grid, scratch, s);
   return launch_adj_t2<N, NDIM, NTB, false>(g, cg, info, P, locs, vals, grid, scratch, s);
 }
