@@ -438,6 +438,7 @@ def run_gpu(args, world, rank, local):
     }
     del img, vals, img_h, grid_h
     torch.cuda.empty_cache()
+    kernels["one_coil"] = bench_one_coil(locs, dev, peak)
     if not args.skip_blocks:
         kernels.update(bench_blocks(dev, peak, args))
     if not args.skip_nufft2d:
@@ -746,6 +747,52 @@ def bench_nufft3d(locs_h, dev):
     del x, y, A, AH, AN
     torch.cuda.empty_cache()
     return out
+
+
+def bench_one_coil(locs, dev, peak):
+    """The headline trajectory with one batch entry (a one-coil NUFFT, the
+    Toeplitz kernel's single image): ungrid a 256^3 complex image at the 2^21
+    points and grid the points back, each the mean of 10 CUDA-event timings
+    with a 512 MB write between timings to flush L2 (the image alone is about
+    the size of L2). The 8-entry kernels run with the other 7 entries empty;
+    the algorithmic bytes are one entry's grid and values plus the
+    coordinates."""
+    import torchlinops_gb300 as T
+
+    kp = dict(beta=kb_beta())
+    gen = torch.Generator(device=dev).manual_seed(11)
+    img = torch.randn(1, N_GRID, N_GRID, N_GRID, dtype=torch.complex64, device=dev, generator=gen)
+    vals = torch.randn(1, N_PTS, dtype=torch.complex64, device=dev, generator=gen)
+    flush = torch.empty(1 << 27, dtype=torch.float32, device=dev)
+    s = torch.cuda.current_stream(dev)
+    for _ in range(3):
+        T.ungrid(img, locs, WIDTH, kernel_params=kp)
+        T.grid(vals, locs, (N_GRID,) * 3, WIDTH, kernel_params=kp)
+
+    def mean_ms(fn, reps=10):
+        ts = []
+        for _ in range(reps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(s)
+            fn()
+            e1.record(s)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return statistics.mean(ts)
+
+    fwd = mean_ms(lambda: T.ungrid(img, locs, WIDTH, kernel_params=kp))
+    adj = mean_ms(lambda: T.grid(vals, locs, (N_GRID,) * 3, WIDTH, kernel_params=kp))
+    algo = N_GRID**3 * 8 + N_PTS * 3 * 4 + N_PTS * 8
+    del img, vals, flush
+    torch.cuda.empty_cache()
+
+    def entry(ms):
+        gbps = algo / (ms / 1e3) / 1e9
+        return {"ms": ms, "GBps": gbps, "frac": gbps / peak, "samples_per_s": N_PTS / (ms / 1e3)}
+
+    return {"workload": f"interp3d_{N_GRID}cube_1coil_{N_PTS}pts", "algorithmic_bytes": algo,
+            "l2": "512 MB write between timings", "ungrid": entry(fwd), "grid": entry(adj)}
 
 
 def bench_toeplitz(locs, maps, xt, n, dev):

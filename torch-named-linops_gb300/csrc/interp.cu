@@ -1187,23 +1187,53 @@ __device__ int g_tlgb_status;
 
 // Point values [batch][npts] (complex) -> point-major [group][npts][8]: the
 // gridding reads 64 contiguous bytes per (point, tile) pair instead of 8
-// scattered 8-byte values. CTA = 32 points x 8 entries of one group.
+// scattered 8-byte values. CTA = 128 points x 8 entries of one group: warp c
+// loads entry c two points per 16-byte load (when the rows are 16-byte
+// aligned), each thread stores two 16-byte pairs of entries; 32 bytes in
+// flight per thread each way. Block (0, group) also zeroes the group's work
+// counter of the gridding launched after it (ctr, when given).
+constexpr int kTrPts = 128;
 __global__ void __launch_bounds__(256) transpose_vals_kernel(const float2* __restrict__ vals, long long npts,
-                                                             long long nbatch, float2* __restrict__ tv) {
-  __shared__ float2 sm[32][9];
+                                                             long long nbatch, float2* __restrict__ tv,
+                                                             int* __restrict__ ctr) {
+  __shared__ __align__(16) float2 sm[kTrPts][10];  // rows of 80 bytes: entry pairs 16-byte aligned
   const int grp = blockIdx.y;
-  const long long p0 = (long long)blockIdx.x * 32;
+  const long long p0 = (long long)blockIdx.x * kTrPts;
   const int t = threadIdx.x;
+  if (ctr && blockIdx.x == 0 && t == 0) ctr[grp] = 0;
   {
-    const int c = t >> 5, i = t & 31;
-    const long long p = p0 + i, cc = (long long)grp * 8 + c;
-    sm[i][c] = (p < npts && cc < nbatch) ? __ldg(vals + cc * npts + p) : make_float2(0.f, 0.f);
+    const int c = t >> 5, lane = t & 31;
+    const long long cc = (long long)grp * 8 + c;
+    const float2* src = vals + cc * npts;
+    const bool vec = ((reinterpret_cast<uintptr_t>(vals) | (uintptr_t)(npts * 8)) & 15) == 0;
+    float2 a[2], b[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const long long p = p0 + h * 64 + 2 * lane;
+      a[h] = b[h] = make_float2(0.f, 0.f);
+      if (cc < nbatch) {
+        if (vec && p + 1 < npts) {
+          const float4 v = __ldg(reinterpret_cast<const float4*>(src + p));
+          a[h] = make_float2(v.x, v.y), b[h] = make_float2(v.z, v.w);
+        } else {
+          if (p < npts) a[h] = __ldg(src + p);
+          if (p + 1 < npts) b[h] = __ldg(src + p + 1);
+        }
+      }
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      sm[h * 64 + 2 * lane][c] = a[h];
+      sm[h * 64 + 2 * lane + 1][c] = b[h];
+    }
   }
   __syncthreads();
-  {
-    const int i = t >> 3, c = t & 7;
+  float4* dst = reinterpret_cast<float4*>(tv) + (long long)grp * npts * 4;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int j = h * 256 + t, i = j >> 2, q = j & 3;  // point i, entries 2q and 2q + 1
     const long long p = p0 + i;
-    if (p < npts) tv[((long long)grp * npts + p) * 8 + c] = sm[i][c];
+    if (p < npts) dst[p * 4 + q] = *reinterpret_cast<const float4*>(&sm[i][2 * q]);
   }
 }
 
@@ -1530,10 +1560,11 @@ __global__ void __launch_bounds__(256, 4) adj_f3_kernel(Geo g, const int4* __res
 
 // ------------------------------------------------- block gridding (3D, 8 entries)
 //
-// A CTA takes 64 consecutive work items (blocks, parts of dense blocks, runs
-// of empty blocks); its warps take them one at a time from a shared counter,
-// so a dense block costs one warp, not the CTA, and which warp takes an item
-// does not change its result. A warp holds its item's 4 x 4 x 4-cell output
+// Work items are blocks, parts of dense blocks and runs of empty blocks. A
+// persistent grid's warps take them one at a time, in list order, from a
+// counter in global memory, so a dense block costs one warp, not a CTA, no
+// SM idles behind a CTA's last items, and which warp takes an item does not
+// change its result. A warp holds its item's 4 x 4 x 4-cell output
 // block x 8 complex entries as the accumulators of warp-level tensor-core
 // products (mma.sync m16n8k8, tf32 inputs, fp32 accumulation): the block's
 // 64 cells are the 4 row tiles (one per x, rows (y, z)), the 8 entries'
@@ -1550,7 +1581,7 @@ __global__ void __launch_bounds__(256, 4) adj_f3_kernel(Geo g, const int4* __res
 // cells of its window only (a zero weight would carry its NaN or Inf to the
 // whole block); the rows mark the cells outside the window with -0.0.
 constexpr int kBC = 32;       // entries per chunk (one per lane while staging)
-constexpr int kB3Items = 64;  // work items per CTA, taken by its warps one at a time
+constexpr int kB3Ctas = 3;    // resident CTAs per SM of the persistent grid
 constexpr int kBS = 40;       // floats per staged entry: x row 0-3 | y row 4-7 | z row 8-11 | values 16-31
                               // (40: the tensor-core operand loads of a group of 8 entries are free of
                               // bank conflicts)
@@ -1634,25 +1665,25 @@ __device__ __forceinline__ void frag_store(const Geo& g, float* __restrict__ gri
 }
 
 template <int NDIM>
-__global__ void __launch_bounds__(256, 3) adj_b3_kernel(Geo g, const int4* __restrict__ items, int nitems,
+__global__ void __launch_bounds__(256, kB3Ctas) adj_b3_kernel(Geo g, const int4* __restrict__ items, int nitems,
                                                         const uint32_t* __restrict__ bentries,
                                                         const float* __restrict__ rows,
                                                         const float2* __restrict__ vals,
                                                         const float4* __restrict__ tv, float* __restrict__ gridv,
-                                                        float* __restrict__ partial) {
+                                                        float* __restrict__ partial, int* __restrict__ ctr) {
   extern __shared__ __align__(16) float bsm[];
-  __shared__ int next_item;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (threadIdx.x == 0) next_item = 0;
-  __syncthreads();  // the only CTA-wide synchronisation: the warps then take items on their own
   float* S = bsm + warp * (kBC * kBS);
   const int cg = blockIdx.y, c0 = cg * 8;
   const int ncoil = (int)min(8ll, g.nbatch - c0);
   const int g8 = lane >> 2, t4 = lane & 3;
-  const int first = blockIdx.x * kB3Items, last = min(nitems, first + kB3Items);
+  const int last = nitems;
+  // the warps of all CTAs take the items in list order from the group's
+  // counter (zeroed before the launch), so the items worked on at one time
+  // are neighbours in the list; the warps never wait for one another
   auto grab = [&]() {
     int i = 0;
-    if (lane == 0) i = first + atomicAdd(&next_item, 1);
+    if (lane == 0) i = atomicAdd(ctr + cg, 1);
     return __shfl_sync(0xffffffffu, i, 0);
   };
   // one item and the next chunk's point indices ahead: a chunk's copies wait
@@ -1842,26 +1873,25 @@ __global__ void __launch_bounds__(256, 3) adj_b3_kernel(Geo g, const int4* __res
 }
 
 // Sum the partial blocks of one split block in slot order, compensated (as
-// adj_reduce_f3_kernel). CTA = 1024 threads: thread (quarter q, cell, entry
-// pair) sums the q-th quarter of the parts in slot order, one float4 of each,
-// eight in flight (the block at the centre of a dense trajectory has a few
-// hundred parts); then the quarters are added in order.
+// adj_reduce_f3_kernel). CTA = 256 threads, thread (cell, entry pair) sums
+// one float4 of every part, eight in flight. Most split blocks have a few
+// parts, so small CTAs keep many blocks in flight per SM; the plan lists the
+// blocks with the most parts (a few hundred at the centre of a dense
+// trajectory) first, so their longer chains overlap the rest.
 template <int NDIM>
-__global__ void __launch_bounds__(1024) adj_reduce_b3_kernel(Geo g, const int4* __restrict__ split,
-                                                             const float* __restrict__ partial,
-                                                             float* __restrict__ gridv) {
-  __shared__ float4 qs[3][256], qc[3][256];
+__global__ void __launch_bounds__(256) adj_reduce_b3_kernel(Geo g, const int4* __restrict__ split,
+                                                            const float* __restrict__ partial,
+                                                            float* __restrict__ gridv) {
   const int4 sp = split[blockIdx.x];
   const int cg = blockIdx.y, ncg = gridDim.y, c0 = cg * 8;
   const int ncoil = (int)min(8ll, g.nbatch - c0);
-  const int q = threadIdx.x >> 8, r = threadIdx.x & 255;
+  const int r = threadIdx.x;
   const int cell = r >> 2, ep = r & 3;  // entries 2 ep, 2 ep + 1
   const long long step = (long long)ncg * 64 * 4;  // float4s between consecutive partials
   const float4* src = reinterpret_cast<const float4*>(partial + ((long long)sp.y * ncg + cg) * 64 * 16) + r;
-  const int k0 = (int)((long long)sp.z * q / 4), k1 = (int)((long long)sp.z * (q + 1) / 4);
   float4 sum = make_float4(0.f, 0.f, 0.f, 0.f), comp = sum;
-  int k = k0;
-  for (; k + 8 <= k1; k += 8) {
+  int k = 0;
+  for (; k + 8 <= sp.z; k += 8) {
     float4 v[8];
 #pragma unroll
     for (int i = 0; i < 8; ++i) v[i] = __ldg(src + (k + i) * step);
@@ -1873,27 +1903,19 @@ __global__ void __launch_bounds__(1024) adj_reduce_b3_kernel(Geo g, const int4* 
       comp_add(sum.w, comp.w, v[i].w);
     }
   }
-  for (; k < k1; ++k) {
-    const float4 v = __ldg(src + k * step);
-    comp_add(sum.x, comp.x, v.x);
-    comp_add(sum.y, comp.y, v.y);
-    comp_add(sum.z, comp.z, v.z);
-    comp_add(sum.w, comp.w, v.w);
-  }
-  if (q > 0) {
-    qs[q - 1][r] = sum;
-    qc[q - 1][r] = comp;
-  }
-  __syncthreads();
-  if (q > 0) return;
+  if (k < sp.z) {  // the last 1-7 parts, loaded together
+    float4 v[7];
 #pragma unroll
-  for (int i = 0; i < 3; ++i) {  // the later quarters in order, their compensations with them
-    const float4 s2 = qs[i][r], c2 = qc[i][r];
-    comp_add(sum.x, comp.x, s2.x);
-    comp_add(sum.y, comp.y, s2.y);
-    comp_add(sum.z, comp.z, s2.z);
-    comp_add(sum.w, comp.w, s2.w);
-    comp.x += c2.x, comp.y += c2.y, comp.z += c2.z, comp.w += c2.w;
+    for (int i = 0; i < 7; ++i)
+      if (k + i < sp.z) v[i] = __ldg(src + (k + i) * step);
+#pragma unroll
+    for (int i = 0; i < 7; ++i)
+      if (k + i < sp.z) {
+        comp_add(sum.x, comp.x, v[i].x);
+        comp_add(sum.y, comp.y, v[i].y);
+        comp_add(sum.z, comp.z, v[i].z);
+        comp_add(sum.w, comp.w, v[i].w);
+      }
   }
   int bx, by, bz;
   block_origin(g, sp.x, bx, by, bz);
@@ -3454,6 +3476,9 @@ extern "C" int tlgb_interp_plan_build(const tlgb_interp_desc* d, const float* lo
             for (int64_t by = cy; by < std::min(nby, cy + kCube); ++by)
               for (int64_t bz = cz; bz < std::min(nbz, cz + kCube); ++bz) add_block((bx * nby + by) * nbz + bz);
     if ((int64_t)bitems.size() > L.max_blk_items) TLGB_FAIL(TLGB_ERR_DEVICE, "block work list larger than its bound");
+    // split blocks with the most parts first: their sums are the longest
+    // chains of the reduction, so they start in its first wave
+    std::stable_sort(bsplit.begin(), bsplit.end(), [](const int4& a, const int4& b) { return a.z > b.z; });
     if (!bitems.empty())
       TLGB_CUDA(cudaMemcpyAsync(P + L.off_blk_items, bitems.data(), bitems.size() * 16, cudaMemcpyHostToDevice, s));
     if (!bsplit.empty())
@@ -3499,13 +3524,19 @@ namespace {
 bool fast3(const Geo& g, int cg);
 bool fast2(const Geo& g, int cg);
 
-// Gridding scratch: the partial tiles of split tiles, then (3D 8-entry path
-// only) the point values transposed to point-major order.
+// bytes of the block path's partial blocks: 4 KB per part and group of 8 entries
+size_t blk_partial_bytes(const tlgb_interp_plan_info* info, int64_t ncg) {
+  return align_up((size_t)info->n_blk_partials * ncg * 64 * 16 * sizeof(float), 256);
+}
+
+// Gridding scratch: the partial tiles of split tiles (block path: the partial
+// blocks and the work counters), then (8-entry paths) the point values
+// transposed to point-major order.
 void adj_scratch_parts(const Geo& g, const tlgb_interp_plan_info* info, size_t& partial_bytes, size_t& tv_bytes) {
   const int cg = adj_cg(g);
   const int64_t ncg = cdiv(std::max<long long>(g.nbatch, 1), cg);
   partial_bytes = (fast3(g, cg) || fast2(g, cg)) && info->n_blk_items > 0
-                      ? align_up((size_t)info->n_blk_partials * ncg * 64 * 16 * sizeof(float), 256)
+                      ? blk_partial_bytes(info, ncg) + align_up((size_t)ncg * sizeof(int), 256)
                       : align_up((size_t)info->n_partials * ncg * tile_floats(g, cg) * sizeof(float), 256);
   tv_bytes = ((fast3(g, cg) || fast2(g, cg)) && info->off_records > 0) ? (size_t)ncg * g.npts * 8 * 8 : 0;
 }
@@ -3645,8 +3676,8 @@ int launch_adj_f3(const Geo& g, const tlgb_interp_plan_info* info, const char* P
   const float4* tv = nullptr;
   if (g.tv_off >= 0 && g.npts > 0) {
     float2* t = reinterpret_cast<float2*>(static_cast<char*>(scratch) + g.tv_off);
-    dim3 gt((unsigned)cdiv(g.npts, 32), (unsigned)ncg);
-    transpose_vals_kernel<<<gt, 256, 0, s>>>((const float2*)vals, g.npts, g.nbatch, t);
+    dim3 gt((unsigned)cdiv(g.npts, kTrPts), (unsigned)ncg);
+    transpose_vals_kernel<<<gt, 256, 0, s>>>((const float2*)vals, g.npts, g.nbatch, t, nullptr);
     TLGB_CHECK_LAUNCH();
     tv = reinterpret_cast<const float4*>(t);
   }
@@ -3674,24 +3705,31 @@ int launch_adj_b3(const Geo& g, const tlgb_interp_plan_info* info, const char* P
   if (((uintptr_t)P & 15) || ((uintptr_t)scratch & 15))
     TLGB_FAIL(TLGB_ERR_INVALID, "interp adjoint: plan and scratch must be 16-byte aligned");
   if ((uintptr_t)vals & 7) TLGB_FAIL(TLGB_ERR_INVALID, "interp adjoint: values must be 8-byte aligned");
+  // the work counters (one per group of 8 entries) follow the partial blocks
+  int* ctr = reinterpret_cast<int*>(static_cast<char*>(scratch) + blk_partial_bytes(info, ncg));
   const float4* tv = nullptr;
   if (g.tv_off >= 0 && g.npts > 0) {
     float2* t = reinterpret_cast<float2*>(static_cast<char*>(scratch) + g.tv_off);
-    dim3 gt((unsigned)cdiv(g.npts, 32), (unsigned)ncg);
-    transpose_vals_kernel<<<gt, 256, 0, s>>>((const float2*)vals, g.npts, g.nbatch, t);
+    dim3 gt((unsigned)cdiv(g.npts, kTrPts), (unsigned)ncg);
+    transpose_vals_kernel<<<gt, 256, 0, s>>>((const float2*)vals, g.npts, g.nbatch, t, ctr);
     TLGB_CHECK_LAUNCH();
     tv = reinterpret_cast<const float4*>(t);
+  } else {
+    TLGB_CUDA(cudaMemsetAsync(ctr, 0, (size_t)ncg * sizeof(int), s));
   }
-  dim3 grd((unsigned)cdiv(info->n_blk_items, kB3Items), (unsigned)ncg);
+  // persistent: kB3Ctas CTAs per SM (fewer when there are few items), any
+  // number of which may be resident at once
+  const int64_t nctas = std::min<int64_t>(cdiv(info->n_blk_items, 8), (int64_t)kB3Ctas * sm_count());
+  dim3 grd((unsigned)std::max<int64_t>(nctas, 1), (unsigned)ncg);
   adj_b3_kernel<NDIM><<<grd, 256, sm, s>>>(g, (const int4*)(P + info->off_blk_items), (int)info->n_blk_items,
                                           (const uint32_t*)(P + info->off_blk_entries),
                                           (const float*)(P + info->off_blk_rows), (const float2*)vals, tv,
-                                          (float*)grid, (float*)scratch);
+                                          (float*)grid, (float*)scratch, ctr);
   TLGB_CHECK_LAUNCH();
   if (info->n_blk_split > 0) {
     dim3 g2((unsigned)info->n_blk_split, (unsigned)ncg);
-    adj_reduce_b3_kernel<NDIM><<<g2, 1024, 0, s>>>(g, (const int4*)(P + info->off_blk_split),
-                                                  (const float*)scratch, (float*)grid);
+    adj_reduce_b3_kernel<NDIM><<<g2, 256, 0, s>>>(g, (const int4*)(P + info->off_blk_split),
+                                                 (const float*)scratch, (float*)grid);
     TLGB_CHECK_LAUNCH();
   }
   return TLGB_OK;
@@ -3707,8 +3745,8 @@ int launch_adj_f2(const Geo& g, const tlgb_interp_plan_info* info, const char* P
   const float4* tv = nullptr;
   if (g.tv_off >= 0 && g.npts > 0) {
     float2* t = reinterpret_cast<float2*>(static_cast<char*>(scratch) + g.tv_off);
-    dim3 gt((unsigned)cdiv(g.npts, 32), (unsigned)ncg);
-    transpose_vals_kernel<<<gt, 256, 0, s>>>((const float2*)vals, g.npts, g.nbatch, t);
+    dim3 gt((unsigned)cdiv(g.npts, kTrPts), (unsigned)ncg);
+    transpose_vals_kernel<<<gt, 256, 0, s>>>((const float2*)vals, g.npts, g.nbatch, t, nullptr);
     TLGB_CHECK_LAUNCH();
     tv = reinterpret_cast<const float4*>(t);
   }
