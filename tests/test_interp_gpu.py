@@ -168,27 +168,28 @@ def test_eight_entry_2d_paths_against_oracle(shape, nb, pad, kernel):
     assert rel_l2(adj, OI.grid(pts, locs, shape, 4.0, beta=beta, dtype=torch.float64, **kw)) < TOL
 
 
+@pytest.mark.parametrize("nb", [8, 3, 1])
 @pytest.mark.parametrize("kernel", ["kaiser_bessel", "spline"])
-def test_grid_nonfinite_values_stay_in_their_windows(kernel):
+def test_grid_nonfinite_values_stay_in_their_windows(kernel, nb):
     """A NaN or Inf point value turns exactly the cells of its window
     non-finite (its valid taps, zero-weight ones included) and no other cell:
-    the 3D 8-entry path, whose rows of tap weights hold zeros outside a
-    window, sends such points through the per-tap path. The reference's own
+    the 3D block paths (8 entries, and 1, 2 or 4), whose rows of tap weights
+    hold zeros outside a window, send such points through the per-tap path. The reference's own
     torch path multiplies every tap of the ceil(W+1)^3 patch by the value,
     masked taps included (grid.py:624, weights * mask * val), so there a NaN
     reaches the whole patch: a superset of the window."""
     gen = torch.Generator().manual_seed(9)
     shape = (32, 32, 32)
     locs = _ball_locs(20000, 12.0, torch.tensor([16.0, 16.0, 16.0]), gen)
-    pts = torch.complex(torch.randn(8, 20000, generator=gen), torch.randn(8, 20000, generator=gen))
-    bad = [(3, 17, complex(float("nan"), 0.0)), (5, 900, complex(float("inf"), 1.0)),
+    pts = torch.complex(torch.randn(nb, 20000, generator=gen), torch.randn(nb, 20000, generator=gen))
+    bad = [(3 % nb, 17, complex(float("nan"), 0.0)), (5 % nb, 900, complex(float("inf"), 1.0)),
            (0, 4000, complex(0.0, float("-inf")))]
     for c, p, v in bad:
         pts[c, p] = v
     beta = OI.nufft_beta(4.0, 1.25)
     out = T.grid(pts.to(DEV), locs.to(DEV), shape, 4.0, kernel=kernel, kernel_params=dict(beta=beta)).cpu()
     ref = OI.grid(pts, locs, shape, 4.0, kernel=kernel, beta=beta)
-    window = torch.zeros(8, *shape, dtype=torch.bool)
+    window = torch.zeros(nb, *shape, dtype=torch.bool)
     for c, p, _ in bad:
         taps = []
         for e in range(3):
@@ -202,10 +203,11 @@ def test_grid_nonfinite_values_stay_in_their_windows(kernel):
     assert rel_l2(out[fin], ref[fin]) < TOL
 
 
-def test_gridding_is_deterministic():
+@pytest.mark.parametrize("nb", [8, 4, 1])
+def test_gridding_is_deterministic(nb):
     gen = torch.Generator().manual_seed(5)
     locs = _ball_locs(200000, 33, 32, gen).to(DEV)
-    pts = torch.randn(8, 200000, dtype=torch.complex64, generator=gen).to(DEV)
+    pts = torch.randn(nb, 200000, dtype=torch.complex64, generator=gen).to(DEV)
     a = T.grid(pts, locs, (64, 64, 64), 4.0)
     T.clear_plan_cache()
     b = T.grid(pts, locs, (64, 64, 64), 4.0)

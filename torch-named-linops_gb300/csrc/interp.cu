@@ -1930,6 +1930,226 @@ __global__ void __launch_bounds__(256) adj_reduce_b3_kernel(Geo g, const int4* _
 }
 
 
+// ------------------------------------ block gridding (3D, 1, 2 or 4 entries)
+//
+// The same work items, counter and staging as adj_b3_kernel, with the block
+// factored the other way: accumulator rows are the 16 (y, z) cells of a block
+// and columns (x, real/imaginary) for each entry, so one 16 x 8 tile per
+// entry holds the whole 4 x 4 x 4 block. A rank-8 update is then
+// A[(y, z), e] = y row * z row (shared by the entries) times
+// B[e, (x, c)] = x row * value: one tensor-core product per entry and group
+// of 8 (point, block) entries, and 8 bytes of values staged per entry instead
+// of 64. D[j] of lane (g8, t4) holds entry j of the cells (x t4, y g8 >> 2,
+// z g8 & 3) (d0, d1) and (x t4, y (g8 >> 2) + 2, z g8 & 3) (d2, d3).
+constexpr int kBSn = 20;  // floats per staged entry: x row 0-3 | y row 4-7 | z row 8-11 | E values 12-19
+                          // (20: the operand loads of a group of 8 entries are free of bank conflicts)
+constexpr int kBnCtas = 4;  // resident CTAs per SM of the persistent grid
+
+template <int E>
+__device__ __forceinline__ void bn_store(const Geo& g, float* __restrict__ gridv, int ncoil, int blk, int g8, int t4,
+                                         const float (&D)[E][4]) {
+  int bx, by, bz;
+  block_origin(g, blk, bx, by, bz);
+  const long long gvol = (long long)g.N[0] * g.N[1] * g.N[2];
+  const int x = bx * 4 + t4, z = bz * 4 + (g8 & 3);
+  if (x >= g.N[0] || z >= g.N[2]) return;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int y = by * 4 + (g8 >> 2) + 2 * h;
+    if (y >= g.N[1]) continue;
+    const long long cell = ((long long)x * g.N[1] + y) * g.N[2] + z;
+#pragma unroll
+    for (int j = 0; j < E; ++j)
+      if (j < ncoil)
+        *reinterpret_cast<float2*>(gridv + ((long long)j * gvol + cell) * 2) = make_float2(D[j][2 * h], D[j][2 * h + 1]);
+  }
+}
+
+template <int E>
+__global__ void __launch_bounds__(256, kBnCtas) adj_bn_kernel(Geo g, const int4* __restrict__ items, int nitems,
+                                                             const uint32_t* __restrict__ bentries,
+                                                             const float* __restrict__ rows,
+                                                             const float2* __restrict__ vals,
+                                                             float* __restrict__ gridv, float* __restrict__ partial,
+                                                             int* __restrict__ ctr) {
+  extern __shared__ __align__(16) float bsm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float* S = bsm + warp * (kBC * kBSn);
+  const int ncoil = (int)min((long long)E, g.nbatch);
+  const int g8 = lane >> 2, t4 = lane & 3;
+  const int last = nitems;
+  auto grab = [&]() {
+    int i = 0;
+    if (lane == 0) i = atomicAdd(ctr, 1);
+    return __shfl_sync(0xffffffffu, i, 0);
+  };
+  int item = grab();
+  if (item >= last) return;
+  int4 itn = items[item];
+  int inext = grab();
+  int4 itnn = inext < last ? items[inext] : make_int4(0, 0, 0, 0);
+  uint32_t enext = lane < min(kBC, itn.z - itn.y) ? bentries[itn.y + lane] : 0u;
+  for (;;) {
+    if (item >= last) return;
+    const int4 it = itn;
+    itn = itnn;
+    item = inext;
+    if (item < last) {
+      inext = grab();
+      itnn = inext < last ? items[inext] : make_int4(0, 0, 0, 0);
+    }
+    float D[E][4];
+#pragma unroll
+    for (int j = 0; j < E; ++j)
+#pragma unroll
+      for (int i = 0; i < 4; ++i) D[j][i] = 0.f;
+    if (it.y == it.z) {  // a run of -it.w empty blocks
+      for (int b = 0; b < -it.w; ++b) bn_store<E>(g, gridv, ncoil, it.x + b, g8, t4, D);
+      if (item < last) enext = lane < min(kBC, itn.z - itn.y) ? bentries[itn.y + lane] : 0u;
+      continue;
+    }
+    for (int c = it.y; c < it.z; c += kBC) {
+      const int n = min(kBC, it.z - c);
+      const int n8 = (n + 7) & ~7;
+      float* sl = S + lane * kBSn;
+      const uint32_t en = enext;
+      if (c + kBC < it.z)
+        enext = lane < min(kBC, it.z - c - kBC) ? bentries[c + kBC + lane] : 0u;
+      else if (item < last)
+        enext = lane < min(kBC, itn.z - itn.y) ? bentries[itn.y + lane] : 0u;
+      if (lane < n) {
+        long long p = en & ((1u << kSelShift) - 1u);
+        if (!TLGB_IN_RANGE(p, g.npts)) p = 0;
+        const float* rsrc = rows + p * row_floats(3);
+        cp_async16(sl + 0, rsrc + 4 * (0 + ((en >> kSelShift) & 1)));
+        cp_async16(sl + 4, rsrc + 4 * (2 + ((en >> (kSelShift + 1)) & 1)));
+        cp_async16(sl + 8, rsrc + 4 * (4 + ((en >> (kSelShift + 2)) & 1)));
+#pragma unroll
+        for (int j = 0; j < E; ++j) {
+          if (j < ncoil)
+            cp_async8(sl + 12 + 2 * j, vals + (long long)j * g.npts + p);
+          else
+            *reinterpret_cast<float2*>(sl + 12 + 2 * j) = make_float2(0.f, 0.f);
+        }
+      } else if (lane < n8) {  // padding entries of the last group: zero weights and values
+        const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        float4* q4 = reinterpret_cast<float4*>(sl);
+        q4[0] = q4[1] = q4[2] = z4;
+#pragma unroll
+        for (int j = 0; j < E; ++j) *reinterpret_cast<float2*>(sl + 12 + 2 * j) = make_float2(0.f, 0.f);
+      }
+      cp_async_wait_all();
+      bool nonfinite = false;
+      if (lane < n) {  // a non-finite value turns the zero product into NaN
+        float chk = 0.f;
+#pragma unroll
+        for (int j = 0; j < 2 * E; ++j) chk = fmaf(sl[12 + j], 0.f, chk);
+        nonfinite = !(chk == 0.f);
+      }
+      const unsigned guarded = __ballot_sync(0xffffffffu, nonfinite);
+      __syncwarp();
+      if (!guarded) {
+        for (int kk = 0; kk < n8; kk += 8) {  // entries kk + t4 and kk + t4 + 4 of this lane's fragments
+          const float* e0 = S + (kk + t4) * kBSn;
+          const float* e1 = e0 + 4 * kBSn;
+          // A: rows g8 and g8 + 8 = (y (g8 >> 2) + 2h, z g8 & 3)
+          const float z0 = e0[8 + (g8 & 3)], z1 = e1[8 + (g8 & 3)];
+          unsigned ah[4], al[4];
+          split_tf32(e0[4 + (g8 >> 2)] * z0, ah[0], al[0]);
+          split_tf32(e0[6 + (g8 >> 2)] * z0, ah[1], al[1]);
+          split_tf32(e1[4 + (g8 >> 2)] * z1, ah[2], al[2]);
+          split_tf32(e1[6 + (g8 >> 2)] * z1, ah[3], al[3]);
+          // B: column g8 = (x g8 >> 1, c g8 & 1) of entry j
+          const float x0 = e0[g8 >> 1], x1 = e1[g8 >> 1];
+#pragma unroll
+          for (int j = 0; j < E; ++j) {
+            unsigned bh0, bl0, bh1, bl1;
+            split_tf32(x0 * e0[12 + 2 * j + (g8 & 1)], bh0, bl0);
+            split_tf32(x1 * e1[12 + 2 * j + (g8 & 1)], bh1, bl1);
+            mma_tf32(D[j], ah, bh0, bh1);
+            mma_tf32(D[j], ah, bl0, bl1);
+            mma_tf32(D[j], al, bh0, bh1);
+          }
+        }
+      } else {
+        // entry by entry on the CUDA cores, in order; a non-finite entry only
+        // reaches the cells of its window (weights with a clear sign bit)
+        for (int q = 0; q < n; ++q) {
+          const float* e = S + q * kBSn;
+          const bool nf = (guarded >> q) & 1u;
+          const float wx = e[t4], z = e[8 + (g8 & 3)];
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const float y = e[4 + (g8 >> 2) + 2 * h];
+            const float w = wx * (y * z);
+            const bool ok = !nf || (!signbit(wx) && !signbit(y) && !signbit(z));
+#pragma unroll
+            for (int j = 0; j < E; ++j) {
+              const float2 v = *reinterpret_cast<const float2*>(e + 12 + 2 * j);
+              if (ok) {
+                D[j][2 * h] = fmaf(w, v.x, D[j][2 * h]);
+                D[j][2 * h + 1] = fmaf(w, v.y, D[j][2 * h + 1]);
+              }
+            }
+          }
+        }
+      }
+      __syncwarp();  // the chunk has been read before the next one is staged
+    }
+    if (it.w >= 0) {  // a part of a split block: its slot of the partial blocks, [cell][entry] complex
+      float* dst = partial + (long long)it.w * 64 * 2 * E;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int cell = cell_index<3>(t4, (g8 >> 2) + 2 * h, g8 & 3);
+#pragma unroll
+        for (int j = 0; j < E; ++j)
+          *reinterpret_cast<float2*>(dst + (cell * E + j) * 2) = make_float2(D[j][2 * h], D[j][2 * h + 1]);
+      }
+    } else {
+      bn_store<E>(g, gridv, ncoil, it.x, g8, t4, D);
+    }
+  }
+}
+
+// Sum the partial blocks of one split block of adj_bn_kernel in slot order,
+// compensated: thread (cell, entry) sums one complex value of every part,
+// eight in flight.
+template <int E>
+__global__ void __launch_bounds__(64 * E) adj_reduce_bn_kernel(Geo g, const int4* __restrict__ split,
+                                                              const float* __restrict__ partial,
+                                                              float* __restrict__ gridv) {
+  const int4 sp = split[blockIdx.x];
+  const int t = threadIdx.x, cell = t / E, j = t % E;
+  const int ncoil = (int)min((long long)E, g.nbatch);
+  const float2* src = reinterpret_cast<const float2*>(partial) + (long long)sp.y * 64 * E + t;
+  const long long step = 64 * E;
+  float2 sum = make_float2(0.f, 0.f), comp = sum;
+  int k = 0;
+  for (; k + 8 <= sp.z; k += 8) {
+    float2 v[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = __ldg(src + (k + i) * step);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      comp_add(sum.x, comp.x, v[i].x);
+      comp_add(sum.y, comp.y, v[i].y);
+    }
+  }
+  for (; k < sp.z; ++k) {
+    const float2 v = __ldg(src + k * step);
+    comp_add(sum.x, comp.x, v.x);
+    comp_add(sum.y, comp.y, v.y);
+  }
+  if (j >= ncoil) return;
+  int bx, by, bz;
+  block_origin(g, sp.x, bx, by, bz);
+  const int x = bx * 4 + (cell >> 4), y = by * 4 + ((cell >> 2) & 3), z = bz * 4 + (cell & 3);
+  if (x >= g.N[0] || y >= g.N[1] || z >= g.N[2]) return;
+  const long long gvol = (long long)g.N[0] * g.N[1] * g.N[2];
+  *reinterpret_cast<float2*>(gridv + ((long long)j * gvol + ((long long)x * g.N[1] + y) * g.N[2] + z) * 2) =
+      make_float2(sum.x + comp.x, sum.y + comp.y);
+}
+
 // 2D gridding. The view of one dimension of a record from a 16-wide tile at o
 // (grid N): f | m << 4 | k0 << 7, as tile_view (f first local position, m
 // taps inside the tile, k0 the first of them in the record). fast is
@@ -3524,9 +3744,17 @@ namespace {
 bool fast3(const Geo& g, int cg);
 bool fast2(const Geo& g, int cg);
 
-// bytes of the block path's partial blocks: 4 KB per part and group of 8 entries
-size_t blk_partial_bytes(const tlgb_interp_plan_info* info, int64_t ncg) {
-  return align_up((size_t)info->n_blk_partials * ncg * 64 * 16 * sizeof(float), 256);
+// Batch entries per group of the block gridding: 1, 2 or 4 for 3D batches of
+// at most 4 entries (adj_bn_kernel), else 8 (adj_b3_kernel).
+int blk_entries(const Geo& g) {
+  if (g.ndim != 3 || g.nbatch > 4) return 8;
+  return g.nbatch <= 1 ? 1 : (g.nbatch <= 2 ? 2 : 4);
+}
+
+// bytes of the block path's partial blocks: 64 cells x E complex entries per
+// part and group
+size_t blk_partial_bytes(const tlgb_interp_plan_info* info, int64_t ncg, int E) {
+  return align_up((size_t)info->n_blk_partials * ncg * 64 * 2 * E * sizeof(float), 256);
 }
 
 // Gridding scratch: the partial tiles of split tiles (block path: the partial
@@ -3535,10 +3763,13 @@ size_t blk_partial_bytes(const tlgb_interp_plan_info* info, int64_t ncg) {
 void adj_scratch_parts(const Geo& g, const tlgb_interp_plan_info* info, size_t& partial_bytes, size_t& tv_bytes) {
   const int cg = adj_cg(g);
   const int64_t ncg = cdiv(std::max<long long>(g.nbatch, 1), cg);
-  partial_bytes = (fast3(g, cg) || fast2(g, cg)) && info->n_blk_items > 0
-                      ? blk_partial_bytes(info, ncg) + align_up((size_t)ncg * sizeof(int), 256)
-                      : align_up((size_t)info->n_partials * ncg * tile_floats(g, cg) * sizeof(float), 256);
-  tv_bytes = ((fast3(g, cg) || fast2(g, cg)) && info->off_records > 0) ? (size_t)ncg * g.npts * 8 * 8 : 0;
+  const bool blocks = (fast3(g, cg) || fast2(g, cg)) && info->n_blk_items > 0;
+  partial_bytes = blocks ? blk_partial_bytes(info, ncg, blk_entries(g)) + align_up((size_t)ncg * sizeof(int), 256)
+                         : align_up((size_t)info->n_partials * ncg * tile_floats(g, cg) * sizeof(float), 256);
+  // adj_bn_kernel reads the values in place
+  tv_bytes = ((fast3(g, cg) || fast2(g, cg)) && info->off_records > 0 && !(blocks && blk_entries(g) < 8))
+                 ? (size_t)ncg * g.npts * 8 * 8
+                 : 0;
 }
 }  // namespace
 }  // namespace tlgb
@@ -3695,9 +3926,41 @@ int launch_adj_f3(const Geo& g, const tlgb_interp_plan_info* info, const char* P
   return TLGB_OK;
 }
 
+template <int E>
+int launch_adj_bn(const Geo& g, const tlgb_interp_plan_info* info, const char* P, const void* vals, void* grid,
+                  void* scratch, cudaStream_t s) {
+  const size_t sm = 8 * kBC * kBSn * sizeof(float);
+  TLGB_TRY(set_smem(adj_bn_kernel<E>, sm));
+  if (((uintptr_t)P & 15) || ((uintptr_t)scratch & 15))
+    TLGB_FAIL(TLGB_ERR_INVALID, "interp adjoint: plan and scratch must be 16-byte aligned");
+  if ((uintptr_t)vals & 7) TLGB_FAIL(TLGB_ERR_INVALID, "interp adjoint: values must be 8-byte aligned");
+  // the work counter follows the partial blocks
+  int* ctr = reinterpret_cast<int*>(static_cast<char*>(scratch) + blk_partial_bytes(info, 1, E));
+  TLGB_CUDA(cudaMemsetAsync(ctr, 0, sizeof(int), s));
+  const int64_t nctas = std::min<int64_t>(cdiv(info->n_blk_items, 8), (int64_t)kBnCtas * sm_count());
+  adj_bn_kernel<E><<<(unsigned)std::max<int64_t>(nctas, 1), 256, sm, s>>>(
+      g, (const int4*)(P + info->off_blk_items), (int)info->n_blk_items, (const uint32_t*)(P + info->off_blk_entries),
+      (const float*)(P + info->off_blk_rows), (const float2*)vals, (float*)grid, (float*)scratch, ctr);
+  TLGB_CHECK_LAUNCH();
+  if (info->n_blk_split > 0) {
+    adj_reduce_bn_kernel<E><<<(unsigned)info->n_blk_split, 64 * E, 0, s>>>(g, (const int4*)(P + info->off_blk_split),
+                                                                          (const float*)scratch, (float*)grid);
+    TLGB_CHECK_LAUNCH();
+  }
+  return TLGB_OK;
+}
+
 template <int NDIM>
 int launch_adj_b3(const Geo& g, const tlgb_interp_plan_info* info, const char* P, const float* locs,
                   const void* vals, void* grid, void* scratch, cudaStream_t s) {
+  if constexpr (NDIM == 3) {
+    switch (blk_entries(g)) {
+      case 1: return launch_adj_bn<1>(g, info, P, vals, grid, scratch, s);
+      case 2: return launch_adj_bn<2>(g, info, P, vals, grid, scratch, s);
+      case 4: return launch_adj_bn<4>(g, info, P, vals, grid, scratch, s);
+      default: break;
+    }
+  }
   const int64_t ncg = cdiv(g.nbatch, 8);
   const size_t sm = 8 * kBC * kBS * sizeof(float);
   TLGB_TRY(set_smem(adj_b3_kernel<NDIM>, sm));
@@ -3706,7 +3969,7 @@ int launch_adj_b3(const Geo& g, const tlgb_interp_plan_info* info, const char* P
     TLGB_FAIL(TLGB_ERR_INVALID, "interp adjoint: plan and scratch must be 16-byte aligned");
   if ((uintptr_t)vals & 7) TLGB_FAIL(TLGB_ERR_INVALID, "interp adjoint: values must be 8-byte aligned");
   // the work counters (one per group of 8 entries) follow the partial blocks
-  int* ctr = reinterpret_cast<int*>(static_cast<char*>(scratch) + blk_partial_bytes(info, ncg));
+  int* ctr = reinterpret_cast<int*>(static_cast<char*>(scratch) + blk_partial_bytes(info, ncg, 8));
   const float4* tv = nullptr;
   if (g.tv_off >= 0 && g.npts > 0) {
     float2* t = reinterpret_cast<float2*>(static_cast<char*>(scratch) + g.tv_off);
