@@ -2412,21 +2412,28 @@ __global__ void __launch_bounds__(256, 4) adj_f2_kernel(Geo g, const int4* __res
   }
 }
 
-// Gather: CTA = 8 warps sharing one 12^3 x 8-entry region ([entry][x][y][z],
-// loaded by one TMA bulk tensor copy when the region needs no wrap), two CTAs
-// per SM. Each warp takes every 8th point of the item, building the records
-// of its next 8 points itself (kGB = 8 warps x 8 slots). Lanes = (entry,
-// z-tap): a lane sums its entry's 4 y-taps x 4 x-taps, two points at a time,
-// then the 4 z-tap lanes of each entry add up.
+// Gather: CTA = 8 warps sharing one 12^3 x CG-entry region ([entry][x][y][z],
+// loaded by one TMA bulk tensor copy when the region needs no wrap). Each warp
+// takes every 8th point of the item, building the records of its next 8
+// points itself (kGB = 8 warps x 8 slots). Lanes = (point, entry, z-tap): a
+// lane sums its entry's 4 y-taps x 4 x-taps, then the 4 z-tap lanes add up.
+// CG = 8 (two CTAs per SM): one point per step across the lanes, two steps
+// interleaved. CG = 1, 2 or 4 (batches of at most 4 entries, 4 CTAs per SM):
+// 8 / CG points per step, so a one-entry batch stages and reads an eighth
+// of the region.
 constexpr int kGB = 64;
 
-__global__ void __launch_bounds__(256, 2) fwd_f3_kernel(const __grid_constant__ CUtensorMap tmap, int use_tma, Geo g,
-                                                        const int4* __restrict__ items,
-                                                        const int32_t* __restrict__ entries,
-                                                        const PRec* __restrict__ precs,
-                                                        const float* __restrict__ locs,
-                                                        const float* __restrict__ gridv, float* __restrict__ out) {
-  constexpr int CG = 8, S = 12, PLANE = S * S, VOL = S * S * S, NW = 8;
+template <int CG>
+__global__ void __launch_bounds__(256, CG == 8 ? 2 : 4) fwd_f3_kernel(const __grid_constant__ CUtensorMap tmap,
+                                                                      int use_tma, Geo g,
+                                                                      const int4* __restrict__ items,
+                                                                      const int32_t* __restrict__ entries,
+                                                                      const PRec* __restrict__ precs,
+                                                                      const float* __restrict__ locs,
+                                                                      const float* __restrict__ gridv,
+                                                                      float* __restrict__ out) {
+  constexpr int S = 12, PLANE = S * S, VOL = S * S * S, NW = 8;
+  constexpr int PPW = 8 / CG;  // points per warp step
   constexpr uint32_t RBYTES = VOL * CG * 8;
   extern __shared__ __align__(128) unsigned char smem[];
   float2* reg = reinterpret_cast<float2*>(smem);               // [8][12][12][12]
@@ -2482,14 +2489,15 @@ __global__ void __launch_bounds__(256, 2) fwd_f3_kernel(const __grid_constant__ 
                     : make_float2(0.f, 0.f);
     }
   }
-  // lane = (entry c, z tap kz). Iteration t reads y tap (t + c) & 3: the 8
-  // entries' regions are 13,824 B apart (the same banks), so rotating the y
-  // taps by entry spreads one load instruction over 4 bank windows.
-  const int c = lane >> 2, kz = lane & 3;
+  // lane = (point q, entry c, z tap kz). Iteration t reads y tap (t + lane /
+  // 4) & 3: the 8 entries' regions are 13,824 B apart (the same banks), so
+  // rotating the y taps by lane group spreads one load instruction over 4
+  // bank windows.
+  const int q = lane / (4 * CG), c = (lane >> 2) % CG, kz = lane & 3;
   int kyo[4], rowoff[4];
 #pragma unroll
   for (int t = 0; t < 4; ++t) {
-    kyo[t] = (t + c) & 3;
+    kyo[t] = (t + (lane >> 2)) & 3;
     rowoff[t] = kyo[t] * S;
   }
   // Each warp takes the item's points warp, warp + 8, ... in mini-batches of
@@ -2564,7 +2572,8 @@ __global__ void __launch_bounds__(256, 2) fwd_f3_kernel(const __grid_constant__ 
       }
       return acc;
     };
-    // the generic record path (exact-integer coordinates)
+    // the generic record path (exact-integer coordinates); with CG < 8 only
+    // the lanes of point group 0 sum (warp-uniform call)
     auto gather_rec = [&](const R3& R) {
       if (lane == 0) {
         float x3[3];
@@ -2574,6 +2583,7 @@ __global__ void __launch_bounds__(256, 2) fwd_f3_kernel(const __grid_constant__ 
       __syncwarp();
       const Rec<5>& Sr = slow[warp];
       float2 acc = make_float2(0.f, 0.f);
+      if (q == 0)
       for (int kzz = kz; kzz < Sr.m[2]; kzz += 4)
         for (int kyy = 0; kyy < Sr.m[1]; ++kyy)
           for (int kx = 0; kx < Sr.m[0]; ++kx) {
@@ -2586,18 +2596,19 @@ __global__ void __launch_bounds__(256, 2) fwd_f3_kernel(const __grid_constant__ 
       return acc;
     };
     // sum over the 4 z-tap lanes of each entry, then lane kz = 0 stores
-    auto finish = [&](float2 acc, int p) {
+    auto finish = [&](float2 acc, int p, bool store) {
       acc.x += __shfl_xor_sync(0xffffffffu, acc.x, 1);
       acc.y += __shfl_xor_sync(0xffffffffu, acc.y, 1);
       acc.x += __shfl_xor_sync(0xffffffffu, acc.x, 2);
       acc.y += __shfl_xor_sync(0xffffffffu, acc.y, 2);
-      if (kz == 0 && c0 + c < g.nbatch && TLGB_IN_RANGE(p, g.npts))
+      if (store && kz == 0 && c0 + c < g.nbatch && TLGB_IN_RANGE(p, g.npts))
         *reinterpret_cast<float2*>(out + ((long long)(c0 + c) * g.npts + p) * 2) = acc;
     };
     auto one = [&](const R3& R) {
       const unsigned view = R.view;
       if (!((view >> 21) & 1)) return;  // no valid tap (warp-uniform)
-      finish((view >> 20) & 1 ? gather_box(R) : gather_rec(R), R.p);
+      const bool box = (view >> 20) & 1;
+      finish(box ? gather_box(R) : gather_rec(R), R.p, box || q == 0);
     };
     for (int base = warp; base < npt; base += 8 * NW) {
       if (base != warp) {
@@ -2605,21 +2616,38 @@ __global__ void __launch_bounds__(256, 2) fwd_f3_kernel(const __grid_constant__ 
         build_records(base);
       }
       const int nb = min(8, (npt - base + NW - 1) / NW);
-      int i = 0;
-      for (; i + 1 < nb; i += 2) {
-        const R3& R0 = wrec[i];
-        const R3& R1 = wrec[i + 1];
-        if ((R0.view & R1.view) >> 20 & 1) {
-          // both on the plain-run path (which implies a valid tap): interleaved
-          const float2 a0 = gather_box(R0), a1 = gather_box(R1);
-          finish(a0, R0.p);
-          finish(a1, R1.p);
-        } else {
-          one(R0);
-          one(R1);
+      if constexpr (CG == 8) {
+        int i = 0;
+        for (; i + 1 < nb; i += 2) {
+          const R3& R0 = wrec[i];
+          const R3& R1 = wrec[i + 1];
+          if ((R0.view & R1.view) >> 20 & 1) {
+            // both on the plain-run path (which implies a valid tap): interleaved
+            const float2 a0 = gather_box(R0), a1 = gather_box(R1);
+            finish(a0, R0.p, true);
+            finish(a1, R1.p, true);
+          } else {
+            one(R0);
+            one(R1);
+          }
+        }
+        if (i < nb) one(wrec[i]);
+      } else {
+        for (int i0 = 0; i0 < nb; i0 += PPW) {
+          // the plain-run points of this step, one per lane group
+          const int i = i0 + q;
+          const R3& R = wrec[i < nb ? i : i0];
+          const bool box = i < nb && ((R.view >> 20) & 1);
+          finish(box ? gather_box(R) : make_float2(0.f, 0.f), R.p, box);
+          // then the step's points with a valid tap off that path, one at a
+          // time by the whole warp
+#pragma unroll 1
+          for (int k = 0; k < PPW && i0 + k < nb; ++k) {
+            const unsigned v = wrec[i0 + k].view;
+            if (((v >> 21) & 1) && !((v >> 20) & 1)) finish(gather_rec(wrec[i0 + k]), wrec[i0 + k].p, q == 0);
+          }
         }
       }
-      if (i < nb) one(wrec[i]);
     }
   }
 }
@@ -3830,11 +3858,12 @@ int launch_adj_t2(const Geo& g, int cg, const tlgb_interp_plan_info* info, const
 
 using sm100::tensor_map_encoder;
 
-int launch_fwd_f3(const Geo& g, const tlgb_interp_plan_info* info, const char* P, const float* locs,
-                  const void* grid, void* out, cudaStream_t s) {
-  const int64_t ncg = cdiv(g.nbatch, 8);
-  const size_t sm = 12 * 12 * 12 * 8 * 8 + kGB * sizeof(R3) + 8 * sizeof(Rec<5>) + 8;
-  // 4D tensor map over [batch][X][Y][Z] complex64 (8-byte elements), box 12^3 x 8
+template <int CG>
+int launch_fwd_f3_t(const Geo& g, const tlgb_interp_plan_info* info, const char* P, const float* locs,
+                    const void* grid, void* out, cudaStream_t s) {
+  const int64_t ncg = cdiv(g.nbatch, CG);
+  const size_t sm = 12 * 12 * 12 * CG * 8 + kGB * sizeof(R3) + 8 * sizeof(Rec<5>) + 8;
+  // 4D tensor map over [batch][X][Y][Z] complex64 (8-byte elements), box 12^3 x CG
   CUtensorMap tmap;
   memset(&tmap, 0, sizeof(tmap));
   int use_tma = 0;
@@ -3843,20 +3872,29 @@ int launch_fwd_f3(const Geo& g, const tlgb_interp_plan_info* info, const char* P
   if (enc && (zb % 16) == 0 && ((uintptr_t)grid % 16) == 0) {
     const cuuint64_t dims[4] = {(cuuint64_t)g.N[2], (cuuint64_t)g.N[1], (cuuint64_t)g.N[0], (cuuint64_t)g.nbatch};
     const cuuint64_t strides[3] = {zb, zb * g.N[1], zb * g.N[1] * g.N[0]};
-    const cuuint32_t box[4] = {12, 12, 12, 8};
+    const cuuint32_t box[4] = {12, 12, 12, (cuuint32_t)CG};
     const cuuint32_t estr[4] = {1, 1, 1, 1};
     const CUresult r = enc(&tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4, const_cast<void*>(grid), dims, strides, box, estr,
                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     use_tma = (r == CUDA_SUCCESS) ? 1 : 0;
   }
-  TLGB_TRY(set_smem(fwd_f3_kernel, sm));
+  TLGB_TRY(set_smem(fwd_f3_kernel<CG>, sm));
   dim3 grd((unsigned)info->n_fwd_items, (unsigned)ncg);
-  fwd_f3_kernel<<<grd, 256, sm, s>>>(tmap, use_tma, g, (const int4*)(P + info->off_fwd_items),
-                                     (const int32_t*)(P + info->off_entries), (const PRec*)(P + info->off_records), locs,
-                                     (const float*)grid, (float*)out);
+  fwd_f3_kernel<CG><<<grd, 256, sm, s>>>(tmap, use_tma, g, (const int4*)(P + info->off_fwd_items),
+                                         (const int32_t*)(P + info->off_entries), (const PRec*)(P + info->off_records),
+                                         locs, (const float*)grid, (float*)out);
   TLGB_CHECK_LAUNCH();
   return TLGB_OK;
+}
+
+// batches of at most 4 entries stage only their own entries' regions
+int launch_fwd_f3(const Geo& g, const tlgb_interp_plan_info* info, const char* P, const float* locs,
+                  const void* grid, void* out, cudaStream_t s) {
+  if (g.nbatch <= 1) return launch_fwd_f3_t<1>(g, info, P, locs, grid, out, s);
+  if (g.nbatch <= 2) return launch_fwd_f3_t<2>(g, info, P, locs, grid, out, s);
+  if (g.nbatch <= 4) return launch_fwd_f3_t<4>(g, info, P, locs, grid, out, s);
+  return launch_fwd_f3_t<8>(g, info, P, locs, grid, out, s);
 }
 
 bool fast2(const Geo& g, int cg) {
