@@ -117,9 +117,10 @@ typedef struct tlgb_interp_plan_info {
   int64_t n_home;         /* points with at least one valid tap (home pairs) */
   int64_t off_records;    /* byte offset of the per-point tap records, 0 = none */
   int64_t kernel_key;     /* kernel, norm and beta the records were built for */
-  /* Block lists of the 3D 8-entry gridding (0 when the plan has none): the
-   * (point, block) pairs of 4x4x4-cell output blocks, sorted stably by block,
-   * and their work items (dense blocks are split into parts summed after). */
+  /* Block lists of the 2D/3D gridding of complex batches (0 when the plan has
+   * none): the (point, block) pairs of 4x4x4-cell (3D) or 8x8-cell (2D) output
+   * blocks, sorted stably by block, and their work items (dense blocks are
+   * split into parts summed after). */
   int64_t n_blk_entries;
   int64_t n_blk_items;
   int64_t n_blk_partials; /* partial blocks of split (dense) blocks */
@@ -141,10 +142,13 @@ int tlgb_interp_plan_size(const tlgb_interp_desc* d, size_t* plan_bytes, size_t*
 int tlgb_interp_plan_build(const tlgb_interp_desc* d, const float* locs, void* plan, size_t plan_bytes,
                            void* tmp, size_t tmp_bytes, tlgb_interp_plan_info* info, tlgb_stream_t stream);
 
-/* Scratch bytes tlgb_interp_adjoint needs for this plan: the partial tiles of
- * split output tiles and, for 3D gridding of 8-entry groups, a point-major
- * copy of the point values (64 bytes per point and group of 8 entries), so
- * that each (point, tile) pair reads its values in one contiguous run. */
+/* Scratch bytes tlgb_interp_adjoint needs for this plan: the partial tiles
+ * (or blocks) of split output tiles, on the block-list path a work counter per
+ * group of 8 entries, and for the 8-entry 2D/3D gridding kernels a
+ * point-major copy of the point values (64 bytes per point and group of 8
+ * entries), so that each (point, block) pair reads its values in one
+ * contiguous run. 3D block-list gridding of at most 4 entries reads the values
+ * in place and needs no copy. The scratch needs no initial contents. */
 int tlgb_interp_adjoint_scratch_size(const tlgb_interp_desc* d, const tlgb_interp_plan_info* info,
                                      size_t* bytes);
 
