@@ -1,8 +1,8 @@
 """The plan's bin permutation, bit-exact against the CPU oracle
 (oracle/binning.py): every (point, tile) pair, ordered by tile, home pairs
-first, then by point index; and in 3D the (point, 4^3 block) lists of the
-gridding, ordered by block, then by point index. Sizes large enough for the
-multi-CTA scans."""
+first, then by point index; and in 2D and 3D the (point, block) lists of the
+gridding, ordered by block, then by point index, with their work items and
+split blocks. Sizes large enough for the multi-CTA scans."""
 
 import numpy as np
 import pytest
@@ -55,6 +55,7 @@ def test_block_lists_are_bit_exact(grid_size, npts, pad):
     locs = torch.rand(npts, nd, generator=gen) * (n + 6) - 3
     locs[:500] = torch.randint(0, 30, (500, nd), generator=gen).float()  # exact integers: 5 taps
     locs[500:520, 1] = float("inf")
+    locs[520:6520] = 10 + 2 * torch.rand(6000, nd, generator=gen)  # dense blocks, split into parts
     keys, pts = OB.block_pairs(locs, grid_size, 4.0, "kaiser_bessel", pad)
     plan = interp.get_plan(locs.to(DEV), grid_size, 4.0, "kaiser_bessel", pad, 6.99666)
     info = plan.info
@@ -72,6 +73,18 @@ def test_block_lists_are_bit_exact(grid_size, npts, pad):
         assert np.all(keys[s0:s1] == b)
         cover[s0:s1] += 1
     assert np.all(cover == 1)
+    # split blocks: listed by falling part count; their partial slots are the
+    # parts' slots, each used once
+    nsp = int(info.n_blk_split)
+    if nsp > 0:
+        off_sp = int(info.off_blk_split)
+        sp = plan.buffer[off_sp:off_sp + 16 * nsp].view(torch.int32).reshape(-1, 4).cpu().numpy()
+        assert np.all(np.diff(sp[:, 2]) <= 0)
+        slots = np.concatenate([np.arange(a, a + c) for a, c in zip(sp[:, 1], sp[:, 2])])
+        assert np.array_equal(np.sort(slots), np.arange(int(info.n_blk_partials)))
+        parts = items[items[:, 3] >= 0]
+        assert np.array_equal(np.sort(parts[:, 3]), np.arange(int(info.n_blk_partials)))
+    assert nsp > 0
     # empty runs and non-empty items together name every block once
     nb = int(np.prod([-(-s // (4 if nd == 3 else 8)) for s in grid_size]))
     named = np.zeros(nb, dtype=np.int64)
