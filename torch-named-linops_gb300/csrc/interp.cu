@@ -2112,33 +2112,53 @@ __global__ void __launch_bounds__(256, kBnCtas) adj_bn_kernel(Geo g, const int4*
 }
 
 // Sum the partial blocks of one split block of adj_bn_kernel in slot order,
-// compensated: thread (cell, entry) sums one complex value of every part,
-// eight in flight.
+// compensated. CTA = 256 threads: thread (range r, cell, entry) sums one
+// complex value of every part of the r-th of 256 / (64 E) consecutive part
+// ranges, eight in flight; then the ranges are added in order. With one or
+// two entries the ranges cut the longest chain (the densest block has a few
+// hundred parts) by 4 or 2.
 template <int E>
-__global__ void __launch_bounds__(64 * E) adj_reduce_bn_kernel(Geo g, const int4* __restrict__ split,
-                                                              const float* __restrict__ partial,
-                                                              float* __restrict__ gridv) {
+__global__ void __launch_bounds__(256) adj_reduce_bn_kernel(Geo g, const int4* __restrict__ split,
+                                                           const float* __restrict__ partial,
+                                                           float* __restrict__ gridv) {
+  constexpr int U = 64 * E, R = 256 / U;  // values per part, part ranges
+  __shared__ float2 rs[R > 1 ? R - 1 : 1][U], rc[R > 1 ? R - 1 : 1][U];
   const int4 sp = split[blockIdx.x];
-  const int t = threadIdx.x, cell = t / E, j = t % E;
+  const int r = threadIdx.x / U, t = threadIdx.x % U, cell = t / E, j = t % E;
   const int ncoil = (int)min((long long)E, g.nbatch);
-  const float2* src = reinterpret_cast<const float2*>(partial) + (long long)sp.y * 64 * E + t;
-  const long long step = 64 * E;
+  const float2* src = reinterpret_cast<const float2*>(partial) + (long long)sp.y * U + t;
+  const int k0 = (int)((long long)sp.z * r / R), k1 = (int)((long long)sp.z * (r + 1) / R);
   float2 sum = make_float2(0.f, 0.f), comp = sum;
-  int k = 0;
-  for (; k + 8 <= sp.z; k += 8) {
+  int k = k0;
+  for (; k + 8 <= k1; k += 8) {
     float2 v[8];
 #pragma unroll
-    for (int i = 0; i < 8; ++i) v[i] = __ldg(src + (k + i) * step);
+    for (int i = 0; i < 8; ++i) v[i] = __ldg(src + (long long)(k + i) * U);
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
       comp_add(sum.x, comp.x, v[i].x);
       comp_add(sum.y, comp.y, v[i].y);
     }
   }
-  for (; k < sp.z; ++k) {
-    const float2 v = __ldg(src + k * step);
+  for (; k < k1; ++k) {
+    const float2 v = __ldg(src + (long long)k * U);
     comp_add(sum.x, comp.x, v.x);
     comp_add(sum.y, comp.y, v.y);
+  }
+  if constexpr (R > 1) {
+    if (r > 0) {
+      rs[r - 1][t] = sum;
+      rc[r - 1][t] = comp;
+    }
+    __syncthreads();
+    if (r > 0) return;
+#pragma unroll
+    for (int i = 0; i < R - 1; ++i) {  // the later ranges in order, their compensations with them
+      const float2 s2 = rs[i][t], c2 = rc[i][t];
+      comp_add(sum.x, comp.x, s2.x);
+      comp_add(sum.y, comp.y, s2.y);
+      comp.x += c2.x, comp.y += c2.y;
+    }
   }
   if (j >= ncoil) return;
   int bx, by, bz;
@@ -3981,8 +4001,8 @@ int launch_adj_bn(const Geo& g, const tlgb_interp_plan_info* info, const char* P
       (const float*)(P + info->off_blk_rows), (const float2*)vals, (float*)grid, (float*)scratch, ctr);
   TLGB_CHECK_LAUNCH();
   if (info->n_blk_split > 0) {
-    adj_reduce_bn_kernel<E><<<(unsigned)info->n_blk_split, 64 * E, 0, s>>>(g, (const int4*)(P + info->off_blk_split),
-                                                                          (const float*)scratch, (float*)grid);
+    adj_reduce_bn_kernel<E><<<(unsigned)info->n_blk_split, 256, 0, s>>>(g, (const int4*)(P + info->off_blk_split),
+                                                                       (const float*)scratch, (float*)grid);
     TLGB_CHECK_LAUNCH();
   }
   return TLGB_OK;
