@@ -1,6 +1,7 @@
 """Checks that need no GPU: the C-ABI library loads, exports every symbol
 that include/tlgb.h declares with the declared parameters, and validates
-descriptors and launch sizes on the host; the Python layer's host-side logic
+descriptors and launch sizes and sizes the gridding scratch on the host; the
+Python layer's host-side logic
 (location rescaling with the reference's rounding, batch ranges, the
 Toeplitz normal's inner operators) runs as the reference's does."""
 
@@ -299,3 +300,26 @@ def test_cached_plans_order_other_streams_after_their_build(monkeypatch):
     # the torch calls the method makes
     assert all(hasattr(torch.cuda.Stream, m) for m in ("wait_event", "cuda_stream"))
     assert hasattr(torch.Tensor, "record_stream") and hasattr(torch.cuda.Event, "record")
+
+
+@pytest.mark.parametrize("ndim,nbatch,entries,ncg,values_copy", [
+    (3, 8, 8, 1, True), (3, 11, 8, 2, True), (3, 1, 1, 1, False), (3, 2, 2, 1, False), (3, 3, 4, 1, False),
+    (3, 4, 4, 1, False), (3, 5, 8, 1, True), (2, 1, 8, 1, True), (2, 8, 8, 1, True)])
+def test_adjoint_scratch_layout_of_the_block_path(ndim, nbatch, entries, ncg, values_copy):
+    """Gridding scratch on the block-list path (host arithmetic only): the
+    split blocks' parts (64 cells x E complex entries each, E = 1, 2 or 4 for
+    3D batches of at most 4 entries, else 8 per group), one work counter per
+    group of 8 entries, and the point-major value copy (64 bytes per point and
+    group) only for the 8-entry kernels."""
+    def up(x):
+        return (x + 255) // 256 * 256
+
+    npts, parts = 1000, 10
+    d = _desc(ndim=ndim, nbatch=nbatch, npts=npts)
+    d.is_complex = 1
+    info = _ext.PlanInfo()
+    info.n_blk_items, info.n_blk_partials, info.off_records = 50, parts, 4096
+    sb = ctypes.c_size_t(0)
+    assert _ext.lib().tlgb_interp_adjoint_scratch_size(ctypes.byref(d), ctypes.byref(info), ctypes.byref(sb)) == 0
+    want = up(parts * ncg * 64 * 2 * entries * 4) + up(ncg * 4) + (ncg * npts * 64 if values_copy else 0)
+    assert sb.value == want
