@@ -59,6 +59,26 @@ def test_block_list_invariants():
     assert np.array_equal(np.unique(pts), np.unique(pt))
 
 
+@pytest.mark.parametrize("pad", ["circular", "zero"])
+def test_block_list_invariants_2d(pad):
+    """2D blocks of 8 x 8 cells: a W = 4 window (5 taps at exact integers)
+    meets at most 2 blocks per axis, so at most 4 per point, 1.9 on average
+    for uniform points; the leading internal dim has one block (selector bit
+    0 clear); every point with a valid tap has at least one block."""
+    gen = torch.Generator().manual_seed(3)
+    locs = torch.rand(4000, 2, generator=gen) * 70 - 3
+    locs[:200] = torch.randint(0, 64, (200, 2), generator=gen).float()
+    keys, ent = OB.block_pairs(locs, (64, 64), 4.0, pad_mode=pad)
+    pts, sel = ent & ((1 << 29) - 1), ent >> 29
+    assert np.all(np.diff(keys) >= 0)
+    same = np.diff(keys) == 0
+    assert np.all(np.diff(pts)[same] > 0)
+    assert np.bincount(pts).max() <= 4 and np.all(sel & 1 == 0) and sel.max() <= 6
+    assert keys.max() < 64 and 1.5 < len(keys) / len(np.unique(pts)) < 2.4
+    kt, pt = OB.plan_pairs(locs, (64, 64), 4.0, pad_mode=pad)
+    assert np.array_equal(np.unique(pts), np.unique(pt))
+
+
 @pytest.mark.parametrize("shape", [(37,), (19, 23), (9, 10, 11)])
 @pytest.mark.parametrize("kernel,norm", [("kaiser_bessel", 1), ("spline", 1), ("kaiser_bessel", 2)])
 @pytest.mark.parametrize("pad", ["circular", "zero"])
