@@ -1937,9 +1937,9 @@ __global__ void __launch_bounds__(256) adj_reduce_b3_kernel(Geo g, const int4* _
 // and columns (x, real/imaginary) for each entry, so one 16 x 8 tile per
 // entry holds the whole 4 x 4 x 4 block. A rank-8 update is then
 // A[(y, z), e] = y row * z row (shared by the entries) times
-// B[e, (x, c)] = x row * value: one tensor-core product per entry and group
-// of 8 (point, block) entries, and 8 bytes of values staged per entry instead
-// of 64. D[j] of lane (g8, t4) holds entry j of the cells (x t4, y g8 >> 2,
+// B[e, (x, c)] = x row * value: one m16n8k8 product (three with the tf32
+// split) per batch entry and group of 8 (point, block) entries, and 8 bytes
+// of values staged per batch entry instead of a 64-byte row of 8. D[j] of lane (g8, t4) holds entry j of the cells (x t4, y g8 >> 2,
 // z g8 & 3) (d0, d1) and (x t4, y (g8 >> 2) + 2, z g8 & 3) (d2, d3).
 constexpr int kBSn = 20;  // floats per staged entry: x row 0-3 | y row 4-7 | z row 8-11 | E values 12-19
                           // (20: the operand loads of a group of 8 entries are free of bank conflicts)
