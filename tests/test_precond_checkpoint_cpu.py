@@ -6,6 +6,7 @@ import os
 import pytest
 import torch
 
+from torchlinops_gb300 import mri
 from torchlinops_gb300 import precond as P
 
 
@@ -57,3 +58,28 @@ def test_checkpoint_of_another_run_is_refused(tmp_path):
     torch.save(ck, path)
     with pytest.raises(ValueError, match="version"):
         P.load_train_checkpoint(path, b, ob, sb, {"seeds": [0, 1]})
+
+
+def test_manifest_of_cg_training_data_pins_the_solutions(tmp_path):
+    """The manifest of (r, e) pairs from plain-CG solutions carries the
+    phantom seeds and a hash of every solution: the same data give the same
+    manifest, and a checkpoint refuses data whose solutions differ."""
+    gen = torch.Generator().manual_seed(4)
+    pairs = [(torch.randn(6, 6, 6, dtype=torch.complex64, generator=gen),
+              torch.randn(6, 6, 6, dtype=torch.complex64, generator=gen)) for _ in range(3)]
+    m = mri.training_manifest(pairs, seed=10, rtol=1e-6)
+    assert m == mri.training_manifest([(r.clone(), e.clone()) for r, e in pairs], seed=10, rtol=1e-6)
+    assert m["phantom_seeds"] == [10, 11, 12] and len(set(m["solution_sha256"])) == 3
+    changed = list(pairs)
+    e = pairs[1][1].clone()
+    e[0, 0, 0] += 1e-6
+    changed[1] = (pairs[1][0], e)
+    other = mri.training_manifest(changed, seed=10, rtol=1e-6)
+    assert other["solution_sha256"][1] != m["solution_sha256"][1] and other["solution_sha256"][0] == m["solution_sha256"][0]
+    path = str(tmp_path / "train.ckpt")
+    a, oa, sa = _setup(0)
+    P.save_train_checkpoint(path, a, oa, sa, 2, [], m)
+    b, ob, sb = _setup(0)
+    assert P.load_train_checkpoint(path, b, ob, sb, m)[0] == 2
+    with pytest.raises(ValueError, match="another training run"):
+        P.load_train_checkpoint(path, b, ob, sb, other)

@@ -30,6 +30,8 @@ __all__ = [
     "random_error_field",
     "shell_field",
     "training_batch",
+    "cg_solution_pairs",
+    "training_manifest",
     "power_method",
     "SenseNormal",
 ]
@@ -157,6 +159,21 @@ def cg_solution_pairs(A, n: int, count: int, seed: int = 0, rtol: float = 1e-6, 
         e, _ = alg.cg_solve(A, r, rtol=rtol, max_iters=max_iters)
         pairs.append((r, e))
     return pairs
+
+
+def training_manifest(pairs, seed: int = 0, rtol: float = 1e-6, noise: float = 0.05) -> dict:
+    """Manifest of :func:`cg_solution_pairs` training data for preconditioner
+    checkpoints (``CNNPreconditioner.fit(..., manifest=...)``): the phantom
+    seeds, the solver tolerance, the noise level and the SHA-256 of every CG
+    solution's bytes, so that a resumed training refuses data that differ
+    from what the checkpoint was trained on (other seeds, another operator,
+    another solver result)."""
+    import hashlib
+
+    sums = [hashlib.sha256(e.detach().to("cpu").contiguous().numpy().tobytes()).hexdigest() for _, e in pairs]
+    return {"source": "seeded 10-ellipsoid phantoms (+ white noise) solved by plain CG",
+            "phantom_seeds": [seed + i for i in range(len(pairs))], "rtol": rtol, "noise": noise,
+            "solution_sha256": sums}
 
 
 def power_method(A, v: Tensor, iters: int = 30) -> float:
