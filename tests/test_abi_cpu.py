@@ -323,3 +323,18 @@ def test_adjoint_scratch_layout_of_the_block_path(ndim, nbatch, entries, ncg, va
     assert _ext.lib().tlgb_interp_adjoint_scratch_size(ctypes.byref(d), ctypes.byref(info), ctypes.byref(sb)) == 0
     want = up(parts * ncg * 64 * 2 * entries * 4) + up(ncg * 4) + (ncg * npts * 64 if values_copy else 0)
     assert sb.value == want
+
+
+def test_cg_info_record_is_valid_json():
+    """The per-solve record: plain numbers and flags, non-finite residuals as
+    null, the history only on request."""
+    import json
+
+    from torchlinops_gb300.alg import CGInfo
+
+    info = CGInfo(iters=5, converged=True, rel_residual=1e-5, true_rel_residual=float("nan"), seconds=0.25,
+                  restarts=1, history=[1.0, 0.1, float("inf")])
+    rec = info.record(history=True)
+    assert json.loads(json.dumps(rec, allow_nan=False)) == rec
+    assert rec["true_rel_residual"] is None and rec["history"] == [1.0, 0.1, None]
+    assert rec["iters"] == 5 and rec["restarts"] == 1 and "history" not in info.record()

@@ -142,6 +142,8 @@ def conjugate_gradients(
 
 @dataclass
 class CGInfo:
+    """What one ``cg_solve`` did; ``record()`` gives it as a JSON-ready dict."""
+
     iters: int = 0
     converged: bool = False
     rel_residual: float = float("nan")  # recursive |r| / |b|
@@ -150,6 +152,19 @@ class CGInfo:
     fallback: bool = False
     restarts: int = 0  # continuations because the true residual was above rtol
     history: list = field(default_factory=list)
+
+    def record(self, history: bool = False) -> dict:
+        """The solve as plain numbers and flags (non-finite residuals as None,
+        so the record stays valid JSON); the residual history on request."""
+        def num(v):
+            return float(v) if math.isfinite(v) else None
+
+        out = {"iters": int(self.iters), "converged": bool(self.converged), "seconds": float(self.seconds),
+               "rel_residual": num(self.rel_residual), "true_rel_residual": num(self.true_rel_residual),
+               "fallback": bool(self.fallback), "restarts": int(self.restarts)}
+        if history:
+            out["history"] = [num(float(h)) for h in self.history]
+        return out
 
 
 def cg_solve(
